@@ -1,0 +1,175 @@
+/*
+ * swpc_gpu.h -- C ABI of the GB300-native swpc_3d time-stepping library.
+ *
+ * This ABI replaces the zero-argument step routines that swpc_3d's driver
+ * loop calls (src/swpc_3d/main.f90:119-139) and the module arrays they
+ * communicate through (src/swpc_3d/m_global.f90:34-41, 86, 93-98).  A host
+ * that keeps the reference's set-up chain (m_global / m_medium / m_source /
+ * m_wav / m_snap, main.f90:64-78) hands the prepared arrays to this library
+ * once, then calls swpc_gpu_run() in place of the loop.  Every entry point
+ * returns 0 on success or a negative code (SWPC_E_*); the message of the
+ * last failure is available from swpc_gpu_last_error().  Nothing throws
+ * across the ABI and nothing calls exit().
+ *
+ * Array conventions (all host pointers; every call copies):
+ *   3-D medium arrays use the reference's Fortran layout A(k,i,j), k fastest,
+ *   with the 3-cell halo k in [-2,nz+3], i in [-2,nx+3], j in [-2,ny+3]
+ *   (m_global.f90:295-300 for one rank): (nz+6)*(nx+6)*(ny+6) floats.
+ *   2-D maps M(i,j) use i in [-2,nx+3], j in [-2,ny+3]: (nx+6)*(ny+6) ints.
+ *   Grid indices (sources, stations, snapshot planes) are the reference's
+ *   1-based i, j, k.
+ */
+#ifndef SWPC_GPU_H
+#define SWPC_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct swpc_sim swpc_sim;
+
+enum {
+    SWPC_OK = 0,
+    SWPC_E_ARG = -1,       /* invalid argument or unsupported option */
+    SWPC_E_CUDA = -2,      /* CUDA runtime failure (message has the CUDA error) */
+    SWPC_E_NOMEM = -3,     /* device allocation failed or exceeds the budget */
+    SWPC_E_STATE = -4,     /* call out of order (e.g. run before upload) */
+    SWPC_E_DIVERGED = -5,  /* max |V| * UC > 1e5 or NaN (m_report.f90:142-151) */
+    SWPC_E_IO = -6,        /* file could not be read or written */
+    SWPC_E_TIMEOUT = -7    /* a bounded device wait gave up */
+};
+
+enum { SWPC_ABC_PML = 0, SWPC_ABC_CERJAN = 1 };
+
+/* Storage precision of the memory variables and medium coefficients.
+ * Arithmetic is FP32 in every mode. */
+enum { SWPC_STORE_FP32 = 0, SWPC_STORE_FP16 = 1, SWPC_STORE_BF16 = 2 };
+
+/* Receiver outputs (m_wav.f90:31-34) */
+enum { SWPC_WAV_V = 1, SWPC_WAV_U = 2, SWPC_WAV_STRESS = 4, SWPC_WAV_STRAIN = 8 };
+
+/* Snapshot kinds (m_snap.f90:105-119); the xy section only in this version */
+enum { SWPC_SNAP_XY_V = 1, SWPC_SNAP_XY_U = 2 };
+
+/* Source time functions (m_fdtool.f90:472-497) */
+enum { SWPC_STF_BOXCAR = 0, SWPC_STF_TRIANGLE = 1, SWPC_STF_HERRMANN = 2,
+       SWPC_STF_KUPPER = 3, SWPC_STF_COSINE = 4, SWPC_STF_TEXP = 5 };
+
+typedef struct swpc_dims {
+    int nx, ny, nz;      /* global grid (m_global.f90:52) */
+    int nt;              /* number of time steps (sizes the receiver buffers) */
+    int na;              /* absorber thickness in cells */
+    int nm;              /* Zener bodies; must be 3 (m_global.f90:31) */
+    int abc_type;        /* SWPC_ABC_PML or SWPC_ABC_CERJAN */
+    int store;           /* SWPC_STORE_* */
+    double dx, dy, dz;   /* grid spacing [km] (real(MP) in m_global.f90:54) */
+    double dt;           /* time step [s] */
+    double xbeg, ybeg, zbeg, tbeg;
+    double fcut;         /* PML a0 = pi * fcut (m_absorb_p.f90:554; fcut from m_source.f90:184-188) */
+    double M0;           /* total moment (m_source.f90:190-198) */
+    double UC;           /* unit conversion (m_global.f90:29; x1e3 in body-force mode) */
+    int ntdec_r;         /* divergence-check interval (m_report.f90:134); 0 = off */
+    int reserved[7];
+} swpc_dims;
+
+/* Create a simulation and allocate its device state on the current CUDA
+ * device.  Replaces kernel__setup's memory_allocate (m_kernel.f90:376-400)
+ * and absorb_p__setup's ADE allocation (m_absorb_p.f90:98-116). */
+int swpc_gpu_create(const swpc_dims* dims, swpc_sim** out);
+
+/* Device bytes swpc_gpu_create() would allocate for these dims (no GPU call). */
+long long swpc_gpu_required_bytes(const swpc_dims* dims);
+
+/* Upload the prepared medium: rho, lam, mu (relaxed moduli) and the tau-method
+ * ratios taup, taus after medium__setup (m_medium.f90:192-229), the surface
+ * maps of surface_detection (m_medium.f90:339-394), and the nm relaxation
+ * times ts (m_fdtool.f90:691-727).  The library derives the Zener
+ * coefficients (m_kernel.f90:58-67) and the PML or Cerjan profiles
+ * (m_absorb_p.f90:74-93, m_absorb_c.f90:27-111) in FP64 here. */
+int swpc_gpu_upload_medium(swpc_sim* sim, const float* rho, const float* lam, const float* mu,
+                           const float* taup, const float* taus,
+                           const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot,
+                           const int* kob_top, const int* kob_bot, const double* ts);
+
+/* Sources (replaces source__stressglut / source__bodyforce state,
+ * m_source.f90:26-36).  ijk: 3n grid indices.  mo: n normalised moments
+ * (mo/M0).  mij: 6n components xx yy zz yz xz xy.  fxyz: 3n normalised body
+ * forces.  prm: 2n (start time, rise time).  bf_mode selects body force. */
+int swpc_gpu_set_sources(swpc_sim* sim, int n, const int* ijk, const double* mo, const double* mij,
+                         const double* fxyz, const double* prm, int stftype, int bf_mode);
+
+/* Receivers (m_wav.f90:54-139): n stations at ijk (3n), sampled every
+ * ntdec_w steps; flags is a mask of SWPC_WAV_*. */
+int swpc_gpu_set_receivers(swpc_sim* sim, int n, const int* ijk, int ntdec_w, int flags);
+
+/* xy-section snapshot (m_snap.f90:95-160, 1587-1653, 1963-2025): plane k0,
+ * decimation idec/jdec, every ntdec_s steps; kinds is a mask of SWPC_SNAP_*. */
+int swpc_gpu_set_snapshot(swpc_sim* sim, int kinds, int k0, int idec, int jdec, int ntdec_s);
+
+/* One time step it (main.f90:120-138 minus host I/O). */
+int swpc_gpu_step(swpc_sim* sim, int it);
+
+/* Steps it0..it1 inclusive, replayed through a captured CUDA graph. */
+int swpc_gpu_run(swpc_sim* sim, int it0, int it1);
+
+/* Block until the simulation's stream is idle; checks divergence. */
+int swpc_gpu_sync(swpc_sim* sim);
+
+/* Receiver traces, Fortran order (ntw, ncmp, nst); kind is one SWPC_WAV_*
+ * bit; ncmp = 3 for V/U, 6 for stress/strain (m_wav.f90:105-123). */
+int swpc_gpu_fetch_waveforms(swpc_sim* sim, int kind, float* out);
+
+/* Snapshot frame `frame` (0-based) of one kind: (nxs, nys, 3) Fortran order. */
+int swpc_gpu_fetch_snapshot(swpc_sim* sim, int kind, int frame, float* out);
+
+/* Number of samples per trace and snapshot geometry. */
+int swpc_gpu_query(swpc_sim* sim, int* ntw, int* nst, int* nxs, int* nys, int* nframes);
+
+/* Max |V| at kob+1 (kernel__vmax, m_kernel.f90:350-374) for the latest
+ * report step, already multiplied by UC * M0 as the progress line prints it. */
+int swpc_gpu_vmax(swpc_sim* sim, float out[3]);
+
+/* One state field over the physical grid, Fortran (nz, nx, ny) order, as
+ * double: which = 0..8 for Vx Vy Vz Sxx Syy Szz Syz Sxz Sxy. */
+int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out);
+
+/* Optional per-kernel timing with CUDA events on the simulation's stream:
+ * enable = 1 records every launch of the interior and PML kernels (graph
+ * replay is bypassed while enabled).  ms[0..5] = accumulated milliseconds of
+ * stress-interior, velocity-interior, stress-PML, velocity-PML, taps,
+ * sources; launches[0..5] the matching counts. */
+int swpc_gpu_profile(swpc_sim* sim, int enable);
+int swpc_gpu_profile_read(swpc_sim* sim, double* ms, long long* launches);
+
+/* The cudaStream_t the simulation launches on (as void*). */
+void* swpc_gpu_stream(swpc_sim* sim);
+
+/* Number of this library's kernels launched since creation. */
+long long swpc_gpu_launch_count(swpc_sim* sim);
+
+int swpc_gpu_destroy(swpc_sim* sim);
+
+/* Copy the last error message into buf; returns its length. */
+int swpc_gpu_last_error(char* buf, size_t n);
+
+/* ------------------------------------------------------------------------
+ * Host driver layer: reads the reference's input files and performs the
+ * reference's host-side set-up (m_global, m_medium, m_source, m_wav, m_snap
+ * set-up routines) in FP64, then creates and uploads the simulation.
+ * ---------------------------------------------------------------------- */
+
+/* Parse input.inf (and the files it names) and return a ready simulation.
+ * Relative file names in input.inf are resolved against the directory of
+ * inf_path. */
+int swpc_host_prepare(const char* inf_path, swpc_sim** out);
+
+/* Write the receiver traces as SAC files named
+ * odir/wav/<title>.3d.<station>.<cmp>.sac (m_wav.f90:782-792). */
+int swpc_host_write_sac(swpc_sim* sim, const char* odir);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWPC_GPU_H */

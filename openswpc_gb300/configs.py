@@ -1,0 +1,214 @@
+"""Synthetic swpc_3d inputs with the shapes of the benchmark workloads.
+
+Every generator writes the same file set the reference reads -- an
+``input.inf`` (key = value, src/shared/m_readini.f90), a layered-model table
+(``fn_lhm``, src/swpc_3d/m_vmodel_lhm.f90:78-89), a source-grid file
+(``fn_stf``, src/swpc_3d/m_source.f90:468-700) and an ``xy`` station file
+(src/swpc_3d/m_wav.f90:141-271) -- so the same directory can be handed to
+the GPU driver, to the Python front end or to the CPU oracle.  All random
+choices come from ``numpy.random.default_rng(seed)``.
+"""
+import os
+import numpy as np
+
+DEFAULT_SEED = 20261203
+
+
+def _fmt(v):
+    if isinstance(v, bool):
+        return ".true." if v else ".false."
+    if isinstance(v, str):
+        return "'%s'" % v
+    if isinstance(v, float):
+        return repr(v)
+    return str(v)
+
+
+def write_inf(path, keys):
+    with open(path, "w") as f:
+        f.write("!! swpc_3d input file (synthetic workload)\n")
+        for k, v in keys.items():
+            f.write("  %-16s = %s\n" % (k, _fmt(v)))
+
+
+def write_lhm(path, rows):
+    with open(path, "w") as f:
+        f.write("# depth  rho(g/cm^3)  vp(km/s)  vs(km/s)  Qp  Qs\n")
+        for r in rows:
+            f.write("  " + "  ".join("%.6g" % x for x in r) + "\n")
+
+
+def base_keys(**kw):
+    keys = dict(
+        title="swpc", odir="./out", ntdec_r=50, strict_mode=False,
+        nproc_x=1, nproc_y=1, nx=128, ny=128, nz=64, nt=1000,
+        dx=0.5, dy=0.5, dz=0.5, dt=0.02, vcut=0.0,
+        xbeg=-32.0, ybeg=-32.0, zbeg=-1.5, tbeg=0.0,
+        clon=139.7604, clat=35.7182, phi=0.0,
+        fq_min=0.05, fq_max=5.0, fq_ref=1.0,
+        snp_format="native", xy_v_sw=False, z0_xy=0.25, ntdec_s=100, idec=1, jdec=1, kdec=1,
+        sw_wav_v=True, sw_wav_u=False, sw_wav_stress=False, sw_wav_strain=False,
+        ntdec_w=1, st_format="xy", fn_stloc="stations.xy", wav_format="sac", ntdec_w_prg=0,
+        stf_format="xym0dc", stftype="kupper", fn_stf="source.dat", sdep_fit="asis",
+        bf_mode=False, pw_mode=False, green_mode=False,
+        abc_type="pml", na=20, stabilize_pml=False,
+        vmodel_type="lhm", is_ocean=False, topo_flatten=False, munk_profile=False, earth_flattening=False,
+        fn_lhm="lhm.dat", stopwatch_mode=False, benchmark_mode=False,
+    )
+    keys.update(kw)
+    # Fortran-style component keys (xy_v%sw) cannot be Python identifiers
+    out = {}
+    for k, v in keys.items():
+        if k.endswith("_sw"):
+            k = k[:-3] + "%sw"
+        out[k] = v
+    return out
+
+
+def double_couple(rng):
+    strike = float(rng.uniform(0.0, 360.0))
+    dip = float(rng.uniform(0.0, 90.0))
+    rake = float(rng.uniform(-180.0, 180.0))
+    return strike, dip, rake
+
+
+def write_plain_small(d, seed=DEFAULT_SEED, nt=1000, **over):
+    """Plain method, small, CPU-runnable: 128x128x64, dx = 0.5 km, dt = 0.02 s,
+    two-layer viscoelastic medium, free surface, 20-point PML, one double
+    couple at 10 km depth, 16 surface receivers on a 4x4 lattice."""
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    strike, dip, rake = double_couple(rng)
+    keys = base_keys(nt=nt, **over)
+    write_inf(os.path.join(d, "input.inf"), keys)
+    write_lhm(os.path.join(d, "lhm.dat"), [(0, 2.7, 5.5, 3.2, 200, 100), (4, 2.9, 6.5, 3.7, 600, 300)])
+    with open(os.path.join(d, "source.dat"), "w") as f:
+        f.write("# x y z tbeg trise mo strike dip rake\n")
+        f.write("  0.0 0.0 10.0 0.0 1.0 1.0e16 %.4f %.4f %.4f\n" % (strike, dip, rake))
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        f.write("# x y z name zsw\n")
+        n = 0
+        for y in (-12.0, -4.0, 4.0, 12.0):
+            for x in (-12.0, -4.0, 4.0, 12.0):
+                n += 1
+                f.write("  %.3f %.3f 0.0 ST%02d fsb\n" % (x, y, n))
+    return os.path.join(d, "input.inf")
+
+
+def write_layered(d, nx, ny, nz, seed, nt=1500, dx=0.5, dt=0.02, n_station=8, body_force=None, **over):
+    """One member of the batched many-instance workload: a seeded 3-5 layer
+    medium (Vp 4.5-7.5 km/s sorted with depth, Vs = Vp/1.73,
+    rho = 1.74 Vp^0.25, Qp = 600, Qs = 300), a single force or a double
+    couple, and receivers at the free surface."""
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    nlay = int(rng.integers(3, 6))
+    zmax = nz * dx
+    depths = np.sort(rng.uniform(0.0, 0.7 * zmax, nlay))
+    depths[0] = 0.0
+    vps = np.sort(rng.uniform(4.5, 7.5, nlay))
+    rows = [(float(z), float(1.74 * vp ** 0.25), float(vp), float(vp / 1.73), 600.0, 300.0) for z, vp in zip(depths, vps)]
+    if body_force is None:
+        body_force = bool(rng.integers(0, 2))
+    xbeg, ybeg, zbeg = -nx * dx / 2, -ny * dx / 2, -1.5 * dx / 0.5 * 0.5
+    keys = base_keys(nx=nx, ny=ny, nz=nz, nt=nt, dx=dx, dy=dx, dz=dx, dt=dt, xbeg=xbeg, ybeg=ybeg,
+                     zbeg=-3 * dx, bf_mode=body_force, stf_format="xy" if body_force else "xym0dc", **over)
+    write_inf(os.path.join(d, "input.inf"), keys)
+    write_lhm(os.path.join(d, "lhm.dat"), rows)
+    margin = (keys["na"] + 4) * dx
+    sx = float(rng.uniform(xbeg + margin, -xbeg - margin))
+    sy = float(rng.uniform(ybeg + margin, -ybeg - margin))
+    sz = float(rng.uniform(3 * dx, zmax - (keys["na"] + 6) * dx))
+    with open(os.path.join(d, "source.dat"), "w") as f:
+        if body_force:
+            v = rng.normal(size=3)
+            v /= np.linalg.norm(v)
+            f.write("  %.4f %.4f %.4f 0.0 1.0 %.6e %.6e %.6e\n" % (sx, sy, sz, v[0] * 1e15, v[1] * 1e15, v[2] * 1e15))
+        else:
+            s, dp, r = double_couple(rng)
+            f.write("  %.4f %.4f %.4f 0.0 1.0 1.0e16 %.4f %.4f %.4f\n" % (sx, sy, sz, s, dp, r))
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        for n in range(n_station):
+            x = float(rng.uniform(xbeg + margin, -xbeg - margin))
+            y = float(rng.uniform(ybeg + margin, -ybeg - margin))
+            f.write("  %.4f %.4f 0.0 R%03d fsb\n" % (x, y, n))
+    return os.path.join(d, "input.inf")
+
+
+def write_uniform(d, nx=64, ny=64, nz=64, nt=100, dx=0.5, dt=0.02, vp=6.0, vs=3.5, rho=2.8, q=1e6,
+                  source="0.0 0.0 0.0", stations=(("0.0", "0.0", "0.0", "C"),), bf=None, **over):
+    """Uniform whole-space medium (no air layer), used by the analytic and
+    reciprocity tests."""
+    os.makedirs(d, exist_ok=True)
+    keys = base_keys(nx=nx, ny=ny, nz=nz, nt=nt, dx=dx, dy=dx, dz=dx, dt=dt,
+                     xbeg=-nx * dx / 2, ybeg=-ny * dx / 2, zbeg=-nz * dx / 2,
+                     vmodel_type="uni", vp0=vp, vs0=vs, rho0=rho, qp0=q, qs0=q, topo0=-1e9, **over)
+    if bf is not None:
+        keys["bf_mode"] = True
+        keys["stf_format"] = "xy"
+    write_inf(os.path.join(d, "input.inf"), keys)
+    with open(os.path.join(d, "source.dat"), "w") as f:
+        if bf is not None:
+            f.write("  %s 0.0 1.0 %g %g %g\n" % (source, bf[0], bf[1], bf[2]))
+        else:
+            f.write("  %s 0.0 1.0 1.0e16 0 0 0 0 0 1\n" % source)
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        for x, y, z, nm in stations:
+            f.write("  %s %s %s %s dep\n" % (x, y, z, nm))
+    return os.path.join(d, "input.inf")
+
+
+def gradient_random_medium(nx, ny, nz, dx, zbeg, seed=DEFAULT_SEED, a=5.0, eps=0.05, na=20, qp=600.0, qs=300.0):
+    """Large single-source workload medium over the halo grid, Fortran (k,i,j)
+    order flattened as (ny+6, nx+6, nz+6): a 1-D gradient Vp = 5 -> 7 km/s
+    over depth, Vs = Vp/1.73, rho = 1.74 Vp^0.25, times (1 + xi) with xi an
+    exponential von Karman field (correlation length ``a`` km, rms ``eps``)
+    made by the spectral method (white noise -> FFT -> sqrt(PSDF) -> IFFT ->
+    de-mean -> rescale), applied per point with rho x (1 + 0.8 xi)
+    (src/swpc_3d/m_vmodel_lhm_rmed.f90:187-206).  Air above z = 0.
+
+    Returns float32 arrays rho, lam, mu, qp, qs of shape (ny+6, nx+6, nz+6).
+    The field is generated on a coarse lattice and replicated periodically
+    (src/shared/m_rdrmed.f90:73-134 wraps its field the same way), which
+    keeps set-up memory bounded for very large grids.
+    """
+    rng = np.random.default_rng(seed)
+    nc = [min(n, 256) for n in (nx, ny, nz)]
+    kx = np.fft.fftfreq(nc[0], d=dx) * 2 * np.pi
+    ky = np.fft.fftfreq(nc[1], d=dx) * 2 * np.pi
+    kz = np.fft.rfftfreq(nc[2], d=dx) * 2 * np.pi
+    K2 = kx[:, None, None] ** 2 + ky[None, :, None] ** 2 + kz[None, None, :] ** 2
+    psdf = 8 * np.pi * eps ** 2 * a ** 3 / (1 + K2 * a * a) ** 2  # exponential ACF
+    w = rng.standard_normal(nc)
+    f = np.fft.irfftn(np.fft.rfftn(w) * np.sqrt(psdf), s=nc)
+    f -= f.mean()
+    f *= eps / f.std()
+    f = f.astype(np.float32)  # (x, y, z)
+    ii = (np.arange(-2, nx + 4) - 1) % nc[0]
+    jj = (np.arange(-2, ny + 4) - 1) % nc[1]
+    kk = (np.arange(-2, nz + 4) - 1) % nc[2]
+    z = (zbeg + (np.arange(-2, nz + 4) - 0.5) * dx).astype(np.float32)
+    zmax = zbeg + nz * dx
+    vp0 = (5.0 + 2.0 * np.clip(z, 0, None) / zmax).astype(np.float32)
+    shape = (ny + 6, nx + 6, nz + 6)
+    rho = np.empty(shape, np.float32)
+    lam = np.empty(shape, np.float32)
+    mu = np.empty(shape, np.float32)
+    fx = f[ii]  # (nx+6, nyc, nzc)
+    for jo, j in enumerate(jj):
+        xi = fx[:, j, :][:, kk]  # (nx+6, nz+6)
+        vp = vp0[None, :] * (1 + xi)
+        vs = vp / 1.73
+        r = (1.74 * vp0[None, :] ** 0.25) * (1 + 0.8 * xi)
+        air = (z < 0)[None, :]
+        vp = np.where(air, 0.0, vp)
+        vs = np.where(air, 0.0, vs)
+        r = np.where(air, 0.001, r)
+        rho[jo] = r
+        mu[jo] = r * vs * vs
+        lam[jo] = r * (vp * vp - 2 * vs * vs)
+    qpa = np.where(z < 0, 10.0, qp).astype(np.float32)
+    qsa = np.where(z < 0, 10.0, qs).astype(np.float32)
+    qpv = np.broadcast_to(qpa[None, None, :], shape)
+    qsv = np.broadcast_to(qsa[None, None, :], shape)
+    return rho, lam, mu, qpv, qsv

@@ -1,0 +1,858 @@
+// kernels.cuh -- sm_103a kernels of the swpc_3d time step.
+//
+// Device layout (see Geo): every 3-D quantity is a group of nf fields stored
+// row-interleaved, [kz][jy][f][x], x fastest, with a padded row pitch.  One
+// base address per (kz, jy) row then reaches every field of the group through
+// immediate offsets f*pitch, and each warp access along x is one coalesced
+// 128-byte line.  Groups: V (Vx Vy Vz), S (Sxx Syy Szz Syz Sxz Sxy), M (rho
+// lam mu taup taus).  The memory variables R live only on the viscoelastic
+// interior box (18 fields, [kz][jy'][f][x']); the 18 ADE auxiliaries live
+// only on the five PML boxes of the absorbing shell.
+//
+// Ghost cells around the physical grid are zero and never written: with one
+// domain the reference's halo exchange (m_global.f90:391-607) only ever
+// copies zeros into them.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace swpc {
+
+constexpr int HYT = 3;   // rows above jy = 0
+constexpr int HZT = 3;   // planes above kz = 0
+constexpr int TBX = 32;  // tile width (one warp)
+constexpr int TBY = 8;   // tile height of the interior sweep kernels
+constexpr int NM = 3;    // Zener bodies (m_global.f90:31)
+
+struct Geo {
+    int nx, ny, nz, na;
+    int hx;     // left x halo, chosen so the interior box starts on a 128-byte boundary
+    int pitch;  // floats per row
+    int nyp;    // rows per plane
+    int nzp;    // planes
+};
+
+__host__ __device__ __forceinline__ size_t goff(const Geo& g, int nf, int f, int ix, int jy, int kz) {
+    return ((size_t)((kz + HZT) * g.nyp + (jy + HYT)) * nf + f) * (size_t)g.pitch + (size_t)(ix + g.hx);
+}
+
+// storage conversion for the memory variables / medium (precision form)
+template <class T> struct St;
+template <> struct St<float> {
+    static __device__ __forceinline__ float ld(const float* p) { return *p; }
+    static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+};
+template <> struct St<__half> {
+    static __device__ __forceinline__ float ld(const __half* p) { return __half2float(*p); }
+    static __device__ __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+};
+template <> struct St<__nv_bfloat16> {
+    static __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+};
+
+struct Coef {
+    float e4x0, e4x1, e4y0, e4y1, e4z0, e4z1;  // 4th order: 9/8/d, 1/24/d
+    float e2x, e2y, e2z;                       // 2nd order near surfaces: 1/d, 0
+    float c1[NM], c2[NM], d1[NM], d2;          // Zener (m_kernel.f90:58-67)
+    float dt;
+};
+
+// Interior (viscoelastic, 4th-order) sweep arguments.
+struct ZArgs {
+    Geo g;
+    float* V;
+    float* S;
+    const float* M;
+    void* R;           // memory variables, storage type per template
+    const int4* band;  // per interior column: kfs_top, kfs_bot, kob_top, kob_bot (1-based k)
+    int x0, y0, nxi, nyi;  // interior box (0-based origin, extent)
+    int kz_end;            // interior planes [0, kz_end)
+    int kchunk;            // planes per block in z
+    int rpitch;            // R row pitch (elements)
+    const float* cer;      // Cerjan profiles (null for PML): xc xb yc yb zc zb, each padded
+    int cer_off[6];
+    Coef c;
+};
+
+// 2nd-order band test of m_kernel.f90:103-111 / 188-196: inside a free-surface
+// or ocean-bottom band (product >= 0, Fortran sign(1,0) = +1) the stencil is
+// 2nd order.
+__device__ __forceinline__ bool in_band(int k, int4 b) {
+    int a = (k - b.x) * (b.y - k);
+    int c = (k - b.z) * (b.w - k);
+    return max(a, c) >= 0;
+}
+
+// Halo cells of a (TBX+4) x (TBY+4) plane tile without its corners:
+// two full rows above and below (x in [2, 34)) plus two cells left and right
+// of every middle row.  Returns the tile coordinate of halo index h.
+__device__ __forceinline__ void halo_xy(int h, int& lx, int& ly) {
+    if (h < 4 * TBX) {
+        int r = h / TBX;  // 0,1 top; 2,3 bottom
+        lx = 2 + (h - r * TBX);
+        ly = (r < 2) ? r : (TBY + r);
+    } else {
+        int q = h - 4 * TBX;
+        int c = q & 3;
+        ly = 2 + (q >> 2);
+        lx = (c < 2) ? c : (TBX + c);
+    }
+}
+constexpr int NHALO = 4 * TBX + 4 * TBY;
+
+// ---------------------------------------------------------------------------
+// Interior stress update: m_kernel.f90:142-348 (normal + shear fused).
+// One thread per (i, j) column, sweeping z.  The x/y neighbours of V come from
+// a shared-memory plane tile (double buffered), the z neighbours of the own
+// column from a 4-deep register window, mu from a 3-plane shared ring.
+// ---------------------------------------------------------------------------
+template <class RT>
+__global__ void __launch_bounds__(TBX * TBY, 2) k_stress_interior(const ZArgs a) {
+    __shared__ float sV[2][3][TBY + 4][TBX + 4];
+    __shared__ float sMu[3][TBY + 1][TBX + 1];
+
+    const Geo& g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TBX + tx;
+    const int xt = a.x0 + blockIdx.x * TBX, yt = a.y0 + blockIdx.y * TBY;
+    const int ix = xt + tx, jy = yt + ty;
+    const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
+    const int kz0 = blockIdx.z * a.kchunk;
+    const int kz1 = min(kz0 + a.kchunk, a.kz_end);
+    if (kz0 >= kz1) return;
+
+    const long long planeV = 3LL * g.pitch * g.nyp;
+    const long long planeS = 6LL * g.pitch * g.nyp;
+    const long long planeM = 5LL * g.pitch * g.nyp;
+    const float* __restrict__ V = a.V;
+    const float* __restrict__ M = a.M;
+    float* __restrict__ S = a.S;
+    RT* __restrict__ R = (RT*)a.R;
+    const int P = g.pitch;
+
+    // column base addresses at kz = 0
+    const long long bV = (long long)goff(g, 3, 0, ix, jy, 0);
+    const long long bS = (long long)goff(g, 6, 0, ix, jy, 0);
+    const long long bM = (long long)goff(g, 5, 0, ix, jy, 0);
+    const long long rrow = 18LL * a.rpitch, rplane = rrow * a.nyi;
+    const long long bR = (long long)(jy - a.y0) * rrow + (ix - a.x0);
+
+    int4 band = make_int4(0, -1, 0, -1);
+    if (act) band = a.band[(size_t)(jy - a.y0) * a.nxi + (ix - a.x0)];
+
+    // z window of the own column: vx,vy at k-1..k+2, vz at k-2..k+1
+    float vx[4], vy[4], vz[4];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        vx[q + 1] = V[bV + (kz0 - 1 + q) * planeV];
+        vy[q + 1] = V[bV + P + (kz0 - 1 + q) * planeV];
+        vz[q + 1] = V[bV + 2 * P + (kz0 - 2 + q) * planeV];
+    }
+
+    // mu plane kz0 into ring slot 0
+    int s0 = 0, s1 = 1, s2 = 2;
+    for (int h = tid; h < (TBX + 1) * (TBY + 1); h += TBX * TBY) {
+        int lx = h % (TBX + 1), ly = h / (TBX + 1);
+        sMu[s0][ly][lx] = M[goff(g, 5, 2, xt + lx, yt + ly, kz0)];
+    }
+
+    const float dt = a.c.dt;
+    const float eps = 1.1920928955078125e-07f;  // epsilon(1.0)
+
+    for (int kz = kz0; kz < kz1; ++kz) {
+        const int b = kz & 1;
+        // advance the window
+#pragma unroll
+        for (int q = 0; q < 3; ++q) { vx[q] = vx[q + 1]; vy[q] = vy[q + 1]; vz[q] = vz[q + 1]; }
+        vx[3] = V[bV + (kz + 2) * planeV];
+        vy[3] = V[bV + P + (kz + 2) * planeV];
+        vz[3] = V[bV + 2 * P + (kz + 1) * planeV];
+
+        // per-point streams of this plane (issued before the barrier)
+        float sxx = 0, syy = 0, szz = 0, syz = 0, sxz = 0, sxy = 0, lam = 0, tp = 0, ts = 0;
+        float r[18];
+        const long long oS = bS + kz * planeS, oM = bM + kz * planeM, oR = bR + kz * rplane;
+        if (act) {
+            sxx = S[oS]; syy = S[oS + P]; szz = S[oS + 2 * P];
+            syz = S[oS + 3 * P]; sxz = S[oS + 4 * P]; sxy = S[oS + 5 * P];
+            lam = M[oM + P]; tp = M[oM + 3 * P]; ts = M[oM + 4 * P];
+#pragma unroll
+            for (int f = 0; f < 18; ++f) r[f] = St<RT>::ld(R + oR + (long long)f * a.rpitch);
+        }
+
+        // plane tile of V (center from the window, halo from global)
+        sV[b][0][ty + 2][tx + 2] = vx[1];
+        sV[b][1][ty + 2][tx + 2] = vy[1];
+        sV[b][2][ty + 2][tx + 2] = vz[2];
+        for (int h = tid; h < 3 * NHALO; h += TBX * TBY) {
+            int c = h / NHALO, lx, ly;
+            halo_xy(h - c * NHALO, lx, ly);
+            sV[b][c][ly][lx] = V[goff(g, 3, c, xt - 2 + lx, yt - 2 + ly, kz)];
+        }
+        // mu plane kz+1 into slot s1
+        for (int h = tid; h < (TBX + 1) * (TBY + 1); h += TBX * TBY) {
+            int lx = h % (TBX + 1), ly = h / (TBX + 1);
+            sMu[s1][ly][lx] = M[goff(g, 5, 2, xt + lx, yt + ly, kz + 1)];
+        }
+        __syncthreads();
+
+        if (act) {
+            const int k = kz + 1;  // reference 1-based k
+            const bool nb = in_band(k, band);
+            const float e40x = nb ? a.c.e2x : a.c.e4x0, e41x = nb ? 0.f : a.c.e4x1;
+            const float e40y = nb ? a.c.e2y : a.c.e4y0, e41y = nb ? 0.f : a.c.e4y1;
+            const float e40z = nb ? a.c.e2z : a.c.e4z0, e41z = nb ? 0.f : a.c.e4z1;
+            const int lx = tx + 2, ly = ty + 2;
+            float (*X)[TBX + 4] = sV[b][0];
+            float (*Y)[TBX + 4] = sV[b][1];
+            float (*Z)[TBX + 4] = sV[b][2];
+
+            const float dxVx = (X[ly][lx] - X[ly][lx - 1]) * e40x - (X[ly][lx + 1] - X[ly][lx - 2]) * e41x;
+            const float dyVy = (Y[ly][lx] - Y[ly - 1][lx]) * e40y - (Y[ly + 1][lx] - Y[ly - 2][lx]) * e41y;
+            const float dzVz = (vz[2] - vz[1]) * e40z - (vz[3] - vz[0]) * e41z;
+            const float dxVy_dyVx = (Y[ly][lx + 1] - Y[ly][lx]) * e40x - (Y[ly][lx + 2] - Y[ly][lx - 1]) * e41x
+                                  + (X[ly + 1][lx] - X[ly][lx]) * e40y - (X[ly + 2][lx] - X[ly - 1][lx]) * e41y;
+            const float dxVz_dzVx = (Z[ly][lx + 1] - Z[ly][lx]) * e40x - (Z[ly][lx + 2] - Z[ly][lx - 1]) * e41x
+                                  + (vx[2] - vx[1]) * e40z - (vx[3] - vx[0]) * e41z;
+            const float dyVz_dzVy = (Z[ly + 1][lx] - Z[ly][lx]) * e40y - (Z[ly + 2][lx] - Z[ly - 1][lx]) * e41y
+                                  + (vy[2] - vy[1]) * e40z - (vy[3] - vy[0]) * e41z;
+
+            // mu at (k,k+1) x (i,i+1) x (j,j+1)
+            const float m000 = sMu[s0][ty][tx], m100 = sMu[s1][ty][tx];
+            const float m010 = sMu[s0][ty][tx + 1], m110 = sMu[s1][ty][tx + 1];
+            const float m001 = sMu[s0][ty + 1][tx], m101 = sMu[s1][ty + 1][tx];
+            const float m011 = sMu[s0][ty + 1][tx + 1];
+
+            // normal components (m_kernel.f90:198-238)
+            const float mu2 = 2.f * m000, lam2mu = lam + mu2;
+            const float d3v3 = dxVx + dyVy + dzVz;
+            const float sx = dyVy + dzVz, sy = dxVx + dzVz, sz = dxVx + dyVy;
+            const float A = lam2mu * tp * d3v3;
+            const float Bx = A - mu2 * ts * sx, By = A - mu2 * ts * sy, Bz = A - mu2 * ts * sz;
+            float rxn = 0.f, ryn = 0.f, rzn = 0.f;
+#pragma unroll
+            for (int m = 0; m < NM; ++m) {
+                r[m] = a.c.c1[m] * r[m] - a.c.c2[m] * Bx * dt;
+                r[3 + m] = a.c.c1[m] * r[3 + m] - a.c.c2[m] * By * dt;
+                r[6 + m] = a.c.c1[m] * r[6 + m] - a.c.c2[m] * Bz * dt;
+                rxn += a.c.d1[m] * r[m];
+                ryn += a.c.d1[m] * r[3 + m];
+                rzn += a.c.d1[m] * r[6 + m];
+            }
+            const float tp1 = 1.f + tp * (1.f + a.c.d2), ts1 = 1.f + ts * (1.f + a.c.d2);
+            const float P2 = lam2mu * tp1 * d3v3;
+            sxx += (P2 - mu2 * ts1 * sx + rxn) * dt;
+            syy += (P2 - mu2 * ts1 * sy + ryn) * dt;
+            szz += (P2 - mu2 * ts1 * sz + rzn) * dt;
+
+            // shear components with harmonic means of mu (m_kernel.f90:285-333)
+            const float muxz = 4.f * m000 * m100 * m010 * m110 /
+                               (m000 * m100 * m010 + m000 * m100 * m110 + m000 * m010 * m110 + m100 * m010 * m110 + eps);
+            const float muxy = 4.f * m000 * m010 * m001 * m011 /
+                               (m000 * m010 * m001 + m000 * m010 * m011 + m000 * m001 * m011 + m010 * m001 * m011 + eps);
+            const float muyz = 4.f * m000 * m100 * m001 * m101 /
+                               (m000 * m100 * m001 + m000 * m100 * m101 + m000 * m001 * m101 + m100 * m001 * m101 + eps);
+            float ryzn = 0.f, rxzn = 0.f, rxyn = 0.f;
+            const float qyz = muyz * ts * dyVz_dzVy, qxz = muxz * ts * dxVz_dzVx, qxy = muxy * ts * dxVy_dyVx;
+#pragma unroll
+            for (int m = 0; m < NM; ++m) {
+                r[9 + m] = a.c.c1[m] * r[9 + m] - a.c.c2[m] * qyz * dt;
+                r[12 + m] = a.c.c1[m] * r[12 + m] - a.c.c2[m] * qxz * dt;
+                r[15 + m] = a.c.c1[m] * r[15 + m] - a.c.c2[m] * qxy * dt;
+                ryzn += a.c.d1[m] * r[9 + m];
+                rxzn += a.c.d1[m] * r[12 + m];
+                rxyn += a.c.d1[m] * r[15 + m];
+            }
+            syz += (muyz * ts1 * dyVz_dzVy + ryzn) * dt;
+            sxz += (muxz * ts1 * dxVz_dzVx + rxzn) * dt;
+            sxy += (muxy * ts1 * dxVy_dyVx + rxyn) * dt;
+
+            if (a.cer) {  // Cerjan sponge epilogue (m_absorb_c.f90:113-168)
+                const float gxc = a.cer[a.cer_off[0] + ix], gxb = a.cer[a.cer_off[1] + ix];
+                const float gyc = a.cer[a.cer_off[2] + jy], gyb = a.cer[a.cer_off[3] + jy];
+                const float gzc = a.cer[a.cer_off[4] + kz], gzb = a.cer[a.cer_off[5] + kz];
+                const float gcc = gxc * gyc * gzc;
+                sxx *= gcc; syy *= gcc; szz *= gcc;
+                syz = syz * gxc * gyb * gzb;
+                sxz = sxz * gxb * gyc * gzb;
+                sxy = sxy * gxb * gyb * gzc;
+            }
+            S[oS] = sxx; S[oS + P] = syy; S[oS + 2 * P] = szz;
+            S[oS + 3 * P] = syz; S[oS + 4 * P] = sxz; S[oS + 5 * P] = sxy;
+#pragma unroll
+            for (int f = 0; f < 18; ++f) St<RT>::st(R + oR + (long long)f * a.rpitch, r[f]);
+        }
+        // rotate the mu ring: next iteration needs (kz+1, kz+2)
+        int t = s0; s0 = s1; s1 = s2; s2 = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Interior velocity update: m_kernel.f90:75-140.
+// Plane tile in shared memory: Sxx Syy Sxy Sxz Syz rho (x/y neighbours);
+// register window for Szz (k-1..k+2), Sxz, Syz (k-2..k+1), rho (k, k+1).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TBX * TBY, 2) k_vel_interior(const ZArgs a) {
+    __shared__ float sT[2][6][TBY + 4][TBX + 4];
+    const Geo& g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TBX + tx;
+    const int xt = a.x0 + blockIdx.x * TBX, yt = a.y0 + blockIdx.y * TBY;
+    const int ix = xt + tx, jy = yt + ty;
+    const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
+    const int kz0 = blockIdx.z * a.kchunk;
+    const int kz1 = min(kz0 + a.kchunk, a.kz_end);
+    if (kz0 >= kz1) return;
+
+    const long long planeV = 3LL * g.pitch * g.nyp;
+    const long long planeS = 6LL * g.pitch * g.nyp;
+    const long long planeM = 5LL * g.pitch * g.nyp;
+    float* __restrict__ V = a.V;
+    const float* __restrict__ S = a.S;
+    const float* __restrict__ M = a.M;
+    const int P = g.pitch;
+    const long long bV = (long long)goff(g, 3, 0, ix, jy, 0);
+    const long long bS = (long long)goff(g, 6, 0, ix, jy, 0);
+    const long long bM = (long long)goff(g, 5, 0, ix, jy, 0);
+
+    int4 band = make_int4(0, -1, 0, -1);
+    if (act) band = a.band[(size_t)(jy - a.y0) * a.nxi + (ix - a.x0)];
+
+    float wzz[4], wxz[4], wyz[4], wr[2];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        wzz[q + 1] = S[bS + 2 * P + (kz0 - 1 + q) * planeS];
+        wxz[q + 1] = S[bS + 4 * P + (kz0 - 2 + q) * planeS];
+        wyz[q + 1] = S[bS + 3 * P + (kz0 - 2 + q) * planeS];
+    }
+    wr[1] = M[bM + kz0 * planeM];
+    const float dt = a.c.dt;
+    // shared tile component -> (group, field) for halo loads
+    for (int kz = kz0; kz < kz1; ++kz) {
+        const int b = kz & 1;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) { wzz[q] = wzz[q + 1]; wxz[q] = wxz[q + 1]; wyz[q] = wyz[q + 1]; }
+        wzz[3] = S[bS + 2 * P + (kz + 2) * planeS];
+        wxz[3] = S[bS + 4 * P + (kz + 1) * planeS];
+        wyz[3] = S[bS + 3 * P + (kz + 1) * planeS];
+        wr[0] = wr[1];
+        wr[1] = M[bM + (kz + 1) * planeM];
+        const float cxx = S[bS + kz * planeS], cyy = S[bS + P + kz * planeS], cxy = S[bS + 5 * P + kz * planeS];
+        float vxo = 0, vyo = 0, vzo = 0;
+        const long long oV = bV + kz * planeV;
+        if (act) { vxo = V[oV]; vyo = V[oV + P]; vzo = V[oV + 2 * P]; }
+
+        sT[b][0][ty + 2][tx + 2] = cxx;
+        sT[b][1][ty + 2][tx + 2] = cyy;
+        sT[b][2][ty + 2][tx + 2] = cxy;
+        sT[b][3][ty + 2][tx + 2] = wxz[2];
+        sT[b][4][ty + 2][tx + 2] = wyz[2];
+        sT[b][5][ty + 2][tx + 2] = wr[0];
+        for (int h = tid; h < 6 * NHALO; h += TBX * TBY) {
+            int c = h / NHALO, lx, ly;
+            halo_xy(h - c * NHALO, lx, ly);
+            int gx = xt - 2 + lx, gy = yt - 2 + ly;
+            float v;
+            if (c == 5) v = M[goff(g, 5, 0, gx, gy, kz)];
+            else v = S[goff(g, 6, c < 2 ? c : 7 - c, gx, gy, kz)];  // Sxx Syy Sxy Sxz Syz
+            sT[b][c][ly][lx] = v;
+        }
+        __syncthreads();
+        if (act) {
+            const int k = kz + 1;
+            const bool nb = in_band(k, band);
+            const float e40x = nb ? a.c.e2x : a.c.e4x0, e41x = nb ? 0.f : a.c.e4x1;
+            const float e40y = nb ? a.c.e2y : a.c.e4y0, e41y = nb ? 0.f : a.c.e4y1;
+            const float e40z = nb ? a.c.e2z : a.c.e4z0, e41z = nb ? 0.f : a.c.e4z1;
+            const int lx = tx + 2, ly = ty + 2;
+            float (*XX)[TBX + 4] = sT[b][0];
+            float (*YY)[TBX + 4] = sT[b][1];
+            float (*XY)[TBX + 4] = sT[b][2];
+            float (*XZ)[TBX + 4] = sT[b][3];
+            float (*YZ)[TBX + 4] = sT[b][4];
+            float (*RH)[TBX + 4] = sT[b][5];
+            const float d3Sx3 = (XX[ly][lx + 1] - XX[ly][lx]) * e40x - (XX[ly][lx + 2] - XX[ly][lx - 1]) * e41x
+                              + (XY[ly][lx] - XY[ly - 1][lx]) * e40y - (XY[ly + 1][lx] - XY[ly - 2][lx]) * e41y
+                              + (wxz[2] - wxz[1]) * e40z - (wxz[3] - wxz[0]) * e41z;
+            const float d3Sy3 = (XY[ly][lx] - XY[ly][lx - 1]) * e40x - (XY[ly][lx + 1] - XY[ly][lx - 2]) * e41x
+                              + (YY[ly + 1][lx] - YY[ly][lx]) * e40y - (YY[ly + 2][lx] - YY[ly - 1][lx]) * e41y
+                              + (wyz[2] - wyz[1]) * e40z - (wyz[3] - wyz[0]) * e41z;
+            const float d3Sz3 = (XZ[ly][lx] - XZ[ly][lx - 1]) * e40x - (XZ[ly][lx + 1] - XZ[ly][lx - 2]) * e41x
+                              + (YZ[ly][lx] - YZ[ly - 1][lx]) * e40y - (YZ[ly + 1][lx] - YZ[ly - 2][lx]) * e41y
+                              + (wzz[2] - wzz[1]) * e40z - (wzz[3] - wzz[0]) * e41z;
+            const float r0 = RH[ly][lx];
+            float vx = vxo + 2.f / (r0 + RH[ly][lx + 1]) * d3Sx3 * dt;
+            float vy = vyo + 2.f / (r0 + RH[ly + 1][lx]) * d3Sy3 * dt;
+            float vz = vzo + 2.f / (r0 + wr[1]) * d3Sz3 * dt;
+            if (a.cer) {  // Cerjan sponge epilogue (m_absorb_c.f90:170-198)
+                const float gxc = a.cer[a.cer_off[0] + ix], gxb = a.cer[a.cer_off[1] + ix];
+                const float gyc = a.cer[a.cer_off[2] + jy], gyb = a.cer[a.cer_off[3] + jy];
+                const float gzc = a.cer[a.cer_off[4] + kz], gzb = a.cer[a.cer_off[5] + kz];
+                vx = vx * gxb * gyc * gzc;
+                vy = vy * gxc * gyb * gzc;
+                vz = vz * gxc * gyc * gzb;
+            }
+            V[oV] = vx; V[oV + P] = vy; V[oV + 2 * P] = vz;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PML shell (ADE-CFS, m_absorb_p.f90).  The shell is five boxes; each has its
+// own compact ADE storage [z][y][9][x] for the V-derivative auxiliaries
+// (used by the stress update) and for the S-derivative auxiliaries (used by
+// the velocity update).  One thread per shell point.
+// ---------------------------------------------------------------------------
+struct PmlBox {
+    int x0, y0, z0, nx, ny, nz;
+    int pitch;           // ADE row pitch
+    long long off;       // offset of this box in the ADE buffers (elements)
+    long long first;     // first linear point index of this box
+};
+
+struct PArgs {
+    Geo g;
+    float* V;
+    float* S;
+    const float* M;
+    float* adeV;        // axVx ayVy azVz ayVx azVx axVy azVy axVz ayVz
+    float* adeS;        // axSxx aySxy azSxz axSxy aySyy azSyz axSxz aySyz azSzz
+    const float* prof;  // gxc gxe (4 x nx each, l-major), gyc gye, gzc gze
+    int pxc, pxe, pyc, pye, pzc, pze;  // offsets of each profile (array of 4*n, l fastest)
+    PmlBox box[5];
+    int nbox;
+    long long npts;
+    float r20x, r20y, r20z, dt;
+};
+
+__device__ __forceinline__ int find_box(const PArgs& a, long long p) {
+    int b = 0;
+#pragma unroll
+    for (int q = 1; q < 5; ++q)
+        if (q < a.nbox && p >= a.box[q].first) b = q;
+    return b;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+__global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) {
+    const Geo& g = a.g;
+    const float eps = 1.1920928955078125e-07f;
+    const int P = g.pitch;
+    const size_t rowV = (size_t)3 * P, planeV = rowV * g.nyp;
+    const size_t rowM = (size_t)5 * P;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.npts; p += (long long)gridDim.x * blockDim.x) {
+        const int b = find_box(a, p);
+        const PmlBox& B = a.box[b];
+        long long q = p - B.first;
+        const int lx = (int)(q % B.nx);
+        q /= B.nx;
+        const int ly = (int)(q % B.ny);
+        const int lz = (int)(q / B.ny);
+        const int ix = B.x0 + lx, jy = B.y0 + ly, kz = B.z0 + lz;
+        const size_t oV = goff(g, 3, 0, ix, jy, kz);
+        const size_t oM = goff(g, 5, 0, ix, jy, kz);
+        const size_t oS = goff(g, 6, 0, ix, jy, kz);
+        const size_t oA = (size_t)B.off + ((size_t)(lz * B.ny + ly) * 9) * B.pitch + lx;
+        const float* __restrict__ V = a.V;
+        const float* __restrict__ M = a.M;
+        const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
+        const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
+        const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
+        const float vx = V[oV], vy = V[oV + P], vz = V[oV + 2 * P];
+        // normal part (m_absorb_p.f90:453-474)
+        const float dxVx = (vx - V[oV - 1]) * a.r20x;
+        const float dyVy = (vy - V[oV + P - rowV]) * a.r20y;
+        const float dzVz = (vz - V[oV + 2 * P - planeV]) * a.r20z;
+        const float lamv = M[oM + P], muv = M[oM + 2 * P];
+        const float lam2mu = lamv + 2.f * muv;
+        const float lamR = lam2mu - 2.f * muv;
+        float* A = a.adeV + oA;
+        const int AP = B.pitch;
+        const float aVx = A[0], aVy = A[AP], aVz = A[2 * AP];
+        const float dxa = gxc.x * dxVx + gxc.y * aVx;
+        const float dya = gyc.x * dyVy + gyc.y * aVy;
+        const float dza = gzc.x * dzVz + gzc.y * aVz;
+        float* S = a.S;
+        S[oS] += (lam2mu * dxa + lamR * (dya + dza)) * a.dt;
+        S[oS + P] += (lam2mu * dya + lamR * (dxa + dza)) * a.dt;
+        S[oS + 2 * P] += (lam2mu * dza + lamR * (dxa + dya)) * a.dt;
+        A[0] = gxc.z * aVx + gxc.w * dxVx * a.dt;
+        A[AP] = gyc.z * aVy + gyc.w * dyVy * a.dt;
+        A[2 * AP] = gzc.z * aVz + gzc.w * dzVz * a.dt;
+        // shear part (m_absorb_p.f90:477-518)
+        const float dxVy = (V[oV + P + 1] - vy) * a.r20x;
+        const float dxVz = (V[oV + 2 * P + 1] - vz) * a.r20x;
+        const float dyVx = (V[oV + rowV] - vx) * a.r20y;
+        const float dyVz = (V[oV + 2 * P + rowV] - vz) * a.r20y;
+        const float dzVx = (V[oV + planeV] - vx) * a.r20z;
+        const float dzVy = (V[oV + P + planeV] - vy) * a.r20z;
+        const size_t planeM = rowM * g.nyp;
+        const float m000 = muv, m100 = M[oM + 2 * P + planeM], m010 = M[oM + 2 * P + 1], m110 = M[oM + 2 * P + planeM + 1];
+        const float m001 = M[oM + 2 * P + rowM], m011 = M[oM + 2 * P + rowM + 1], m101 = M[oM + 2 * P + planeM + rowM];
+        const float muxz = 4.f * m000 * m100 * m010 * m110 /
+                           (m000 * m100 * m010 + m000 * m100 * m110 + m000 * m010 * m110 + m100 * m010 * m110 + eps);
+        const float muxy = 4.f * m000 * m010 * m001 * m011 /
+                           (m000 * m010 * m001 + m000 * m010 * m011 + m000 * m001 * m011 + m010 * m001 * m011 + eps);
+        const float muyz = 4.f * m000 * m100 * m001 * m101 /
+                           (m000 * m100 * m001 + m000 * m100 * m101 + m000 * m001 * m101 + m100 * m001 * m101 + eps);
+        const float ayVx = A[3 * AP], azVx = A[4 * AP], axVy = A[5 * AP], azVy = A[6 * AP], axVz = A[7 * AP], ayVz = A[8 * AP];
+        S[oS + 3 * P] += muyz * (gye.x * dyVz + gze.x * dzVy + gye.y * ayVz + gze.y * azVy) * a.dt;
+        S[oS + 4 * P] += muxz * (gxe.x * dxVz + gze.x * dzVx + gxe.y * axVz + gze.y * azVx) * a.dt;
+        S[oS + 5 * P] += muxy * (gxe.x * dxVy + gye.x * dyVx + gxe.y * axVy + gye.y * ayVx) * a.dt;
+        A[3 * AP] = gye.z * ayVx + gye.w * dyVx * a.dt;
+        A[4 * AP] = gze.z * azVx + gze.w * dzVx * a.dt;
+        A[5 * AP] = gxe.z * axVy + gxe.w * dxVy * a.dt;
+        A[6 * AP] = gze.z * azVy + gze.w * dzVy * a.dt;
+        A[7 * AP] = gxe.z * axVz + gxe.w * dxVz * a.dt;
+        A[8 * AP] = gye.z * ayVz + gye.w * dyVz * a.dt;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_vel_pml(const PArgs a) {
+    const Geo& g = a.g;
+    const int P = g.pitch;
+    const size_t rowS = (size_t)6 * P, planeS = rowS * g.nyp;
+    const size_t rowM = (size_t)5 * P, planeM = rowM * g.nyp;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.npts; p += (long long)gridDim.x * blockDim.x) {
+        const int b = find_box(a, p);
+        const PmlBox& B = a.box[b];
+        long long q = p - B.first;
+        const int lx = (int)(q % B.nx);
+        q /= B.nx;
+        const int ly = (int)(q % B.ny);
+        const int lz = (int)(q / B.ny);
+        const int ix = B.x0 + lx, jy = B.y0 + ly, kz = B.z0 + lz;
+        const size_t oV = goff(g, 3, 0, ix, jy, kz);
+        const size_t oM = goff(g, 5, 0, ix, jy, kz);
+        const size_t oS = goff(g, 6, 0, ix, jy, kz);
+        const size_t oA = (size_t)B.off + ((size_t)(lz * B.ny + ly) * 9) * B.pitch + lx;
+        const float* __restrict__ S = a.S;
+        const float* __restrict__ M = a.M;
+        const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
+        const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
+        const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
+        // m_absorb_p.f90:265-305
+        const float sxx = S[oS], syy = S[oS + P], szz = S[oS + 2 * P];
+        const float syz = S[oS + 3 * P], sxz = S[oS + 4 * P], sxy = S[oS + 5 * P];
+        const float dxSxx = (S[oS + 1] - sxx) * a.r20x;
+        const float dySyy = (S[oS + P + rowS] - syy) * a.r20y;
+        const float dzSzz = (S[oS + 2 * P + planeS] - szz) * a.r20z;
+        const float dySyz = (syz - S[oS + 3 * P - rowS]) * a.r20y;
+        const float dzSyz = (syz - S[oS + 3 * P - planeS]) * a.r20z;
+        const float dxSxz = (sxz - S[oS + 4 * P - 1]) * a.r20x;
+        const float dzSxz = (sxz - S[oS + 4 * P - planeS]) * a.r20z;
+        const float dxSxy = (sxy - S[oS + 5 * P - 1]) * a.r20x;
+        const float dySxy = (sxy - S[oS + 5 * P - rowS]) * a.r20y;
+        const float r0 = M[oM];
+        const float bx = 2.f / (r0 + M[oM + 1]);
+        const float by = 2.f / (r0 + M[oM + rowM]);
+        const float bz = 2.f / (r0 + M[oM + planeM]);
+        float* A = a.adeS + oA;
+        const int AP = B.pitch;
+        const float axSxx = A[0], aySxy = A[AP], azSxz = A[2 * AP], axSxy = A[3 * AP], aySyy = A[4 * AP];
+        const float azSyz = A[5 * AP], axSxz = A[6 * AP], aySyz = A[7 * AP], azSzz = A[8 * AP];
+        float* V = a.V;
+        V[oV] += bx * (gxe.x * dxSxx + gyc.x * dySxy + gzc.x * dzSxz + gxe.y * axSxx + gyc.y * aySxy + gzc.y * azSxz) * a.dt;
+        V[oV + P] += by * (gxc.x * dxSxy + gye.x * dySyy + gzc.x * dzSyz + gxc.y * axSxy + gye.y * aySyy + gzc.y * azSyz) * a.dt;
+        V[oV + 2 * P] += bz * (gxc.x * dxSxz + gyc.x * dySyz + gze.x * dzSzz + gxc.y * axSxz + gyc.y * aySyz + gze.y * azSzz) * a.dt;
+        A[0] = gxe.z * axSxx + gxe.w * dxSxx * a.dt;
+        A[AP] = gyc.z * aySxy + gyc.w * dySxy * a.dt;
+        A[2 * AP] = gzc.z * azSxz + gzc.w * dzSxz * a.dt;
+        A[3 * AP] = gxc.z * axSxy + gxc.w * dxSxy * a.dt;
+        A[4 * AP] = gye.z * aySyy + gye.w * dySyy * a.dt;
+        A[5 * AP] = gzc.z * azSyz + gzc.w * dzSyz * a.dt;
+        A[6 * AP] = gxc.z * axSxz + gxc.w * dxSxz * a.dt;
+        A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
+        A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sources, receivers, snapshots, divergence check
+// ---------------------------------------------------------------------------
+
+// m_fdtool.f90:339-497
+__device__ __forceinline__ float momentrate(float t, int stf, float ts, float tr) {
+    const float pi = 3.14159265358979f;
+    switch (stf) {
+    case 0: return (ts <= t && t <= ts + tr) ? 1.f / tr : 0.f;
+    case 1:
+        if (ts <= t && t <= ts + tr / 2) return 4 * (t - ts) / (tr * tr);
+        if (ts + tr / 2 < t && t <= ts + tr) return -4 * (t - ts - tr) / (tr * tr);
+        return 0.f;
+    case 2: {
+        float t1 = ts + tr / 4, t2 = ts + 3 * tr / 4;
+        if (ts <= t && t < t1) return 16 * (t - ts) * (t - ts) / (tr * tr * tr);
+        if (t1 <= t && t < t2) return -2 * (8 * (t * t + tr * ts + ts * ts - t * tr - 2 * t * ts) + tr * tr) / (tr * tr * tr);
+        if (t2 <= t && t <= ts + tr) return 16 * (ts + tr - t) * (ts + tr - t) / (tr * tr * tr);
+        return 0.f;
+    }
+    case 4: return (ts <= t && t <= ts + tr) ? (1 - cosf(2 * pi * (t - ts) / tr)) / tr : 0.f;
+    case 5: {
+        if (ts <= t) { float tt = t - ts; return (2 * pi) * (2 * pi) * tt / (tr * tr) * expf(-2 * pi * tt / tr); }
+        return 0.f;
+    }
+    default: {
+        if (ts <= t && t <= ts + tr) { float s = sinf(pi * (t - ts) / tr); return 3 * pi * s * s * s / (4 * tr); }
+        return 0.f;
+    }
+    }
+}
+
+struct SrcArgs {
+    Geo g;
+    float* V;
+    float* S;
+    const float* M;
+    const int* ijk;      // 3n, 0-based
+    const float* mij;    // 6n (xx yy zz yz xz xy) multiplied by mo
+    const float* fxyz;   // 3n
+    const float* prm;    // 2n
+    int n, stf;
+    float tbeg, dt, dt_dxyz;
+    const int* it;       // device step counter
+};
+
+// Ghost planes in x/y are never stored to: the reference zeroes the ones the
+// stencils read right after injection (m_global.f90:458-488, 569-601).
+__device__ __forceinline__ bool in_xy(const Geo& g, int ix, int jy) { return ix >= 0 && ix < g.nx && jy >= 0 && jy < g.ny; }
+
+// m_source.f90:776-848
+__global__ void k_stressglut(const SrcArgs a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    const int it = *a.it;
+    const float t = a.tbeg + ((float)it - 0.5f) * a.dt;
+    const float st = momentrate(t, a.stf, a.prm[2 * s], a.prm[2 * s + 1]);
+    const float sdrop = st * a.dt_dxyz;
+    const int i = a.ijk[3 * s], j = a.ijk[3 * s + 1], k = a.ijk[3 * s + 2];
+    const float* m = a.mij + 6 * s;
+    const Geo& g = a.g;
+    auto add = [&](int f, int ii, int jj, int kk, float v) {
+        if (in_xy(g, ii, jj)) atomicAdd(a.S + goff(g, 6, f, ii, jj, kk), -v);
+    };
+    add(0, i, j, k, m[0] * sdrop);
+    add(1, i, j, k, m[1] * sdrop);
+    add(2, i, j, k, m[2] * sdrop);
+    const float qyz = m[3] * sdrop / 4, qxz = m[4] * sdrop / 4, qxy = m[5] * sdrop / 4;
+    add(5, i, j, k, qxy); add(5, i, j - 1, k, qxy); add(5, i - 1, j, k, qxy); add(5, i - 1, j - 1, k, qxy);
+    add(4, i, j, k, qxz); add(4, i, j, k - 1, qxz); add(4, i - 1, j, k, qxz); add(4, i - 1, j, k - 1, qxz);
+    add(3, i, j, k, qyz); add(3, i, j, k - 1, qyz); add(3, i, j - 1, k, qyz); add(3, i, j - 1, k - 1, qyz);
+}
+
+// m_source.f90:850-898
+__global__ void k_bodyforce(const SrcArgs a) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    const int it = *a.it;
+    const float st = momentrate(a.tbeg + (float)it * a.dt, a.stf, a.prm[2 * s], a.prm[2 * s + 1]);
+    const int i = a.ijk[3 * s], j = a.ijk[3 * s + 1], k = a.ijk[3 * s + 2];
+    const Geo& g = a.g;
+    const float* f = a.fxyz + 3 * s;
+    auto rho = [&](int ii, int jj, int kk) { return a.M[goff(g, 5, 0, ii, jj, kk)]; };
+    auto add = [&](int c, int ii, int jj, int kk, float b, float fc) {
+        if (in_xy(g, ii, jj)) atomicAdd(a.V + goff(g, 3, c, ii, jj, kk), b * fc * st * a.dt_dxyz / 2);
+    };
+    const float r0 = rho(i, j, k);
+    add(0, i, j, k, 2.f / (r0 + rho(i + 1, j, k)), f[0]);
+    add(0, i - 1, j, k, 2.f / (r0 + rho(i - 1, j, k)), f[0]);
+    add(1, i, j, k, 2.f / (r0 + rho(i, j + 1, k)), f[1]);
+    add(1, i, j - 1, k, 2.f / (r0 + rho(i, j - 1, k)), f[1]);
+    add(2, i, j, k, 2.f / (r0 + rho(i, j, k + 1)), f[2]);
+    add(2, i, j, k - 1, 2.f / (r0 + rho(i, j, k - 1)), f[2]);
+}
+
+struct TapArgs {
+    Geo g;
+    const float* V;
+    const float* S;
+    const int* ijk;   // 3n, 0-based
+    int n, ntw, ntdec_w, flags;
+    float* wav_v;     // (ntw, 3, n)
+    float* wav_u;
+    float* wav_s;     // (ntw, 6, n)
+    float* wav_e;
+    double* acc;      // 9n: ux uy uz exx eyy ezz eyz exz exy (FP64 time integration)
+    float vscale, sscale, escale;  // M0*UC*1e9, M0*UC*1e6, M0*UC*1e-3
+    float dt;
+    float r40x, r40y, r40z, r41x, r41y, r41z;  // 9/8/d, 1/24/d
+    const int* it;
+};
+
+// m_wav.f90:397-625: taps of the *previous* step's velocity/stress
+__global__ void k_taps(const TapArgs a) {
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.n) return;
+    const int it = *a.it;
+    const Geo& g = a.g;
+    const int i = a.ijk[3 * n], j = a.ijk[3 * n + 1], k = a.ijk[3 * n + 2];
+    auto v = [&](int c, int ii, int jj, int kk) { return a.V[goff(g, 3, c, ii, jj, kk)]; };
+    auto s = [&](int f, int ii, int jj, int kk) { return a.S[goff(g, 6, f, ii, jj, kk)]; };
+    double* acc = a.acc + 9 * n;
+    if (a.flags & 2) {  // displacement by time integration (FP64)
+        acc[0] += ((double)v(0, i, j, k) + (double)v(0, i - 1, j, k)) * 0.5 * (double)a.dt;
+        acc[1] += ((double)v(1, i, j, k) + (double)v(1, i, j - 1, k)) * 0.5 * (double)a.dt;
+        acc[2] -= ((double)v(2, i, j, k) + (double)v(2, i, j, k - 1)) * 0.5 * (double)a.dt;
+    }
+    if (a.flags & 8) {  // strain (4th order, m_wav.f90:465-504)
+        auto D = [&](int c, int di, int dj, int dk, int ax, float r40, float r41) {
+            // forward difference along axis ax at offset (di,dj,dk): (f(+1)-f(0))*r40 - (f(+2)-f(-1))*r41
+            int ei = (ax == 0), ej = (ax == 1), ek = (ax == 2);
+            int ii = i + di, jj = j + dj, kk = k + dk;
+            return (v(c, ii + ei, jj + ej, kk + ek) - v(c, ii, jj, kk)) * r40 -
+                   (v(c, ii + 2 * ei, jj + 2 * ej, kk + 2 * ek) - v(c, ii - ei, jj - ej, kk - ek)) * r41;
+        };
+        const float dxVx = D(0, -1, 0, 0, 0, a.r40x, a.r41x);
+        const float dyVy = D(1, 0, -1, 0, 1, a.r40y, a.r41y);
+        const float dzVz = D(2, 0, 0, -1, 2, a.r40z, a.r41z);
+        const float dxVy = (D(1, 0, 0, 0, 0, a.r40x, a.r41x) + D(1, 0, -1, 0, 0, a.r40x, a.r41x) +
+                            D(1, -1, 0, 0, 0, a.r40x, a.r41x) + D(1, -1, -1, 0, 0, a.r40x, a.r41x)) / 4.f;
+        const float dxVz = (D(2, 0, 0, 0, 0, a.r40x, a.r41x) + D(2, 0, 0, -1, 0, a.r40x, a.r41x) +
+                            D(2, -1, 0, 0, 0, a.r40x, a.r41x) + D(2, -1, 0, -1, 0, a.r40x, a.r41x)) / 4.f;
+        const float dyVx = (D(0, 0, 0, 0, 1, a.r40y, a.r41y) + D(0, -1, 0, 0, 1, a.r40y, a.r41y) +
+                            D(0, 0, -1, 0, 1, a.r40y, a.r41y) + D(0, -1, -1, 0, 1, a.r40y, a.r41y)) / 4.f;
+        const float dyVz = (D(2, 0, 0, 0, 1, a.r40y, a.r41y) + D(2, 0, 0, -1, 1, a.r40y, a.r41y) +
+                            D(2, 0, -1, 0, 1, a.r40y, a.r41y) + D(2, 0, -1, -1, 1, a.r40y, a.r41y)) / 4.f;
+        const float dzVx = (D(0, 0, 0, 0, 2, a.r40z, a.r41z) + D(0, -1, 0, 0, 2, a.r40z, a.r41z) +
+                            D(0, 0, 0, -1, 2, a.r40z, a.r41z) + D(0, -1, 0, -1, 2, a.r40z, a.r41z)) / 4.f;
+        const float dzVy = (D(1, 0, 0, 0, 2, a.r40z, a.r41z) + D(1, 0, -1, 0, 2, a.r40z, a.r41z) +
+                            D(1, 0, 0, -1, 2, a.r40z, a.r41z) + D(1, 0, -1, -1, 2, a.r40z, a.r41z)) / 4.f;
+        acc[3] += (double)dxVx * a.dt;
+        acc[4] += (double)dyVy * a.dt;
+        acc[5] += (double)dzVz * a.dt;
+        acc[6] += (double)((dyVz + dzVy) / 2.f) * a.dt;
+        acc[7] += (double)((dxVz + dzVx) / 2.f) * a.dt;
+        acc[8] += (double)((dxVy + dyVx) / 2.f) * a.dt;
+    }
+    if ((it - 1) % a.ntdec_w != 0) return;
+    const int itw = (it - 1) / a.ntdec_w;
+    if (itw >= a.ntw) return;
+    if (a.flags & 1) {
+        float* w = a.wav_v + (size_t)n * 3 * a.ntw + itw;
+        w[0] = (v(0, i, j, k) + v(0, i - 1, j, k)) / 2.f * a.vscale;
+        w[a.ntw] = (v(1, i, j, k) + v(1, i, j - 1, k)) / 2.f * a.vscale;
+        w[2 * a.ntw] = -(v(2, i, j, k) + v(2, i, j, k - 1)) / 2.f * a.vscale;
+    }
+    if (a.flags & 2) {
+        float* w = a.wav_u + (size_t)n * 3 * a.ntw + itw;
+        for (int c = 0; c < 3; ++c) w[c * a.ntw] = (float)acc[c] * a.vscale;
+    }
+    if (a.flags & 4) {
+        float* w = a.wav_s + (size_t)n * 6 * a.ntw + itw;
+        w[0] = s(0, i, j, k) * a.sscale;
+        w[a.ntw] = s(1, i, j, k) * a.sscale;
+        w[2 * a.ntw] = s(2, i, j, k) * a.sscale;
+        w[3 * a.ntw] = (s(3, i, j, k) + s(3, i, j - 1, k) + s(3, i, j, k - 1) + s(3, i, j - 1, k - 1)) / 4.f * a.sscale;
+        w[4 * a.ntw] = (s(4, i, j, k) + s(4, i - 1, j, k) + s(4, i, j, k - 1) + s(4, i - 1, j, k - 1)) / 4.f * a.sscale;
+        w[5 * a.ntw] = (s(5, i, j, k) + s(5, i, j - 1, k) + s(5, i - 1, j, k) + s(5, i - 1, j - 1, k)) / 4.f * a.sscale;
+    }
+    if (a.flags & 8) {
+        float* w = a.wav_e + (size_t)n * 6 * a.ntw + itw;
+        for (int c = 0; c < 6; ++c) w[c * a.ntw] = (float)acc[3 + c] * a.escale;
+    }
+}
+
+struct SnapArgs {
+    Geo g;
+    const float* V;
+    int kinds, kz0, idec, jdec, ntdec_s, nxs, nys, maxframes;
+    float vscale;   // UC * M0
+    float dt;
+    float* xy_v;    // frames of (nxs, nys, 3)
+    float* xy_u;    // same
+    double* uacc;   // (nxs, nys, 3) running displacement
+    const int* it;
+};
+
+// m_snap.f90:1587-1653 (xy_v) and 1963-2025 (xy_u)
+__global__ void k_snap_xy(const SnapArgs a) {
+    const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+    const int jj = blockIdx.y;
+    if (ii >= a.nxs || jj >= a.nys) return;
+    const int it = *a.it;
+    const int i = (ii + 1) * a.idec - a.idec / 2 - 1;
+    const int j = (jj + 1) * a.jdec - a.jdec / 2 - 1;
+    const Geo& g = a.g;
+    const size_t pl = (size_t)a.nxs * a.nys;
+    const size_t q = (size_t)jj * a.nxs + ii;
+    float v3[3];
+    for (int c = 0; c < 3; ++c) v3[c] = a.V[goff(g, 3, c, i, j, a.kz0)];
+    if (a.kinds & 2)
+        for (int c = 0; c < 3; ++c) a.uacc[q + c * pl] += (double)v3[c] * (double)a.vscale * (double)a.dt;
+    if ((it - 1) % a.ntdec_s != 0) return;
+    const int fr = (it - 1) / a.ntdec_s;
+    if (fr >= a.maxframes) return;
+    if (a.kinds & 1)
+        for (int c = 0; c < 3; ++c) a.xy_v[(size_t)fr * 3 * pl + c * pl + q] = v3[c] * a.vscale;
+    if (a.kinds & 2)
+        for (int c = 0; c < 3; ++c) a.xy_u[(size_t)fr * 3 * pl + c * pl + q] = (float)a.uacc[q + c * pl];
+}
+
+struct VmaxArgs {
+    Geo g;
+    const float* V;
+    const int* kob;        // (nx, ny) 1-based kob of each column, 0-based map
+    int i0, i1, j0, j1;    // 0-based inclusive ranges
+    int ntdec_r, nrep;
+    unsigned int* rep;     // (nrep, 3) float bits of max |V|
+    const int* it;
+};
+
+// m_kernel.f90:350-374 (+ the NaN check the report's divergence test implies)
+__global__ void k_vmax(const VmaxArgs a) {
+    const int it = *a.it;
+    if (a.ntdec_r <= 0 || it % a.ntdec_r != 0) return;
+    const int r = it / a.ntdec_r - 1;
+    if (r >= a.nrep) return;
+    float m[3] = {0.f, 0.f, 0.f};
+    const int ni = a.i1 - a.i0 + 1, nj = a.j1 - a.j0 + 1;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ni * nj; p += gridDim.x * blockDim.x) {
+        int i = a.i0 + p % ni, j = a.j0 + p / ni;
+        int kz = a.kob[j * a.g.nx + i];  // kob + 1 (1-based) == kob (0-based)
+        for (int c = 0; c < 3; ++c) {
+            float v = fabsf(a.V[goff(a.g, 3, c, i, j, kz)]);
+            if (v != v) v = __int_as_float(0x7fc00000);
+            m[c] = (v != v || v > m[c]) ? v : m[c];
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        float v = m[c];
+        for (int o = 16; o > 0; o >>= 1) {
+            float w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = (w != w || w > v) ? w : v;
+        }
+        if ((threadIdx.x & 31) == 0) atomicMax(a.rep + 3 * r + c, __float_as_uint(v));
+    }
+}
+
+__global__ void k_set_it(int* it, int v) { *it = v; }
+__global__ void k_advance(int* it) { *it += 1; }
+
+// Fortran (k,i,j) halo array -> one field of a device group (upload)
+__global__ void k_scatter_f(const float* src, float* dst, Geo g, int nf, int f, int store_kind, void* dst16) {
+    const long long n = (long long)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(p % (g.nz + 6)) - 3;
+        long long q = p / (g.nz + 6);
+        int i = (int)(q % (g.nx + 6)) - 3;
+        int j = (int)(q / (g.nx + 6)) - 3;
+        dst[goff(g, nf, f, i, j, k)] = src[p];
+        (void)store_kind; (void)dst16;
+    }
+}
+
+// one field of a device group -> Fortran (nz, nx, ny) physical-grid double array
+__global__ void k_gather_d(const float* src, double* dst, Geo g, int nf, int f) {
+    const long long n = (long long)g.nz * g.nx * g.ny;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(p % g.nz);
+        long long q = p / g.nz;
+        int i = (int)(q % g.nx);
+        int j = (int)(q / g.nx);
+        dst[p] = (double)src[goff(g, nf, f, i, j, k)];
+    }
+}
+
+}  // namespace swpc

@@ -1,0 +1,74 @@
+// sim.hpp -- per-simulation device state behind the swpc_sim handle.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "../../include/swpc_gpu.h"
+#include "kernels.cuh"
+
+namespace swpc {
+
+int set_err(int code, const std::string& msg);
+
+// Geometry and sizes of one simulation's device state.
+struct Plan {
+    Geo g;
+    bool pml;
+    int x0, y0, nxi, nyi, nzi;  // viscoelastic interior box
+    int rpitch, rbytes;
+    long long nV, nS, nM, nR, nade, npml, bytes;
+    PmlBox box[5];
+    int nbox;
+};
+
+struct Sim {
+    swpc_dims dims;
+    Plan p;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = 8;
+    long long launches = 0, launches_per_graph = 0;
+    std::vector<void*> allocs;
+
+    float *V = nullptr, *S = nullptr, *M = nullptr;
+    void* R = nullptr;
+    int4* band = nullptr;
+    float *adeV = nullptr, *adeS = nullptr;
+    float* cer = nullptr;
+    int cer_off[6] = {0, 0, 0, 0, 0, 0};
+    int* d_it = nullptr;
+    int* d_kob = nullptr;
+    Coef coef{};
+    int kchunk = 1, pml_blocks = 1;
+
+    PArgs pml_args{};
+    SrcArgs src_args{};
+    TapArgs tap_args{};
+    SnapArgs snap_args{};
+    VmaxArgs vmax_args{};
+    std::vector<unsigned int> rep_host;
+    bool bf_mode = false, medium_ready = false, diverged = false, profiling = false;
+    int it_done = 0;
+
+    cudaEvent_t evs[12] = {};
+    double prof_ms[6] = {0, 0, 0, 0, 0, 0};
+    long long prof_n[6] = {0, 0, 0, 0, 0, 0};
+
+    ~Sim();
+    int dalloc(void** ptr, size_t bytes);
+    int allocate();
+    int upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
+                      const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top, const int* kob_bot,
+                      const double* ts);
+    int set_sources(int n, const int* ijk, const double* mo, const double* mij, const double* fxyz, const double* prm,
+                    int stftype, bool bf);
+    int set_receivers(int n, const int* ijk, int ntdec_w, int flags);
+    int set_snapshot(int kinds, int k0, int idec, int jdec, int ntdec_s);
+    void fill_zargs(ZArgs& z) const;
+    int launch_step(bool timed);
+    int ensure_graph();
+    int check_divergence();
+};
+
+}  // namespace swpc

@@ -1,0 +1,697 @@
+// swpc_gpu.cu -- C ABI, device memory and launch sequencing of the GB300
+// swpc_3d time step.  The kernels are in kernels.cuh.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/swpc_gpu.h"
+#include "kernels.cuh"
+#include "sim.hpp"
+
+using namespace swpc;
+
+namespace {
+thread_local std::string g_err;
+}
+
+namespace swpc {
+int set_err(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+}  // namespace swpc
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return set_err(SWPC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+static inline long long rup(long long v, long long m) { return (v + m - 1) / m * m; }
+
+// ---------------------------------------------------------------------------
+// geometry and allocation plan
+// ---------------------------------------------------------------------------
+static int plan(const swpc_dims* d, Plan& p) {
+    if (!d) return set_err(SWPC_E_ARG, "null dims");
+    if (d->nm != NM) return set_err(SWPC_E_ARG, "nm must be 3 (compile-time constant NM of m_global.f90:31)");
+    if (d->nx < 8 || d->ny < 8 || d->nz < 8) return set_err(SWPC_E_ARG, "grid too small (nx, ny, nz >= 8)");
+    if (d->abc_type != SWPC_ABC_PML && d->abc_type != SWPC_ABC_CERJAN) return set_err(SWPC_E_ARG, "abc_type must be PML or Cerjan");
+    if (d->na < 0 || (d->abc_type == SWPC_ABC_PML && (d->nx <= 2 * d->na + 2 || d->ny <= 2 * d->na + 2 || d->nz <= d->na + 2)))
+        return set_err(SWPC_E_ARG, "absorber thickness na leaves no interior");
+    if (!(d->dx > 0 && d->dy > 0 && d->dz > 0 && d->dt > 0)) return set_err(SWPC_E_ARG, "dx, dy, dz, dt must be positive");
+    if (d->store < SWPC_STORE_FP32 || d->store > SWPC_STORE_BF16) return set_err(SWPC_E_ARG, "bad store mode");
+    if ((long long)d->nx * d->ny * d->nz > (1LL << 36)) return set_err(SWPC_E_ARG, "grid too large");
+    p.pml = d->abc_type == SWPC_ABC_PML;
+    p.x0 = p.pml ? d->na : 0;
+    p.y0 = p.pml ? d->na : 0;
+    p.nxi = p.pml ? d->nx - 2 * d->na : d->nx;
+    p.nyi = p.pml ? d->ny - 2 * d->na : d->ny;
+    p.nzi = p.pml ? d->nz - d->na : d->nz;
+    Geo& g = p.g;
+    g.nx = d->nx; g.ny = d->ny; g.nz = d->nz; g.na = d->na;
+    g.hx = 4 + ((32 - (4 + p.x0) % 32) % 32);
+    g.pitch = (int)rup(g.hx + d->nx + 40, 32);
+    g.nyp = HYT + d->ny + TBY + 3;
+    g.nzp = HZT + d->nz + 3;
+    p.rpitch = (int)rup(p.nxi, 32);
+    const long long cell = (long long)g.pitch * g.nyp * g.nzp;
+    p.nV = 3 * cell; p.nS = 6 * cell; p.nM = 5 * cell;
+    p.rbytes = d->store == SWPC_STORE_FP32 ? 4 : 2;
+    p.nR = 18LL * p.rpitch * p.nyi * p.nzi;
+    // PML shell boxes
+    p.nbox = 0;
+    p.nade = 0;
+    long long first = 0;
+    if (p.pml) {
+        const int na = d->na, nx = d->nx, ny = d->ny, nz = d->nz;
+        int bx[5][6] = {{0, 0, 0, na, ny, nz}, {nx - na, 0, 0, na, ny, nz}, {na, 0, 0, nx - 2 * na, na, nz},
+                        {na, ny - na, 0, nx - 2 * na, na, nz}, {na, na, nz - na, nx - 2 * na, ny - 2 * na, na}};
+        for (int b = 0; b < 5; ++b) {
+            if (bx[b][3] <= 0 || bx[b][4] <= 0 || bx[b][5] <= 0) continue;
+            PmlBox& B = p.box[p.nbox++];
+            B.x0 = bx[b][0]; B.y0 = bx[b][1]; B.z0 = bx[b][2]; B.nx = bx[b][3]; B.ny = bx[b][4]; B.nz = bx[b][5];
+            B.pitch = (int)rup(B.nx, 32);
+            B.off = p.nade;
+            B.first = first;
+            p.nade += 9LL * B.pitch * B.ny * B.nz;
+            first += (long long)B.nx * B.ny * B.nz;
+        }
+    }
+    p.npml = first;
+    p.bytes = 4 * (p.nV + p.nS + p.nM) + p.rbytes * p.nR + 4 * 2 * p.nade + 16LL * p.nxi * p.nyi;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 coefficient set-up
+// ---------------------------------------------------------------------------
+static void damping_profile(double x, double H, double xb, double xe, double na, double fcut, double dt, float* g) {
+    // m_absorb_p.f90:533-573 (FP64 arithmetic, rounded to FP32 storage)
+    const double R0 = std::pow(10.0, -(std::log10(na) - 1) / std::log10(2.0) - 3.0);
+    const double d0 = -(1.0 / (2.0 * H)) * 2.0 * 6.0 * std::log(R0);
+    const double b0 = 7.0, a0 = M_PI * fcut;
+    double xx;
+    if (x <= xb + H) xx = (xb + H) - x;
+    else if (x >= xe - H) xx = x - (xe - H);
+    else xx = 0;
+    const double r = std::fabs(xx / H);
+    const double d = d0 * r, a = a0 * (1 - r), b = 1 + (b0 - 1) * r * r;
+    const double h = dt / 2.0, den = 1 + h * (a + d / b);
+    g[0] = (float)(((1 + h * a) / b) / den);
+    g[1] = (float)((-1.0 / b) / den);
+    g[2] = (float)((1 - h * (a + d / b)) / den);
+    g[3] = (float)((d / b) / den);
+}
+
+static void cerjan_profile(int n, int na, double d, std::vector<float>& c, std::vector<float>& bnd, bool zaxis) {
+    // m_absorb_c.f90:55-101: exp(-alpha (1 - x/L)^2) at cell centre and boundary
+    const double alpha = 0.09, L = na * d;
+    c.assign(n, 1.f); bnd.assign(n, 1.f);
+    for (int q = 1; q <= n; ++q) {
+        auto e = [&](double x) { double t = 1.0 - x / L; return (float)std::exp(-alpha * t * t); };
+        if (q <= na && !zaxis) {
+            double xc = (q - 0.5) * d;
+            c[q - 1] = e(xc); bnd[q - 1] = e(xc + d / 2);
+        } else if (q >= n - na + 1) {
+            double xr = n * d - (q - 0.5) * d;
+            c[q - 1] = e(xr + d / 2); bnd[q - 1] = e(xr);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launches
+// ---------------------------------------------------------------------------
+void Sim::fill_zargs(ZArgs& z) const {
+    z.g = p.g;
+    z.V = V; z.S = S; z.M = M; z.R = R; z.band = band;
+    z.x0 = p.x0; z.y0 = p.y0; z.nxi = p.nxi; z.nyi = p.nyi; z.kz_end = p.nzi;
+    z.kchunk = kchunk; z.rpitch = p.rpitch;
+    z.cer = p.pml ? nullptr : cer;
+    for (int q = 0; q < 6; ++q) z.cer_off[q] = cer_off[q];
+    z.c = coef;
+}
+
+int Sim::launch_step(bool timed) {
+    const dim3 blk(TBX, TBY);
+    const dim3 grd((p.nxi + TBX - 1) / TBX, (p.nyi + TBY - 1) / TBY, (p.nzi + kchunk - 1) / kchunk);
+    auto ev0 = [&](int c) { if (timed) cudaEventRecord(evs[2 * c], stream); };
+    auto ev1 = [&](int c) {
+        if (timed) {
+            cudaEventRecord(evs[2 * c + 1], stream);
+            cudaEventSynchronize(evs[2 * c + 1]);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, evs[2 * c], evs[2 * c + 1]);
+            prof_ms[c] += ms;
+            prof_n[c] += 1;
+        }
+    };
+    if (vmax_args.ntdec_r > 0) { k_vmax<<<64, 256, 0, stream>>>(vmax_args); ++launches; }
+    if (tap_args.n > 0) {
+        ev0(4);
+        k_taps<<<(tap_args.n + 127) / 128, 128, 0, stream>>>(tap_args); ++launches;
+        ev1(4);
+    }
+    if (snap_args.kinds) {
+        dim3 sg((snap_args.nxs + 127) / 128, snap_args.nys);
+        k_snap_xy<<<sg, 128, 0, stream>>>(snap_args); ++launches;
+    }
+    ZArgs z;
+    fill_zargs(z);
+    ev0(0);
+    if (p.rbytes == 4) k_stress_interior<float><<<grd, blk, 0, stream>>>(z);
+    else if (dims.store == SWPC_STORE_FP16) k_stress_interior<__half><<<grd, blk, 0, stream>>>(z);
+    else k_stress_interior<__nv_bfloat16><<<grd, blk, 0, stream>>>(z);
+    ++launches;
+    ev1(0);
+    if (p.pml) {
+        ev0(2);
+        k_stress_pml<<<pml_blocks, 256, 0, stream>>>(pml_args); ++launches;
+        ev1(2);
+    }
+    if (src_args.n > 0 && !bf_mode) {
+        ev0(5);
+        k_stressglut<<<(src_args.n + 127) / 128, 128, 0, stream>>>(src_args); ++launches;
+        ev1(5);
+    }
+    ev0(1);
+    k_vel_interior<<<grd, blk, 0, stream>>>(z); ++launches;
+    ev1(1);
+    if (p.pml) {
+        ev0(3);
+        k_vel_pml<<<pml_blocks, 256, 0, stream>>>(pml_args); ++launches;
+        ev1(3);
+    }
+    if (src_args.n > 0 && bf_mode) {
+        k_bodyforce<<<(src_args.n + 127) / 128, 128, 0, stream>>>(src_args); ++launches;
+    }
+    k_advance<<<1, 1, 0, stream>>>(d_it); ++launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+int Sim::ensure_graph() {
+    if (graph_exec) return 0;
+    long long l0 = launches;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int q = 0; q < graph_steps && rc == 0; ++q) rc = launch_step(false);
+    cudaGraph_t gr;
+    cudaError_t e = cudaStreamEndCapture(stream, &gr);
+    if (rc) return rc;
+    if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&graph_exec, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    launches_per_graph = launches - l0;
+    launches = l0;
+    return 0;
+}
+
+int Sim::check_divergence() {
+    if (vmax_args.ntdec_r <= 0 || !rep_host.size()) return 0;
+    CK(cudaMemcpyAsync(rep_host.data(), vmax_args.rep, rep_host.size() * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    for (size_t q = 0; q < rep_host.size(); ++q) {
+        float v;
+        std::memcpy(&v, &rep_host[q], 4);
+        if (v != v || (double)v * dims.UC > 1e5) {
+            char buf[160];
+            snprintf(buf, sizeof buf, "numerical divergence detected at it=%d with max amp = %g [(m/s)/moment]",
+                     (int)((q / 3 + 1) * vmax_args.ntdec_r), (double)v * dims.UC);
+            diverged = true;
+            return set_err(SWPC_E_DIVERGED, buf);
+        }
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+long long swpc_gpu_required_bytes(const swpc_dims* d) {
+    Plan p;
+    if (plan(d, p)) return -1;
+    return p.bytes;
+}
+
+int swpc_gpu_create(const swpc_dims* d, swpc_sim** out) {
+    if (!out) return set_err(SWPC_E_ARG, "null output pointer");
+    *out = nullptr;
+    Sim* s = new Sim();
+    int rc = plan(d, s->p);
+    if (rc) { delete s; return rc; }
+    s->dims = *d;
+    rc = s->allocate();
+    if (rc) { delete s; return rc; }
+    *out = reinterpret_cast<swpc_sim*>(s);
+    return 0;
+}
+
+int swpc_gpu_destroy(swpc_sim* sim) {
+    delete reinterpret_cast<Sim*>(sim);
+    return 0;
+}
+
+int swpc_gpu_last_error(char* buf, size_t n) {
+    if (buf && n) {
+        size_t m = std::min(n - 1, g_err.size());
+        std::memcpy(buf, g_err.data(), m);
+        buf[m] = 0;
+    }
+    return (int)g_err.size();
+}
+
+void* swpc_gpu_stream(swpc_sim* sim) { return sim ? (void*)reinterpret_cast<Sim*>(sim)->stream : nullptr; }
+
+long long swpc_gpu_launch_count(swpc_sim* sim) { return sim ? reinterpret_cast<Sim*>(sim)->launches : -1; }
+
+int swpc_gpu_upload_medium(swpc_sim* sim, const float* rho, const float* lam, const float* mu, const float* taup,
+                           const float* taus, const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot,
+                           const int* kob_top, const int* kob_bot, const double* ts) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !rho || !lam || !mu || !taup || !taus || !kob || !kfs_top || !kfs_bot || !kob_top || !kob_bot || !ts)
+        return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium");
+    (void)kfs;
+    return s->upload_medium(rho, lam, mu, taup, taus, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts);
+}
+
+int swpc_gpu_set_sources(swpc_sim* sim, int n, const int* ijk, const double* mo, const double* mij, const double* fxyz,
+                         const double* prm, int stftype, int bf_mode) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || n < 0 || (n > 0 && (!ijk || !prm || (bf_mode ? !fxyz : (!mo || !mij)))))
+        return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_sources");
+    if (stftype < 0 || stftype > 5) return set_err(SWPC_E_ARG, "unknown source time function");
+    return s->set_sources(n, ijk, mo, mij, fxyz, prm, stftype, bf_mode != 0);
+}
+
+int swpc_gpu_set_receivers(swpc_sim* sim, int n, const int* ijk, int ntdec_w, int flags) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || n < 0 || (n > 0 && !ijk) || ntdec_w <= 0 || (flags & ~15))
+        return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_receivers");
+    return s->set_receivers(n, ijk, ntdec_w, flags);
+}
+
+int swpc_gpu_set_snapshot(swpc_sim* sim, int kinds, int k0, int idec, int jdec, int ntdec_s) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || (kinds & ~3) || idec <= 0 || jdec <= 0 || ntdec_s <= 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_snapshot");
+    if (kinds && (k0 < 1 || k0 > s->dims.nz)) return set_err(SWPC_E_ARG, "snapshot plane k0 outside 1..nz");
+    return s->set_snapshot(kinds, k0, idec, jdec, ntdec_s);
+}
+
+int swpc_gpu_step(swpc_sim* sim, int it) { return swpc_gpu_run(sim, it, it); }
+
+int swpc_gpu_run(swpc_sim* sim, int it0, int it1) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    if (!s->medium_ready) return set_err(SWPC_E_STATE, "upload the medium before stepping");
+    if (s->diverged) return set_err(SWPC_E_DIVERGED, "simulation has diverged");
+    if (it1 < it0) return 0;
+    k_set_it<<<1, 1, 0, s->stream>>>(s->d_it, it0);
+    ++s->launches;
+    int n = it1 - it0 + 1, rc = 0;
+    if (s->profiling) {
+        for (int q = 0; q < n && rc == 0; ++q) rc = s->launch_step(true);
+    } else {
+        if (n >= s->graph_steps) {
+            rc = s->ensure_graph();
+            while (rc == 0 && n >= s->graph_steps) {
+                cudaError_t e = cudaGraphLaunch(s->graph_exec, s->stream);
+                if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+                s->launches += s->launches_per_graph;
+                n -= s->graph_steps;
+            }
+        }
+        for (int q = 0; q < n && rc == 0; ++q) rc = s->launch_step(false);
+    }
+    s->it_done = it1;
+    return rc;
+}
+
+int swpc_gpu_sync(swpc_sim* sim) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    CK(cudaStreamSynchronize(s->stream));
+    return s->check_divergence();
+}
+
+int swpc_gpu_query(swpc_sim* sim, int* ntw, int* nst, int* nxs, int* nys, int* nframes) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    if (ntw) *ntw = s->tap_args.ntw;
+    if (nst) *nst = s->tap_args.n;
+    if (nxs) *nxs = s->snap_args.nxs;
+    if (nys) *nys = s->snap_args.nys;
+    if (nframes) *nframes = s->snap_args.kinds ? std::min(s->snap_args.maxframes, (s->it_done - 1) / std::max(1, s->snap_args.ntdec_s) + 1) : 0;
+    return 0;
+}
+
+int swpc_gpu_fetch_waveforms(swpc_sim* sim, int kind, float* out) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out) return set_err(SWPC_E_ARG, "null argument");
+    const TapArgs& t = s->tap_args;
+    float* src = nullptr;
+    int nc = 3;
+    switch (kind) {
+    case SWPC_WAV_V: src = t.wav_v; break;
+    case SWPC_WAV_U: src = t.wav_u; break;
+    case SWPC_WAV_STRESS: src = t.wav_s; nc = 6; break;
+    case SWPC_WAV_STRAIN: src = t.wav_e; nc = 6; break;
+    default: return set_err(SWPC_E_ARG, "kind must be one SWPC_WAV_* bit");
+    }
+    if (!src || !(t.flags & kind)) return set_err(SWPC_E_STATE, "that waveform kind was not requested");
+    CK(cudaMemcpyAsync(out, src, (size_t)t.ntw * nc * t.n * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return s->check_divergence();
+}
+
+int swpc_gpu_fetch_snapshot(swpc_sim* sim, int kind, int frame, float* out) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out) return set_err(SWPC_E_ARG, "null argument");
+    const SnapArgs& a = s->snap_args;
+    if (!(a.kinds & kind) || (kind != 1 && kind != 2)) return set_err(SWPC_E_STATE, "that snapshot kind was not requested");
+    if (frame < 0 || frame >= a.maxframes) return set_err(SWPC_E_ARG, "frame out of range");
+    const size_t pl = (size_t)a.nxs * a.nys * 3;
+    CK(cudaMemcpyAsync(out, (kind == 1 ? a.xy_v : a.xy_u) + frame * pl, pl * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int swpc_gpu_vmax(swpc_sim* sim, float out[3]) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out) return set_err(SWPC_E_ARG, "null argument");
+    out[0] = out[1] = out[2] = 0;
+    if (s->vmax_args.ntdec_r <= 0 || s->rep_host.empty()) return 0;
+    int rc = swpc_gpu_sync(sim);
+    int r = s->it_done / s->vmax_args.ntdec_r - 1;
+    if (r < 0) return rc;
+    r = std::min(r, s->vmax_args.nrep - 1);
+    for (int c = 0; c < 3; ++c) {
+        float v;
+        std::memcpy(&v, &s->rep_host[3 * r + c], 4);
+        out[c] = (float)((double)v * s->dims.UC * s->dims.M0);
+    }
+    return rc;
+}
+
+int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out || which < 0 || which > 8) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_fetch_field");
+    const Geo& g = s->p.g;
+    size_t n = (size_t)g.nx * g.ny * g.nz;
+    double* d = nullptr;
+    CK(cudaMallocAsync(&d, n * 8, s->stream));
+    if (which < 3) k_gather_d<<<1024, 256, 0, s->stream>>>(s->V, d, g, 3, which);
+    else k_gather_d<<<1024, 256, 0, s->stream>>>(s->S, d, g, 6, which - 3);
+    ++s->launches;
+    CK(cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaFreeAsync(d, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int swpc_gpu_profile(swpc_sim* sim, int enable) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    s->profiling = enable != 0;
+    for (int c = 0; c < 6; ++c) { s->prof_ms[c] = 0; s->prof_n[c] = 0; }
+    return 0;
+}
+
+int swpc_gpu_profile_read(swpc_sim* sim, double* ms, long long* n) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    for (int c = 0; c < 6; ++c) {
+        if (ms) ms[c] = s->prof_ms[c];
+        if (n) n[c] = s->prof_n[c];
+    }
+    return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Sim methods
+// ---------------------------------------------------------------------------
+Sim::~Sim() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (void* q : allocs) cudaFree(q);
+    for (auto& e : evs) if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+int Sim::dalloc(void** ptr, size_t bytes) {
+    cudaError_t e = cudaMalloc(ptr, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(SWPC_E_NOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+    }
+    allocs.push_back(*ptr);
+    e = cudaMemsetAsync(*ptr, 0, bytes ? bytes : 16, stream);
+    if (e != cudaSuccess) return set_err(SWPC_E_CUDA, cudaGetErrorString(e));
+    return 0;
+}
+
+int Sim::allocate() {
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (auto& e : evs) CK(cudaEventCreate(&e));
+    int rc;
+    if ((rc = dalloc((void**)&V, p.nV * 4))) return rc;
+    if ((rc = dalloc((void**)&S, p.nS * 4))) return rc;
+    if ((rc = dalloc((void**)&M, p.nM * 4))) return rc;
+    if ((rc = dalloc(&R, p.nR * p.rbytes))) return rc;
+    if ((rc = dalloc((void**)&band, 16 * (size_t)p.nxi * p.nyi))) return rc;
+    if (p.pml) {
+        if ((rc = dalloc((void**)&adeV, p.nade * 4))) return rc;
+        if ((rc = dalloc((void**)&adeS, p.nade * 4))) return rc;
+    }
+    if ((rc = dalloc((void**)&d_it, 16))) return rc;
+    if ((rc = dalloc((void**)&d_kob, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
+    // z chunking: enough blocks to fill the GPU at least ~4 times
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    long long cols = (long long)((p.nxi + TBX - 1) / TBX) * ((p.nyi + TBY - 1) / TBY);
+    long long want = 8LL * nsm;
+    int nchunk = (int)std::max(1LL, std::min((long long)(p.nzi / 8), (want + cols - 1) / cols));
+    kchunk = (p.nzi + nchunk - 1) / nchunk;
+    pml_blocks = (int)std::min<long long>((p.npml + 255) / 256, 64LL * nsm);
+    if (pml_blocks < 1) pml_blocks = 1;
+    graph_steps = 8;
+    return 0;
+}
+
+int Sim::upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
+                       const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top, const int* kob_bot,
+                       const double* ts) {
+    const Geo& g = p.g;
+    const size_t n3 = (size_t)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
+    float* stage = nullptr;
+    CK(cudaMallocAsync((void**)&stage, n3 * 4, stream));
+    const float* fields[5] = {rho, lam, mu, taup, taus};
+    for (int f = 0; f < 5; ++f) {
+        CK(cudaMemcpyAsync(stage, fields[f], n3 * 4, cudaMemcpyHostToDevice, stream));
+        k_scatter_f<<<2048, 256, 0, stream>>>(stage, M, g, 5, f, 0, nullptr);
+        ++launches;
+    }
+    CK(cudaFreeAsync(stage, stream));
+    // band table over the interior columns and the kob map
+    const int mx = g.nx + 6;
+    auto at = [&](const int* m, int i, int j) { return m[(size_t)(j + 2) * mx + (i + 2)]; };  // 1-based i, j
+    std::vector<int> bnd(4 * (size_t)p.nxi * p.nyi);
+    for (int jj = 0; jj < p.nyi; ++jj)
+        for (int ii = 0; ii < p.nxi; ++ii) {
+            int i = p.x0 + ii + 1, j = p.y0 + jj + 1;
+            size_t q = 4 * ((size_t)jj * p.nxi + ii);
+            bnd[q] = at(kfs_top, i, j); bnd[q + 1] = at(kfs_bot, i, j);
+            bnd[q + 2] = at(kob_top, i, j); bnd[q + 3] = at(kob_bot, i, j);
+        }
+    std::vector<int> kb((size_t)g.nx * g.ny);
+    for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i) kb[(size_t)j * g.nx + i] = std::max(0, std::min(g.nz - 1, at(kob, i + 1, j + 1)));
+    CK(cudaMemcpyAsync(band, bnd.data(), bnd.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_kob, kb.data(), kb.size() * 4, cudaMemcpyHostToDevice, stream));
+
+    // FD and Zener coefficients in FP64 (m_kernel.f90:43-67)
+    const double dt = dims.dt, dx = dims.dx, dy = dims.dy, dz = dims.dz;
+    coef.e4x0 = (float)(18.0 / 16.0 / dx); coef.e4x1 = (float)(2.0 / 48.0 / dx);
+    coef.e4y0 = (float)(18.0 / 16.0 / dy); coef.e4y1 = (float)(2.0 / 48.0 / dy);
+    coef.e4z0 = (float)(18.0 / 16.0 / dz); coef.e4z1 = (float)(2.0 / 48.0 / dz);
+    coef.e2x = (float)(1.0 / dx); coef.e2y = (float)(1.0 / dy); coef.e2z = (float)(1.0 / dz);
+    double d2 = 0;
+    for (int m = 0; m < NM; ++m) {
+        coef.c1[m] = (float)((2 * ts[m] - dt) / (2 * ts[m] + dt));
+        coef.c2[m] = (float)(2.0 / (2 * ts[m] + dt) / NM);
+        coef.d1[m] = (float)(2 * ts[m] / (2 * ts[m] - dt));
+        d2 += dt / (2 * ts[m] - dt);
+    }
+    coef.d2 = (float)(d2 / NM);
+    coef.dt = (float)dt;
+
+    // absorbing boundary profiles in FP64
+    if (p.pml) {
+        std::vector<float> prof;
+        auto add = [&](int n, double beg, double d) {
+            int o0 = (int)prof.size();
+            prof.resize(prof.size() + 8 * (size_t)n);
+            const double H = dims.na * d, end = beg + n * d;
+            for (int q = 0; q < n; ++q) {
+                double xc = beg + (q + 0.5) * d;
+                damping_profile(xc, H, beg, end, dims.na, dims.fcut, dt, &prof[o0 + 4 * q]);
+                damping_profile(xc + d / 2, H, beg, end, dims.na, dims.fcut, dt, &prof[o0 + 4 * n + 4 * q]);
+            }
+            return o0;
+        };
+        PArgs& a = pml_args;
+        a.pxc = add(g.nx, dims.xbeg, dx); a.pxe = a.pxc + 4 * g.nx;
+        a.pyc = add(g.ny, dims.ybeg, dy); a.pye = a.pyc + 4 * g.ny;
+        a.pzc = add(g.nz, dims.zbeg, dz); a.pze = a.pzc + 4 * g.nz;
+        float* dp = nullptr;
+        int rc = dalloc((void**)&dp, prof.size() * 4);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(dp, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, stream));
+        a.g = g; a.V = V; a.S = S; a.M = M; a.adeV = adeV; a.adeS = adeS; a.prof = dp;
+        a.nbox = p.nbox;
+        for (int b = 0; b < p.nbox; ++b) a.box[b] = p.box[b];
+        a.npts = p.npml;
+        a.r20x = (float)(1.0 / dx); a.r20y = (float)(1.0 / dy); a.r20z = (float)(1.0 / dz); a.dt = (float)dt;
+    } else {
+        std::vector<float> c, b, all;
+        int n[3] = {g.nx, g.ny, g.nz};
+        double d[3] = {dx, dy, dz};
+        for (int ax = 0; ax < 3; ++ax) {
+            cerjan_profile(n[ax], dims.na, d[ax], c, b, ax == 2);
+            cer_off[2 * ax] = (int)all.size(); all.insert(all.end(), c.begin(), c.end());
+            cer_off[2 * ax + 1] = (int)all.size(); all.insert(all.end(), b.begin(), b.end());
+        }
+        int rc = dalloc((void**)&cer, all.size() * 4);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(cer, all.data(), all.size() * 4, cudaMemcpyHostToDevice, stream));
+    }
+    // divergence check (m_report.f90:120-152)
+    VmaxArgs& v = vmax_args;
+    v.g = g; v.V = V; v.kob = d_kob; v.it = d_it;
+    v.ntdec_r = dims.ntdec_r;
+    const int ibk = p.x0 + 1, iek = p.x0 + p.nxi, jbk = p.y0 + 1, jek = p.y0 + p.nyi;
+    v.i0 = std::max(dims.na + 5 + 1, ibk) - 1; v.i1 = std::min(g.nx - dims.na - 5, iek) - 1;
+    v.j0 = std::max(dims.na + 5 + 1, jbk) - 1; v.j1 = std::min(g.ny - dims.na - 5, jek) - 1;
+    if (v.i1 < v.i0 || v.j1 < v.j0) v.ntdec_r = 0;
+    if (v.ntdec_r > 0) {
+        v.nrep = std::max(1, dims.nt / v.ntdec_r + 1);
+        int rc = dalloc((void**)&v.rep, (size_t)v.nrep * 12);
+        if (rc) return rc;
+        rep_host.assign((size_t)v.nrep * 3, 0u);
+    }
+    CK(cudaStreamSynchronize(stream));
+    medium_ready = true;
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    return 0;
+}
+
+int Sim::set_sources(int n, const int* ijk, const double* mo, const double* mij, const double* fxyz, const double* prm,
+                     int stftype, bool bf) {
+    SrcArgs& a = src_args;
+    a.g = p.g; a.V = V; a.S = S; a.M = M; a.it = d_it;
+    a.n = n; a.stf = stftype;
+    a.tbeg = (float)dims.tbeg; a.dt = (float)dims.dt;
+    a.dt_dxyz = (float)(dims.dt / (dims.dx * dims.dy * dims.dz));
+    bf_mode = bf;
+    if (n == 0) return 0;
+    std::vector<int> q(3 * (size_t)n);
+    std::vector<float> m6(6 * (size_t)n, 0.f), f3(3 * (size_t)n, 0.f), pr(2 * (size_t)n);
+    for (int s = 0; s < n; ++s) {
+        for (int c = 0; c < 3; ++c) {
+            q[3 * s + c] = ijk[3 * s + c] - 1;
+            int lim = c == 0 ? p.g.nx : c == 1 ? p.g.ny : p.g.nz;
+            if (q[3 * s + c] < -2 || q[3 * s + c] > lim + 1) return set_err(SWPC_E_ARG, "source grid point outside the model sleeve");
+        }
+        if (bf) for (int c = 0; c < 3; ++c) f3[3 * s + c] = (float)fxyz[3 * s + c];
+        else for (int c = 0; c < 6; ++c) m6[6 * s + c] = (float)(mo[s] * mij[6 * s + c]);
+        pr[2 * s] = (float)prm[2 * s];
+        pr[2 * s + 1] = (float)prm[2 * s + 1];
+    }
+    int* di; float *dm, *df, *dp;
+    int rc;
+    if ((rc = dalloc((void**)&di, q.size() * 4))) return rc;
+    if ((rc = dalloc((void**)&dm, m6.size() * 4))) return rc;
+    if ((rc = dalloc((void**)&df, f3.size() * 4))) return rc;
+    if ((rc = dalloc((void**)&dp, pr.size() * 4))) return rc;
+    CK(cudaMemcpyAsync(di, q.data(), q.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(dm, m6.data(), m6.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(df, f3.data(), f3.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(dp, pr.data(), pr.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    a.ijk = di; a.mij = dm; a.fxyz = df; a.prm = dp;
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    return 0;
+}
+
+int Sim::set_receivers(int n, const int* ijk, int ntdec_w, int flags) {
+    TapArgs& a = tap_args;
+    a.g = p.g; a.V = V; a.S = S; a.it = d_it;
+    a.n = n; a.ntdec_w = ntdec_w; a.flags = flags;
+    a.ntw = (int)std::floor((float)(dims.nt - 1) / (float)ntdec_w + 1.0f);
+    a.dt = (float)dims.dt;
+    a.vscale = (float)(dims.M0 * dims.UC * 1e9);
+    a.sscale = (float)(dims.M0 * dims.UC * 1e6);
+    a.escale = (float)(dims.M0 * dims.UC * 1e-3);
+    a.r40x = (float)(9.0 / 8.0 / dims.dx); a.r40y = (float)(9.0 / 8.0 / dims.dy); a.r40z = (float)(9.0 / 8.0 / dims.dz);
+    a.r41x = (float)(1.0 / 24.0 / dims.dx); a.r41y = (float)(1.0 / 24.0 / dims.dy); a.r41z = (float)(1.0 / 24.0 / dims.dz);
+    if (n == 0 || flags == 0) { a.n = 0; return 0; }
+    std::vector<int> q(3 * (size_t)n);
+    for (int s = 0; s < n; ++s)
+        for (int c = 0; c < 3; ++c) {
+            q[3 * s + c] = ijk[3 * s + c] - 1;
+            int lim = c == 0 ? p.g.nx : c == 1 ? p.g.ny : p.g.nz;
+            if (q[3 * s + c] < 0 || q[3 * s + c] >= lim) return set_err(SWPC_E_ARG, "receiver outside the grid");
+        }
+    int rc;
+    int* di;
+    if ((rc = dalloc((void**)&di, q.size() * 4))) return rc;
+    CK(cudaMemcpyAsync(di, q.data(), q.size() * 4, cudaMemcpyHostToDevice, stream));
+    a.ijk = di;
+    const size_t w3 = (size_t)a.ntw * 3 * n, w6 = (size_t)a.ntw * 6 * n;
+    a.wav_v = a.wav_u = a.wav_s = a.wav_e = nullptr;
+    if ((flags & 1) && (rc = dalloc((void**)&a.wav_v, w3 * 4))) return rc;
+    if ((flags & 2) && (rc = dalloc((void**)&a.wav_u, w3 * 4))) return rc;
+    if ((flags & 4) && (rc = dalloc((void**)&a.wav_s, w6 * 4))) return rc;
+    if ((flags & 8) && (rc = dalloc((void**)&a.wav_e, w6 * 4))) return rc;
+    if ((rc = dalloc((void**)&a.acc, 9 * (size_t)n * 8))) return rc;
+    CK(cudaStreamSynchronize(stream));
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    return 0;
+}
+
+int Sim::set_snapshot(int kinds, int k0, int idec, int jdec, int ntdec_s) {
+    SnapArgs& a = snap_args;
+    a.g = p.g; a.V = V; a.it = d_it;
+    a.kinds = kinds;
+    if (!kinds) return 0;
+    a.kz0 = k0 - 1; a.idec = idec; a.jdec = jdec; a.ntdec_s = ntdec_s;
+    a.nxs = (p.g.nx + idec / 2) / idec;
+    a.nys = (p.g.ny + jdec / 2) / jdec;
+    a.maxframes = (dims.nt - 1) / ntdec_s + 1;
+    a.vscale = (float)(dims.UC * dims.M0);
+    a.dt = (float)dims.dt;
+    const size_t fr = (size_t)a.maxframes * 3 * a.nxs * a.nys;
+    int rc;
+    a.xy_v = a.xy_u = nullptr; a.uacc = nullptr;
+    if ((kinds & 1) && (rc = dalloc((void**)&a.xy_v, fr * 4))) return rc;
+    if (kinds & 2) {
+        if ((rc = dalloc((void**)&a.xy_u, fr * 4))) return rc;
+        if ((rc = dalloc((void**)&a.uacc, (size_t)3 * a.nxs * a.nys * 8))) return rc;
+    }
+    CK(cudaStreamSynchronize(stream));
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    return 0;
+}

@@ -1,0 +1,246 @@
+"""ctypes binding of include/swpc_gpu.h -- the Python mirror of the host
+side of swpc_3d's time loop.
+
+The reference's driver (src/swpc_3d/main.f90) sets up the grid, medium,
+sources and stations on the host, then calls the step routines nt times and
+finally writes waveforms and snapshots.  ``Simulation`` exposes exactly those
+stages over the C ABI; ``Simulation.from_inf`` runs the whole host set-up
+chain from an ``input.inf`` file.  There is no CPU fallback: if the CUDA
+library cannot be loaded, every call raises.
+"""
+import ctypes
+import os
+import numpy as np
+
+from . import build as _build
+
+SWPC_WAV_V, SWPC_WAV_U, SWPC_WAV_STRESS, SWPC_WAV_STRAIN = 1, 2, 4, 8
+SWPC_SNAP_XY_V, SWPC_SNAP_XY_U = 1, 2
+STORE = {"fp32": 0, "fp16": 1, "bf16": 2}
+STF = {"boxcar": 0, "triangle": 1, "herrmann": 2, "kupper": 3, "cosine": 4, "scosine": 4, "texp": 5}
+FIELDS = ["Vx", "Vy", "Vz", "Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"]
+
+
+class SwpcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("swpc_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Dims(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("nt", ctypes.c_int),
+                ("na", ctypes.c_int), ("nm", ctypes.c_int), ("abc_type", ctypes.c_int), ("store", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+                ("xbeg", ctypes.c_double), ("ybeg", ctypes.c_double), ("zbeg", ctypes.c_double),
+                ("tbeg", ctypes.c_double), ("fcut", ctypes.c_double), ("M0", ctypes.c_double),
+                ("UC", ctypes.c_double), ("ntdec_r", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+_lib = None
+
+# every entry point declared in include/swpc_gpu.h
+EXPORTS = [
+    "swpc_gpu_create", "swpc_gpu_required_bytes", "swpc_gpu_upload_medium", "swpc_gpu_set_sources",
+    "swpc_gpu_set_receivers", "swpc_gpu_set_snapshot", "swpc_gpu_step", "swpc_gpu_run", "swpc_gpu_sync",
+    "swpc_gpu_fetch_waveforms", "swpc_gpu_fetch_snapshot", "swpc_gpu_query", "swpc_gpu_vmax",
+    "swpc_gpu_fetch_field", "swpc_gpu_profile", "swpc_gpu_profile_read", "swpc_gpu_stream",
+    "swpc_gpu_launch_count", "swpc_gpu_destroy", "swpc_gpu_last_error", "swpc_host_prepare",
+    "swpc_host_write_sac",
+]
+
+
+def lib(build=True):
+    """Load libswpc_gb300.so (building it first when sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise SwpcError(-2, "CUDA library %s is missing; run openswpc_gb300.build.build()" % _build.LIB)
+    L = ctypes.CDLL(_build.LIB)
+    vp, i, d, fp, ip, dp = (ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_void_p)
+    L.swpc_gpu_create.argtypes = [ctypes.POINTER(Dims), ctypes.POINTER(vp)]
+    L.swpc_gpu_required_bytes.argtypes = [ctypes.POINTER(Dims)]
+    L.swpc_gpu_required_bytes.restype = ctypes.c_longlong
+    L.swpc_gpu_upload_medium.argtypes = [vp] + [fp] * 5 + [ip] * 6 + [dp]
+    L.swpc_gpu_set_sources.argtypes = [vp, i, ip, dp, dp, dp, dp, i, i]
+    L.swpc_gpu_set_receivers.argtypes = [vp, i, ip, i, i]
+    L.swpc_gpu_set_snapshot.argtypes = [vp, i, i, i, i, i]
+    L.swpc_gpu_step.argtypes = [vp, i]
+    L.swpc_gpu_run.argtypes = [vp, i, i]
+    L.swpc_gpu_sync.argtypes = [vp]
+    L.swpc_gpu_fetch_waveforms.argtypes = [vp, i, fp]
+    L.swpc_gpu_fetch_snapshot.argtypes = [vp, i, i, fp]
+    L.swpc_gpu_query.argtypes = [vp, ip, ip, ip, ip, ip]
+    L.swpc_gpu_vmax.argtypes = [vp, fp]
+    L.swpc_gpu_fetch_field.argtypes = [vp, i, dp]
+    L.swpc_gpu_profile.argtypes = [vp, i]
+    L.swpc_gpu_profile_read.argtypes = [vp, dp, ip]
+    L.swpc_gpu_stream.argtypes = [vp]
+    L.swpc_gpu_stream.restype = vp
+    L.swpc_gpu_launch_count.argtypes = [vp]
+    L.swpc_gpu_launch_count.restype = ctypes.c_longlong
+    L.swpc_gpu_destroy.argtypes = [vp]
+    L.swpc_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.swpc_host_prepare.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.swpc_host_write_sac.argtypes = [vp, ctypes.c_char_p]
+    if hasattr(L, "swpc_host_nt"):
+        L.swpc_host_nt.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(2048)
+    lib().swpc_gpu_last_error(buf, 2048)
+    return buf.value.decode(errors="replace")
+
+
+def _ck(rc):
+    if rc != 0:
+        raise SwpcError(rc, last_error())
+    return rc
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xbeg=0.0, ybeg=0.0, zbeg=0.0,
+              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0):
+    d = Dims()
+    d.nx, d.ny, d.nz, d.nt, d.na, d.nm = nx, ny, nz, nt, na, 3
+    d.abc_type = 0 if abc == "pml" else 1
+    d.store = STORE[store]
+    d.dx, d.dy, d.dz, d.dt = dx, dy, dz, dt
+    d.xbeg, d.ybeg, d.zbeg, d.tbeg = xbeg, ybeg, zbeg, tbeg
+    d.fcut, d.M0, d.UC, d.ntdec_r = fcut, M0, UC, ntdec_r
+    return d
+
+
+def required_bytes(dims):
+    return int(lib().swpc_gpu_required_bytes(ctypes.byref(dims)))
+
+
+class Simulation:
+    """One swpc_3d simulation resident on the current CUDA device."""
+
+    def __init__(self, dims=None, handle=None):
+        self._h = ctypes.c_void_p()
+        if handle is not None:
+            self._h = handle
+        else:
+            _ck(lib().swpc_gpu_create(ctypes.byref(dims), ctypes.byref(self._h)))
+        self.dims = dims
+        self._keep = []
+
+    @classmethod
+    def from_inf(cls, inf_path):
+        h = ctypes.c_void_p()
+        _ck(lib().swpc_host_prepare(os.fsencode(os.path.abspath(inf_path)), ctypes.byref(h)))
+        return cls(handle=h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def upload_medium(self, rho, lam, mu, taup, taus, kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts):
+        f = [np.ascontiguousarray(a, np.float32) for a in (rho, lam, mu, taup, taus)]
+        m = [np.ascontiguousarray(a, np.int32) for a in (kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot)]
+        t = np.ascontiguousarray(ts, np.float64)
+        _ck(lib().swpc_gpu_upload_medium(self._h, *[_ptr(a) for a in f], *[_ptr(a) for a in m], _ptr(t)))
+
+    def set_sources(self, ijk, prm, mo=None, mij=None, fxyz=None, stftype="kupper", bf_mode=False):
+        ijk = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
+        n = ijk.shape[0]
+        prm = np.ascontiguousarray(prm, np.float64).reshape(n, 2)
+        mo = None if mo is None else np.ascontiguousarray(mo, np.float64).reshape(n)
+        mij = None if mij is None else np.ascontiguousarray(mij, np.float64).reshape(n, 6)
+        fxyz = None if fxyz is None else np.ascontiguousarray(fxyz, np.float64).reshape(n, 3)
+        stf = STF[stftype] if isinstance(stftype, str) else int(stftype)
+        _ck(lib().swpc_gpu_set_sources(self._h, n, _ptr(ijk), _ptr(mo), _ptr(mij), _ptr(fxyz), _ptr(prm), stf,
+                                       int(bool(bf_mode))))
+
+    def set_receivers(self, ijk, ntdec_w=1, flags=SWPC_WAV_V):
+        ijk = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
+        _ck(lib().swpc_gpu_set_receivers(self._h, ijk.shape[0], _ptr(ijk), int(ntdec_w), int(flags)))
+
+    def set_snapshot(self, kinds, k0, idec=1, jdec=1, ntdec_s=10):
+        _ck(lib().swpc_gpu_set_snapshot(self._h, int(kinds), int(k0), int(idec), int(jdec), int(ntdec_s)))
+
+    def step(self, it):
+        _ck(lib().swpc_gpu_step(self._h, int(it)))
+
+    def run(self, it0, it1):
+        _ck(lib().swpc_gpu_run(self._h, int(it0), int(it1)))
+
+    def sync(self):
+        _ck(lib().swpc_gpu_sync(self._h))
+
+    def query(self):
+        v = np.zeros(5, np.int32)
+        _ck(lib().swpc_gpu_query(self._h, *[v[q:].ctypes.data for q in range(5)]))
+        return dict(ntw=int(v[0]), nst=int(v[1]), nxs=int(v[2]), nys=int(v[3]), nframes=int(v[4]))
+
+    def waveforms(self, kind=SWPC_WAV_V):
+        q = self.query()
+        nc = 3 if kind in (SWPC_WAV_V, SWPC_WAV_U) else 6
+        out = np.zeros((q["nst"], nc, q["ntw"]), np.float32)
+        _ck(lib().swpc_gpu_fetch_waveforms(self._h, int(kind), out.ctypes.data))
+        return out
+
+    def snapshot(self, kind, frame):
+        q = self.query()
+        out = np.zeros((3, q["nys"], q["nxs"]), np.float32)
+        _ck(lib().swpc_gpu_fetch_snapshot(self._h, int(kind), int(frame), out.ctypes.data))
+        return out
+
+    def field(self, name):
+        d = self.dims
+        if d is None:
+            raise SwpcError(-1, "field() needs the dims the simulation was created with")
+        out = np.zeros((d.ny, d.nx, d.nz), np.float64)
+        _ck(lib().swpc_gpu_fetch_field(self._h, FIELDS.index(name), out.ctypes.data))
+        return out
+
+    def vmax(self):
+        out = np.zeros(3, np.float32)
+        _ck(lib().swpc_gpu_vmax(self._h, out.ctypes.data))
+        return out
+
+    def profile(self, enable=True):
+        _ck(lib().swpc_gpu_profile(self._h, int(enable)))
+
+    def profile_read(self):
+        ms = np.zeros(6, np.float64)
+        n = np.zeros(6, np.int64)
+        _ck(lib().swpc_gpu_profile_read(self._h, ms.ctypes.data, n.ctypes.data))
+        return ms, n
+
+    def stream(self):
+        return lib().swpc_gpu_stream(self._h)
+
+    def launch_count(self):
+        return int(lib().swpc_gpu_launch_count(self._h))
+
+    def write_sac(self, odir=None):
+        _ck(lib().swpc_host_write_sac(self._h, os.fsencode(odir) if odir else None))
+
+    def close(self):
+        if self._h:
+            lib().swpc_gpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

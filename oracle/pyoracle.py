@@ -1,0 +1,164 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle is a C++ restatement of OpenSWPC's swpc_3d time loop
+(oracle/swpc_oracle.cpp).  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline legs load it; the product (openswpc_gb300) never does.
+"""
+import ctypes
+import os
+import subprocess
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "swpc_oracle.cpp")
+
+# -ffp-contract=off and no fast-math keep the restatement's rounding
+# deterministic and close to the reference's scalar evaluation order.
+CXXFLAGS = ["-O2", "-fno-fast-math", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c++17"]
+
+MODES = {"fp32": 0, "mixed": 1, "fp64": 2}
+FIELDS = ["Vx", "Vy", "Vz", "Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"]
+MEDIA = ["rho", "lam", "mu", "taup", "taus", "kfs", "kob", "kfs_top", "kfs_bot", "kob_top", "kob_bot", "ts"]
+
+
+def build(force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        tmp = LIB + ".tmp"
+        subprocess.check_call(["g++", *CXXFLAGS, "-o", tmp, SRC])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp = ctypes.c_void_p
+        L.oracle_create.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(vp)]
+        L.oracle_last_error.restype = ctypes.c_char_p
+        L.oracle_run.argtypes = [vp, ctypes.c_int]
+        L.oracle_info.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_waveforms.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_stations.argtypes = [vp, ctypes.c_void_p]
+        L.oracle_field.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_medium.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_vmax.argtypes = [vp, ctypes.c_void_p]
+        L.oracle_snap_xy_v.argtypes = [vp, ctypes.c_void_p]
+        L.oracle_destroy.argtypes = [vp]
+        L.oracle_sources.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_stf.argtypes = [vp]
+        L.oracle_momentrate.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
+        L.oracle_momentrate.restype = ctypes.c_float
+        L.oracle_sdr2moment.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """One oracle simulation built from an input.inf file."""
+
+    def __init__(self, inf_path, mode="fp32", nthreads=0, medium=None):
+        L = lib()
+        h = ctypes.c_void_p()
+        vm = None
+        if medium is not None:
+            vm = np.ascontiguousarray(medium, dtype=np.float32)
+        rc = L.oracle_create(os.fsencode(inf_path), MODES[mode], int(nthreads),
+                             vm.ctypes.data if vm is not None else None, ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError("oracle: " + L.oracle_last_error().decode())
+        self.h = h
+        self._keep = vm
+        self.refresh()
+
+    def refresh(self):
+        ints = np.zeros(16, np.int32)
+        reals = np.zeros(16, np.float64)
+        lib().oracle_info(self.h, ints.ctypes.data, reals.ctypes.data)
+        (self.nx, self.ny, self.nz, self.nt, self.na, self.nst, self.ntw, self.nt_done,
+         self.nxs, self.nys, self.k0_xy, self.nvmax, self.nsnap) = [int(v) for v in ints[:13]]
+        self.M0, self.UC, self.fcut = [float(v) for v in reals[:3]]
+        self.dx, self.dy, self.dz, self.dt, self.xbeg, self.ybeg, self.zbeg, self.tbeg = [float(v) for v in reals[3:11]]
+        self.ntdec_w, self.ntdec_r, self.bf_mode = int(ints[13]), int(ints[14]), bool(ints[15])
+
+    def run(self, n):
+        if lib().oracle_run(self.h, int(n)) != 0:
+            raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+        self.refresh()
+
+    def waveforms(self, kind=0):
+        ncmp = 3 if kind in (0, 1) else 6
+        out = np.zeros((self.nst, ncmp, self.ntw), np.float32)  # Fortran (ntw,ncmp,nst)
+        lib().oracle_waveforms(self.h, kind, out.ctypes.data)
+        return out
+
+    def stations(self):
+        out = np.zeros((self.nst, 3), np.int32)
+        lib().oracle_stations(self.h, out.ctypes.data)
+        return out
+
+    def field(self, name):
+        out = np.zeros((self.ny, self.nx, self.nz), np.float64)  # Fortran (nz,nx,ny)
+        if lib().oracle_field(self.h, FIELDS.index(name), out.ctypes.data) != 0:
+            raise RuntimeError(lib().oracle_last_error().decode())
+        return out
+
+    def medium(self, name):
+        w = MEDIA.index(name)
+        if w < 5:
+            out = np.zeros((self.ny + 6, self.nx + 6, self.nz + 6), np.float32)
+        elif w < 11:
+            out = np.zeros((self.ny + 6, self.nx + 6), np.float32)
+        else:
+            out = np.zeros(3, np.float32)
+        if lib().oracle_medium(self.h, w, out.ctypes.data) != 0:
+            raise RuntimeError(lib().oracle_last_error().decode())
+        return out if w < 5 or w == 11 else out.astype(np.int32)
+
+    def vmax_log(self):
+        out = np.zeros((self.nvmax, 4), np.float32)
+        lib().oracle_vmax(self.h, out.ctypes.data)
+        return out
+
+    def snap_xy_v(self):
+        out = np.zeros(self.nsnap, np.float32)
+        lib().oracle_snap_xy_v(self.h, out.ctypes.data)
+        return out.reshape(-1, 3, self.nys, self.nxs)
+
+    def sources(self):
+        n = lib().oracle_sources(self.h, None, None)
+        ijk = np.zeros((n, 3), np.int32)
+        vals = np.zeros((n, 12), np.float64)
+        lib().oracle_sources(self.h, ijk.ctypes.data, vals.ctypes.data)
+        return ijk, vals
+
+    def stf(self):
+        return lib().oracle_stf(self.h)
+
+    def close(self):
+        if self.h:
+            lib().oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def momentrate(t, stf, ts, tr):
+    return lib().oracle_momentrate(t, stf, ts, tr)
+
+
+def sdr2moment(strike, dip, rake):
+    m = np.zeros(6, np.float32)
+    lib().oracle_sdr2moment(strike, dip, rake, m.ctypes.data)
+    return m  # xx yy zz yz xz xy
