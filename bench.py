@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 swpc_3d time loop.
+
+Workload (the large single-source configuration): a 1024 x 1024 x 512 grid,
+dx = dy = dz = 0.25 km, dt = 0.01 s, nt = 4000, FP32 fields, nm = 3 Zener
+bodies over 0.05-5 Hz, 1-D gradient background (Vp 5 -> 7 km/s, Vs = Vp/1.73,
+rho = 1.74 Vp^0.25) with a seeded exponential von Karman perturbation
+(a = 5 km, 5 % rms), Qp/Qs = 600/300, free surface below 3 air cells, a 20-cell
+ADE-CFS PML on the other faces, one moment-tensor source at 15 km depth, 1024
+receivers on the free surface and an xy velocity snapshot every 100 steps.
+Inputs are synthetic (seeded); the reference names no public data set for
+this path.
+
+A step is one time step of the whole grid (stress update, PML, source,
+velocity update, PML, receiver and snapshot taps).  The metric is grid-point
+updates per second (nx*ny*nz per step).  The working set (~73 GB) is far
+larger than L2, so every step streams from HBM; no L2 flush is needed.
+
+`--impl reference` times the reference's CPU path (the C++ restatement in
+oracle/, built with the reference's -O2 -ffast-math -fopenmp flags, mixed
+precision as the reference's default MP = DP) on all host threads.
+
+Multi-GPU: the plain path does not shard (one domain per GPU); `--gpus N`
+under torchrun runs N independent replicas ("replicas only").
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAK_FALLBACK_GBS = 6800.0
+
+WORKLOADS = {
+    # name: grid, spacing, dt, nt, receivers, snapshot interval
+    "large": dict(nx=1024, ny=1024, nz=512, dx=0.25, dt=0.01, nt=4000, nst=1024, ntdec_s=100),
+    "mid": dict(nx=512, ny=512, nz=256, dx=0.5, dt=0.02, nt=3000, nst=256, ntdec_s=100),
+    "small": dict(nx=128, ny=128, nz=64, dx=0.5, dt=0.02, nt=1000, nst=16, ntdec_s=100),
+}
+
+# Algorithmic bytes per grid point and step (FP32 storage, nm = 3): every
+# state word read and written once, every medium word read once.
+#   viscoelastic interior: (3 V + 6 S + 18 R) x 2 + 5 medium = 59 words
+#   PML shell:             (3 V + 6 S + 18 ADE) x 2 + 3 medium = 57 words
+B_INT, B_PML = 236, 228
+# Per kernel (compulsory traffic of each kernel of the two-kernel schedule):
+#   stress interior: V read 3, lam mu taup taus 4, S RMW 12, R RMW 36 -> 55 words
+#   velocity interior: S read 6, rho 1, V RMW 6 -> 13 words
+KERNEL_BYTES = {"stress_interior": 220, "vel_interior": 52, "stress_pml": 140, "vel_pml": 124}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return PEAK_FALLBACK_GBS, "fallback"
+
+
+def counts(w):
+    nx, ny, nz, na = w["nx"], w["ny"], w["nz"], 20
+    n_int = (nx - 2 * na) * (ny - 2 * na) * (nz - na)
+    return n_int, nx * ny * nz - n_int
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx.append(float(c[2]))
+            except ValueError:
+                continue
+            for nme, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nme)
+        os.unlink(self.f.name)
+        if sm:
+            out = {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "samples": len(sm), "reasons": sorted(reasons)}
+        return out
+
+
+def make_medium(w, seed):
+    """Raw model over the halo grid, then the reference's medium
+    post-processing (FP64, swpc_host_medium)."""
+    from openswpc_gb300 import configs, gpu
+    nx, ny, nz, dx = w["nx"], w["ny"], w["nz"], w["dx"]
+    zbeg = -3 * dx
+    rho, lam, mu, qp, qs = configs.gradient_random_medium(nx, ny, nz, dx, zbeg, seed=seed)
+    qp = np.ascontiguousarray(qp)
+    qs = np.ascontiguousarray(qs)
+    taup, taus, maps, ts = gpu.host_medium(nx, ny, nz, 20, 0.05, 5.0, 1.0, rho, lam, mu, qp, qs)
+    return dict(rho=rho, lam=lam, mu=mu, taup=taup, taus=taus, maps=maps, ts=ts, zbeg=zbeg)
+
+
+def source_and_stations(w, med, seed):
+    rng = np.random.default_rng(seed + 1)
+    nx, ny, nz, dx = w["nx"], w["ny"], w["nz"], w["dx"]
+    zbeg = med["zbeg"]
+    ks = int(np.ceil((min(15.0, 0.6 * nz * dx) - zbeg) / dx))
+    src = np.array([[nx // 2, ny // 2, ks]], np.int32)
+    s, d, r = [np.deg2rad(v) for v in (rng.uniform(0, 360), rng.uniform(0, 90), rng.uniform(-180, 180))]
+    mij = np.array([[-(np.sin(d) * np.cos(r) * np.sin(2 * s) + np.sin(2 * d) * np.sin(r) * np.sin(s) ** 2),
+                     np.sin(d) * np.cos(r) * np.sin(2 * s) - np.sin(2 * d) * np.sin(r) * np.cos(s) ** 2,
+                     np.sin(2 * d) * np.sin(r),
+                     -(np.cos(d) * np.cos(r) * np.sin(s) - np.cos(2 * d) * np.sin(r) * np.cos(s)),
+                     -(np.cos(d) * np.cos(r) * np.cos(s) + np.cos(2 * d) * np.sin(r) * np.sin(s)),
+                     np.sin(d) * np.cos(r) * np.cos(2 * s) + 0.5 * np.sin(2 * d) * np.sin(r) * np.sin(2 * s)]])
+    kfs = med["maps"][0]
+    ii = rng.integers(26, nx - 25, w["nst"])
+    jj = rng.integers(26, ny - 25, w["nst"])
+    kk = kfs[jj + 2, ii + 2] + 1
+    sta = np.stack([ii, jj, kk], 1).astype(np.int32)
+    return src, mij, sta
+
+
+def build_sim(w, med, nt, store="fp32", ntdec_r=100):
+    from openswpc_gb300 import gpu
+    dims = gpu.make_dims(w["nx"], w["ny"], w["nz"], nt, w["dx"], w["dx"], w["dx"], w["dt"], na=20, store=store,
+                         xbeg=-w["nx"] * w["dx"] / 2, ybeg=-w["ny"] * w["dx"] / 2, zbeg=med["zbeg"], fcut=1.0,
+                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r)
+    sim = gpu.Simulation(dims)
+    m = med["maps"]
+    sim.upload_medium(med["rho"], med["lam"], med["mu"], med["taup"], med["taus"], m[0], m[1], m[2], m[3], m[4], m[5],
+                      med["ts"])
+    src, mij, sta = med["src"], med["mij"], med["sta"]
+    sim.set_sources(src, np.array([[0.0, 1.0]]), mo=np.array([1.0]), mij=mij, stftype="kupper")
+    sim.set_receivers(sta, ntdec_w=1, flags=gpu.SWPC_WAV_V)
+    z0 = int(np.ceil((0.25 - med["zbeg"]) / w["dx"]))
+    sim.set_snapshot(gpu.SWPC_SNAP_XY_V, z0, 1, 1, w["ntdec_s"])
+    return sim
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def reduce_max(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample(steps=8, warmup=2, n=(512, 512, 256), dx=0.5, dt=0.02, mode="mixed", seed=20261203):
+    """The reference's CPU path (oracle restatement, -O2 -ffast-math -fopenmp,
+    all host threads) on a bounded sample of the workload: the same medium
+    construction on a smaller grid."""
+    from openswpc_gb300 import configs
+    from oracle import pyoracle
+    pyoracle.use_fast_build()
+    nx, ny, nz = n
+    with tempfile.TemporaryDirectory() as d:
+        inf = configs.write_plain_small(d, nt=steps + warmup, nx=nx, ny=ny, nz=nz, dx=dx, dy=dx, dz=dx, dt=dt,
+                                        xbeg=-nx * dx / 2, ybeg=-ny * dx / 2, zbeg=-3 * dx, sw_wav_v=False)
+        rho, lam, mu, qp, qs = configs.gradient_random_medium(nx, ny, nz, dx, -3 * dx, seed=seed)
+        vm = np.stack([rho, lam, mu, np.ascontiguousarray(qp), np.ascontiguousarray(qs)])
+        del rho, lam, mu, qp, qs
+        cores = os.cpu_count() or 1
+        o = pyoracle.Oracle(inf, mode, cores, medium=vm)
+        del vm
+        o.run(warmup)
+        t = time.perf_counter()
+        o.run(steps)
+        el = time.perf_counter() - t
+        o.close()
+    return dict(value=nx * ny * nz * steps / el, unit="pt/s", cores=cores, kind="port",
+                sample="%dx%dx%d grid of the same medium model, %d timed steps after %d warm-up, %s precision"
+                       % (nx, ny, nz, steps, warmup, mode),
+                seconds=el)
+
+
+def run_reference(args, w):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    cb = cpu_sample(steps=args.steps, warmup=args.warmup)
+    line = {
+        "metric": "grid-pt updates/s", "value": cb["value"], "unit": "pt/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * cb["seconds"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64/f32 (mixed, reference default)", "data": "synthetic",
+        "config": {"workload": "large single source 1024x1024x512 (bounded CPU sample)", "sample": cb["sample"],
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": cb["value"], "unit": "pt/s", "cores": cb["cores"], "kind": "port",
+                         "sample": cb["sample"]},
+        "e2e": {"value": cb["value"], "unit": "pt/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, w):
+    world, rank, local = dist_init()
+    from openswpc_gb300 import gpu
+    import torch
+    torch.cuda.set_device(local)
+    gpu.lib()
+    peak, peak_kind = peaks()
+    seed = 20261203 + 7 * rank
+    t_setup = time.time()
+    med = make_medium(w, seed)
+    med["src"], med["mij"], med["sta"] = source_and_stations(w, med, seed)
+    sim = build_sim(w, med, w["nt"])
+    stream = torch.cuda.ExternalStream(sim.stream())
+    t_setup = time.time() - t_setup
+
+    it = 1
+    sim.run(it, it + args.warmup - 1)
+    it += args.warmup
+    sim.sync()
+    # timed region: per-kernel CUDA events on the simulation's stream
+    sim.profile(True)
+    n0 = sim.launch_count()
+    clk = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clk.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.run(it, it + args.steps - 1)
+    e1.record(stream)
+    it += args.steps
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    launches = sim.launch_count() - n0
+    kms, kn = sim.profile_read()
+    sim.profile(False)
+    sim.sync()
+    ms_max = reduce_max(ms, world)
+    npt = w["nx"] * w["ny"] * w["nz"]
+    value = world * npt * args.steps / (ms_max / 1e3)
+    n_int, n_pml = counts(w)
+    step_bytes = B_INT * n_int + B_PML * n_pml
+    names = ["stress_interior", "vel_interior", "stress_pml", "vel_pml"]
+    kavg = {nm: float(kms[q] / max(kn[q], 1)) for q, nm in enumerate(names)}
+    units = {"stress_interior": n_int, "vel_interior": n_int, "stress_pml": n_pml, "vel_pml": n_pml}
+    kern = {nm: {"ms": kavg[nm], "GBps": KERNEL_BYTES[nm] * units[nm] / (kavg[nm] / 1e3) / 1e9 if kavg[nm] > 0 else None,
+                 "share": float(kms[q] / max(kms[:4].sum(), 1e-12))} for q, nm in enumerate(names)}
+    top = "stress_interior"
+    achieved = kern[top]["GBps"]
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            with open(tp) as f:
+                traffic = json.load(f).get(top + "_bytes_per_launch")
+        except Exception:
+            traffic = None
+    sim.close()
+    del stream
+
+    # end to end through the C ABI: create + upload from pinned host memory +
+    # K steps + waveform read-back + destroy
+    e2e = None
+    if not args.no_e2e:
+        pin = {}
+        for k in ("rho", "lam", "mu", "taup", "taus"):
+            t = torch.empty(med[k].shape, dtype=torch.float32, pin_memory=True)
+            t.numpy()[...] = med[k]
+            pin[k] = t
+        med_p = dict(med)
+        for k in pin:
+            med_p[k] = pin[k].numpy()
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim2 = build_sim(w, med_p, args.steps)
+        sim2.run(1, args.steps)
+        wav = sim2.waveforms()
+        sim2.close()
+        t1 = time.perf_counter()
+        e_s = reduce_max(t1 - t0, world)
+        h2d = sum(int(med[k].nbytes) for k in ("rho", "lam", "mu", "taup", "taus")) + sum(int(m.nbytes) for m in med["maps"])
+        e2e = {"value": world * npt * args.steps / e_s, "unit": "pt/s",
+               "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": int(wav.nbytes) // args.steps,
+               "job": "create + upload_medium (pinned host) + %d steps + fetch_waveforms + destroy" % args.steps,
+               "seconds": e_s}
+        del pin, med_p
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cb = cpu_sample()
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {
+            "metric": "grid-pt updates/s", "value": value, "unit": "pt/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "large single source %dx%dx%d" % (w["nx"], w["ny"], w["nz"]),
+                       "dx_km": w["dx"], "dt_s": w["dt"], "nt": w["nt"], "nm": 3, "na": 20, "receivers": w["nst"],
+                       "snapshot": "xy_v every %d steps" % w["ntdec_s"], "parallelism": "replicas x%d" % world,
+                       "l2": "inputs larger than L2 (%.0f GB working set), no flush" % (gpu.required_bytes(
+                           gpu.make_dims(w["nx"], w["ny"], w["nz"], w["nt"], w["dx"], w["dx"], w["dx"], w["dt"])) / 1e9)},
+            "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
+                                  "peak": peak, "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak,
+                                  "model": "236 B/interior pt + 228 B/PML pt per step"},
+            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "traffic": traffic,
+                         "bytes_per_point": KERNEL_BYTES[top], "peak_source": peak_kind},
+            "kernels": kern,
+            "clocks": clocks,
+            "gpu_launches": launches,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "setup_s": t_setup,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_gpu(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -165,6 +165,26 @@ int swpc_gpu_last_error(char* buf, size_t n);
  * inf_path. */
 int swpc_host_prepare(const char* inf_path, swpc_sim** out);
 
+/* Run the whole host set-up of swpc_host_prepare without touching a GPU and
+ * write a JSON summary (grid, M0, fcut, relaxation times, source and station
+ * grid indices) into summary.  Returns the summary length or a negative
+ * error code. */
+int swpc_host_check(const char* inf_path, char* summary, size_t n);
+
+/* Number of time steps nt read from input.inf by swpc_host_prepare (0 if the
+ * simulation was not made by it). */
+int swpc_host_nt(swpc_sim* sim);
+
+/* Medium post-processing of medium__setup (m_medium.f90:124-394) in FP64 for
+ * hosts that bring their own velocity model.  On entry rho, lam, mu, qp_taup
+ * and qs_taus hold density, unrelaxed moduli and Qp, Qs over the halo grid;
+ * on return the absorber band is homogenised, lam/mu are relaxed to fq_ref,
+ * qp_taup/qs_taus hold the tau-method ratios, the six surface maps are
+ * filled and ts[3] holds the relaxation times.  Host memory only. */
+int swpc_host_medium(int nx, int ny, int nz, int na, double fq_min, double fq_max, double fq_ref,
+                     float* rho, float* lam, float* mu, float* qp_taup, float* qs_taus,
+                     int* kfs, int* kob, int* kfs_top, int* kfs_bot, int* kob_top, int* kob_bot, double* ts);
+
 /* Write the receiver traces as SAC files named
  * odir/wav/<title>.3d.<station>.<cmp>.sac (m_wav.f90:782-792). */
 int swpc_host_write_sac(swpc_sim* sim, const char* odir);

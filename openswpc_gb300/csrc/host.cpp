@@ -1,13 +1,813 @@
-// host.cpp -- host driver layer (input files -> prepared simulation).
-#include "../../include/swpc_gpu.h"
+// host.cpp -- host driver layer: the reference's host-side set-up chain
+// (src/swpc_3d/main.f90:48-116) rebuilt in C++ with FP64 arithmetic, feeding
+// the device library through the C ABI of include/swpc_gpu.h, plus SAC
+// output of the receiver traces.
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <stdexcept>
 #include <string>
-namespace swpc { int set_err(int code, const std::string& msg); }
-extern "C" int swpc_host_prepare(const char* inf_path, swpc_sim** out) {
-    (void)inf_path; if (out) *out = nullptr;
-    return swpc::set_err(SWPC_E_STATE, "host driver layer not built yet");
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/swpc_gpu.h"
+
+namespace swpc {
+int set_err(int code, const std::string& msg);
 }
-extern "C" int swpc_host_write_sac(swpc_sim* sim, const char* odir) {
-    (void)sim; (void)odir;
-    return swpc::set_err(SWPC_E_STATE, "host driver layer not built yet");
+
+namespace {
+
+const double PI = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// input.inf reader (semantics of src/shared/m_readini.f90:29-166): the first
+// non-comment line whose text starts with the key followed by '=' wins; the
+// value is the first list-directed item; ${VAR} is expanded.
+// ---------------------------------------------------------------------------
+std::string ltrim(const std::string& s) {
+    size_t p = s.find_first_not_of(" \t\r");
+    return p == std::string::npos ? std::string() : s.substr(p);
 }
-extern "C" int swpc_host_nt(swpc_sim* sim) { (void)sim; return 0; }
+
+struct Inf {
+    std::vector<std::string> lines;
+    std::string dir;
+    bool strict = false;
+    explicit Inf(const std::string& path) {
+        std::ifstream f(path);
+        if (!f) throw std::runtime_error("cannot open " + path);
+        for (std::string s; std::getline(f, s);) lines.push_back(s);
+        size_t sl = path.find_last_of('/');
+        dir = sl == std::string::npos ? "." : path.substr(0, sl);
+    }
+    static std::string item(const std::string& v0) {
+        std::string v = ltrim(v0);
+        if (v.empty()) return v;
+        if (v[0] == '\'' || v[0] == '"') {
+            size_t e = v.find(v[0], 1);
+            return v.substr(1, e == std::string::npos ? std::string::npos : e - 1);
+        }
+        size_t e = v.find_first_of(" \t,/\r");
+        return v.substr(0, e);
+    }
+    bool find(const std::string& key, std::string& out) const {
+        for (const auto& l0 : lines) {
+            std::string l = ltrim(l0);
+            if (l.empty() || l[0] == '#' || l[0] == '!') continue;
+            if (l.compare(0, key.size(), key) != 0) continue;
+            std::string r = ltrim(l.substr(key.size()));
+            if (r.empty() || r[0] != '=') continue;
+            out = item(r.substr(1));
+            for (size_t p; (p = out.find("${")) != std::string::npos;) {
+                size_t e = out.find('}', p);
+                if (e == std::string::npos) break;
+                const char* ev = std::getenv(out.substr(p + 2, e - p - 2).c_str());
+                out = out.substr(0, p) + (ev ? ev : "") + out.substr(e + 1);
+            }
+            return true;
+        }
+        if (strict) throw std::runtime_error("key " + key + " is not found (strict_mode)");
+        return false;
+    }
+    static double num(std::string s) {
+        for (auto& c : s) if (c == 'd' || c == 'D') c = 'e';
+        char* e = nullptr;
+        double v = std::strtod(s.c_str(), &e);
+        if (e == s.c_str()) throw std::runtime_error("not a number: '" + s + "'");
+        return v;
+    }
+    double r(const std::string& k, double d) const { std::string v; return find(k, v) ? num(v) : d; }
+    int i(const std::string& k, int d) const { std::string v; return find(k, v) ? (int)std::lround(num(v)) : d; }
+    std::string s(const std::string& k, const std::string& d) const { std::string v; return find(k, v) ? v : d; }
+    bool b(const std::string& k, bool d) const {
+        std::string v;
+        if (!find(k, v)) return d;
+        size_t p = (!v.empty() && v[0] == '.') ? 1 : 0;
+        if (p >= v.size()) return d;
+        char c = (char)std::tolower((unsigned char)v[p]);
+        if (c != 't' && c != 'f') throw std::runtime_error("not a logical value for " + k + ": '" + v + "'");
+        return c == 't';
+    }
+    std::string path(const std::string& f) const { return (f.empty() || f[0] == '/') ? f : dir + "/" + f; }
+};
+
+std::vector<std::string> table_rows(const std::string& path) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::vector<std::string> rows;
+    for (std::string s; std::getline(f, s);) {
+        std::string t = ltrim(s);
+        if (t.empty() || t[0] == '#') continue;
+        if (t.find_first_not_of(" \t\r") == std::string::npos) continue;
+        rows.push_back(t);
+    }
+    return rows;
+}
+std::vector<std::string> split(const std::string& s) {
+    std::vector<std::string> v;
+    std::string cur;
+    bool q = false;
+    char qc = 0;
+    for (char c : s) {
+        if (q) { if (c == qc) q = false; else cur += c; continue; }
+        if (c == '\'' || c == '"') { q = true; qc = c; continue; }
+        if (c == ' ' || c == '\t' || c == ',' || c == '\r') { if (!cur.empty()) { v.push_back(cur); cur.clear(); } continue; }
+        cur += c;
+    }
+    if (!cur.empty()) v.push_back(cur);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Krueger (transverse Mercator, GRS80, scale 0.9999) -- Krueger's
+// n-series as published by Karney (2011, J. Geodesy 85:475) and used by the
+// Japanese plane rectangular system; x to the north, y to the east, km.
+// ---------------------------------------------------------------------------
+struct GK {
+    double a = 6378137.0, f = 298.257222101, k0 = 0.9999, n;
+    double al[6], be[6], de[7], A[6];
+    GK() {
+        n = 1.0 / (2.0 * f - 1.0);
+        const double n2 = n * n, n3 = n2 * n, n4 = n3 * n, n5 = n4 * n, n6 = n5 * n;
+        al[1] = n / 2 - 2 * n2 / 3 + 5 * n3 / 16 + 41 * n4 / 180 - 127 * n5 / 288;
+        al[2] = 13 * n2 / 48 - 3 * n3 / 5 + 557 * n4 / 1440 + 281 * n5 / 630;
+        al[3] = 61 * n3 / 240 - 103 * n4 / 140 + 15061 * n5 / 26880;
+        al[4] = 49561 * n4 / 161280 - 179 * n5 / 168;
+        al[5] = 34729 * n5 / 80640;
+        be[1] = n / 2 - 2 * n2 / 3 + 37 * n3 / 96 - n4 / 360 - 81 * n5 / 512;
+        be[2] = n2 / 48 + n3 / 15 - 437 * n4 / 1440 + 46 * n5 / 105;
+        be[3] = 17 * n3 / 480 - 37 * n4 / 840 - 209 * n5 / 4480;
+        be[4] = 4397 * n4 / 161280 - 11 * n5 / 504;
+        be[5] = 4583 * n5 / 161280;
+        de[1] = 2 * n - 2 * n2 / 3 - 2 * n3 + 116 * n4 / 45 + 26 * n5 / 45 - 2854 * n6 / 675;
+        de[2] = 7 * n2 / 3 - 8 * n3 / 5 - 227 * n4 / 45 + 2704 * n5 / 315 + 2323 * n6 / 945;
+        de[3] = 56 * n3 / 15 - 136 * n4 / 35 - 1262 * n5 / 105 + 73814 * n6 / 2835;
+        de[4] = 4279 * n4 / 630 - 332 * n5 / 35 - 399572 * n6 / 14175;
+        de[5] = 4174 * n5 / 315 - 144838 * n6 / 6237;
+        de[6] = 601676 * n6 / 22275;
+        A[0] = 1 + n2 / 4 + n4 / 64;
+        A[1] = -1.5 * (n - n3 / 8 - n5 / 64);
+        A[2] = 15.0 / 16 * (n2 - n4 / 4);
+        A[3] = -35.0 / 48 * (n3 - 5 * n5 / 16);
+        A[4] = 315.0 / 512 * n4;
+        A[5] = -693.0 / 1280 * n5;
+    }
+    double meridian(double phi0) const {  // scaled meridian arc length to latitude phi0
+        double s = A[0] * phi0;
+        for (int j = 1; j <= 5; ++j) s += A[j] * std::sin(2 * j * phi0);
+        return k0 * a / (1 + n) * s;
+    }
+    void ll2xy(double lon, double lat, double lon0, double lat0, double& x, double& y) const {
+        const double lam = lon * PI / 180, lam0 = lon0 * PI / 180, phi = lat * PI / 180, phi0 = lat0 * PI / 180;
+        const double e2n = 2 * std::sqrt(n) / (1 + n);
+        const double t = std::sinh(std::atanh(std::sin(phi)) - e2n * std::atanh(e2n * std::sin(phi)));
+        const double c = std::sqrt(1 + t * t);
+        const double xi = std::atan2(t, std::cos(lam - lam0)), eta = std::atanh(std::sin(lam - lam0) / c);
+        double X = xi, Y = eta;
+        for (int j = 1; j <= 5; ++j) {
+            X += al[j] * std::sin(2 * j * xi) * std::cosh(2 * j * eta);
+            Y += al[j] * std::cos(2 * j * xi) * std::sinh(2 * j * eta);
+        }
+        const double Ab = k0 * a / (1 + n) * A[0];
+        x = (Ab * X - meridian(phi0)) / 1000;
+        y = Ab * Y / 1000;
+    }
+    void xy2ll(double x, double y, double lon0, double lat0, double& lon, double& lat) const {
+        const double phi0 = lat0 * PI / 180;
+        const double Ab = k0 * a / (1 + n) * A[0];
+        const double xi = (x * 1000 + meridian(phi0)) / Ab, eta = y * 1000 / Ab;
+        double X = xi, Y = eta;
+        for (int j = 1; j <= 5; ++j) {
+            X -= be[j] * std::sin(2 * j * xi) * std::cosh(2 * j * eta);
+            Y -= be[j] * std::cos(2 * j * xi) * std::sinh(2 * j * eta);
+        }
+        const double chi = std::asin(std::sin(X) / std::cosh(Y));
+        double phi = chi;
+        for (int j = 1; j <= 6; ++j) phi += de[j] * std::sin(2 * j * chi);
+        lon = lon0 + std::atan(std::sinh(Y) / std::cos(X)) * 180 / PI;
+        lat = phi * 180 / PI;
+    }
+};
+const GK gk;
+
+// src/shared/m_geomap.f90:16-64: azimuth phi rotates the local frame clockwise
+void g2c(double lon, double lat, double lon0, double lat0, double phi, double& x, double& y) {
+    double xx, yy, p = phi * PI / 180;
+    gk.ll2xy(lon, lat, lon0, lat0, xx, yy);
+    x = std::cos(p) * xx + std::sin(p) * yy;
+    y = -std::sin(p) * xx + std::cos(p) * yy;
+}
+void c2g(double x, double y, double lon0, double lat0, double phi, double& lon, double& lat) {
+    double p = phi * PI / 180;
+    gk.xy2ll(std::cos(p) * x - std::sin(p) * y, std::sin(p) * x + std::cos(p) * y, lon0, lat0, lon, lat);
+}
+
+// ---------------------------------------------------------------------------
+// Model and set-up state
+// ---------------------------------------------------------------------------
+struct Params {
+    std::string title, odir, abc_type, vmodel_type, stftype, stf_format, fn_stf, sdep_fit, st_format, fn_stloc, wav_format;
+    int nx, ny, nz, nt, na, ntdec_w, ntdec_r, ntdec_s, idec, jdec;
+    double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut, z0_xy;
+    bool bf_mode, sw_v, sw_u, sw_stress, sw_strain, xy_v, xy_u, munk;
+};
+
+struct Station { std::string name; double x, y, z, lon, lat; int i, j, k; };
+
+struct Meta {  // what the SAC writer needs after set-up
+    Params p;
+    std::vector<Station> st;
+    double M0 = 0, UC = 1e-15, evlo = 0, evla = 0, evdp = 0, sx0 = 0, sy0 = 0, otim = 0;
+    double m6[6] = {0, 0, 0, 0, 0, 0}, f3[3] = {0, 0, 0};
+    long long exedate = 0;
+    int ntw = 0, flags = 0;
+};
+std::mutex g_meta_mu;
+std::map<swpc_sim*, Meta> g_meta;
+
+struct Grid {  // Fortran halo-array geometry
+    int nx, ny, nz;
+    size_t n3() const { return (size_t)(nz + 6) * (nx + 6) * (ny + 6); }
+    size_t idx(int k, int i, int j) const { return ((size_t)(j + 2) * (nx + 6) + (i + 2)) * (nz + 6) + (k + 2); }
+    size_t n2() const { return (size_t)(nx + 6) * (ny + 6); }
+    size_t idx2(int i, int j) const { return (size_t)(j + 2) * (nx + 6) + (i + 2); }
+};
+
+double seawater_vel(double z, bool munk) {  // src/shared/m_seawater.f90:34-47
+    double eps = munk ? 0.00737 : 0.0, zc = 1300.0, zb = 2 * (z * 1000. - zc) / zc;
+    return 1.5 * (1.0 + eps * (zb - 1.0 + std::exp(-zb)));
+}
+
+// velocity models (m_vmodel_uni.f90:40-149, m_vmodel_lhm.f90:21-169,
+// m_vmodel_lgm.f90:21-174); rho, lam, mu, Qp, Qs over the halo grid and
+// the topography depth bd0
+void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& rho, std::vector<float>& lam,
+            std::vector<float>& mu, std::vector<float>& qp, std::vector<float>& qs, double& bd0) {
+    const size_t n3 = G.n3();
+    rho.assign(n3, 0); lam.assign(n3, 0); mu.assign(n3, 0); qp.assign(n3, 0); qs.assign(n3, 0);
+    auto zc = [&](int k) { return p.zbeg + (k - 0.5) * p.dz; };
+    auto fill = [&](int k, double r, double vp, double vs, double q1, double q2) {
+        for (int j = -2; j <= p.ny + 3; ++j)
+            for (int i = -2; i <= p.nx + 3; ++i) {
+                size_t q = G.idx(k, i, j);
+                rho[q] = (float)r; mu[q] = (float)(r * vs * vs); lam[q] = (float)(r * (vp * vp - 2 * vs * vs));
+                qp[q] = (float)q1; qs[q] = (float)q2;
+            }
+    };
+    if (inf.b("earth_flattening", false)) throw std::runtime_error("earth_flattening is not supported by this build");
+    if (p.vmodel_type == "uni") {
+        double vp0 = inf.r("vp0", 5.0), vs0 = inf.r("vs0", vp0 / std::sqrt(3.0)), rho0 = inf.r("rho0", 2.7);
+        double qp0 = inf.r("qp0", 1e6), qs0 = inf.r("qs0", 1e6), topo0 = inf.r("topo0", 0.0);
+        bd0 = topo0;
+        for (int k = -2; k <= p.nz + 3; ++k) {
+            double z = zc(k);
+            if (z > topo0) fill(k, rho0, vp0, vs0, qp0, qs0);
+            else if (z > 0) fill(k, 1.0, seawater_vel(z, p.munk), 0, 1e6, 1e6);
+            else fill(k, 0.001, 0, 0, 10, 10);
+        }
+        return;
+    }
+    if (p.vmodel_type != "lhm" && p.vmodel_type != "lgm")
+        throw std::runtime_error("vmodel_type '" + p.vmodel_type + "' is not supported by this build (uni, lhm, lgm)");
+    auto rows = table_rows(inf.path(inf.s("fn_lhm", "")));
+    const int nl = (int)rows.size();
+    if (nl < 1) throw std::runtime_error("empty layer table");
+    std::vector<double> dep(nl), r0(nl), vp(nl), vs(nl), q1(nl), q2(nl);
+    for (int l = 0; l < nl; ++l) {
+        auto t = split(rows[l]);
+        if (t.size() < 6) throw std::runtime_error("bad layer line: " + rows[l]);
+        dep[l] = Inf::num(t[0]); r0[l] = Inf::num(t[1]); vp[l] = Inf::num(t[2]);
+        vs[l] = Inf::num(t[3]); q1[l] = Inf::num(t[4]); q2[l] = Inf::num(t[5]);
+    }
+    for (int l = nl - 2; l >= 0; --l)  // velocity cut-off
+        if ((vp[l] < p.vcut || vs[l] < p.vcut) && vp[l] > 0 && vs[l] > 0) {
+            vp[l] = vp[l + 1]; vs[l] = vs[l + 1]; r0[l] = r0[l + 1]; q1[l] = q1[l + 1]; q2[l] = q2[l + 1];
+        }
+    bd0 = dep[0];
+    for (int k = -2; k <= p.nz + 3; ++k) {
+        double z = zc(k);
+        if (z < dep[0]) {
+            if (z < 0) fill(k, 0.001, 0, 0, 10, 10);
+            else fill(k, 1.0, seawater_vel(z, p.munk), 0, 1e6, 1e6);
+            continue;
+        }
+        if (p.vmodel_type == "lhm") {
+            int L = 0;
+            for (int l = 0; l < nl; ++l) if (z >= dep[l]) L = l;
+            fill(k, r0[L], vp[L], vs[L], q1[L], q2[L]);
+        } else {
+            double R = r0[nl - 1], P = vp[nl - 1], S = vs[nl - 1], A = q1[nl - 1], B = q2[nl - 1];
+            for (int l = 0; l < nl - 1; ++l)
+                if (dep[l] <= z && z < dep[l + 1]) {
+                    double w = (z - dep[l]) / (dep[l + 1] - dep[l]);
+                    R = r0[l] + (r0[l + 1] - r0[l]) * w; P = vp[l] + (vp[l + 1] - vp[l]) * w; S = vs[l] + (vs[l + 1] - vs[l]) * w;
+                    A = q1[l] + (q1[l + 1] - q1[l]) * w; B = q2[l] + (q2[l + 1] - q2[l]) * w;
+                    break;
+                }
+            fill(k, R, P, S, A, B);
+        }
+    }
+}
+
+// src/shared/m_fdtool.f90:691-812 in FP64
+void relaxation_times(int nm, double fmin, double fmax, double* ts) {
+    double oa = 2 * PI * fmin, ob = 2 * PI * fmax;
+    if (nm == 1) { ts[0] = 1.0 / std::sqrt(oa * ob); return; }
+    for (int m = 0; m < nm; ++m) ts[m] = 1.0 / (oa * std::pow(ob / oa, (double)m / (nm - 1)));
+}
+double constq_zeta(int nm, double fmin, double fmax, const double* ts) {
+    double oa = 2 * PI * fmin, ob = 2 * PI * fmax, i0 = 0, i1 = 0, i2 = 0;
+    for (int m = 0; m < nm; ++m) {
+        double t = ts[m];
+        i0 += (std::log(1 + ob * ob * t * t) - std::log(1 + oa * oa * t * t)) / (2 * t);
+        i1 += ((std::atan(ob * t) - ob * t / (1 + ob * ob * t * t)) - (std::atan(oa * t) - oa * t / (1 + oa * oa * t * t))) / (2 * t);
+    }
+    for (int a = 0; a < nm - 1; ++a)
+        for (int b = a + 1; b < nm; ++b) {
+            double w1 = std::atan(ob * ts[a]) / ts[a] - std::atan(ob * ts[b]) / ts[b];
+            double w2 = std::atan(oa * ts[a]) / ts[a] - std::atan(oa * ts[b]) / ts[b];
+            i2 += ts[a] * ts[b] / (ts[b] * ts[b] - ts[a] * ts[a]) * (w1 - w2);
+        }
+    return i0 / (i1 + 2 * i2);
+}
+
+// src/swpc_3d/m_medium.f90:124-394 in FP64: absorber homogenisation,
+// tau-method, relaxation of the moduli to fq_ref, surface detection.
+void medium_post(int nx, int ny, int nz, int na, double fq_min, double fq_max, double fq_ref, float* rho, float* lam,
+                 float* mu, float* qp, float* qs, int* kfs, int* kob, int* kfs_top, int* kfs_bot, int* kob_top,
+                 int* kob_bot, double* ts) {
+    Grid G{nx, ny, nz};
+    float* F[5] = {rho, lam, mu, qp, qs};
+    auto cp = [&](int k, int i, int j, int ks, int is, int js) {
+        for (auto f : F) f[G.idx(k, i, j)] = f[G.idx(ks, is, js)];
+    };
+    for (int i = -2; i <= na; ++i)
+        for (int j = -2; j <= ny + 3; ++j) for (int k = -2; k <= nz + 3; ++k) cp(k, i, j, k, na + 1, j);
+    for (int i = nx - na + 1; i <= nx + 3; ++i)
+        for (int j = -2; j <= ny + 3; ++j) for (int k = -2; k <= nz + 3; ++k) cp(k, i, j, k, nx - na, j);
+    for (int j = -2; j <= na; ++j)
+        for (int i = -2; i <= nx + 3; ++i) for (int k = -2; k <= nz + 3; ++k) cp(k, i, j, k, i, na + 1);
+    for (int j = ny - na + 1; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) for (int k = -2; k <= nz + 3; ++k) cp(k, i, j, k, i, ny - na);
+    for (int j = -2; j <= ny + 3; ++j)
+        for (int i = -2; i <= nx + 3; ++i) for (int k = nz - na + 1; k <= nz + 3; ++k) cp(k, i, j, nz - na, i, j);
+    const int nm = 3;
+    relaxation_times(nm, fq_min, fq_max, ts);
+    const double zeta = constq_zeta(nm, fq_min, fq_max, ts);
+    std::complex<double> cc(0, 0);
+    const double om = 2 * PI * fq_ref;
+    for (int m = 0; m < nm; ++m) {
+        std::complex<double> iw(0, om * ts[m]);
+        cc += iw / (1.0 - iw);
+    }
+    cc /= (double)nm;
+    const size_t n3 = G.n3();
+    // chi depends on Q only; media hold few distinct Q values, so remember the last ones
+    float lq[2] = {-1.f, -1.f};
+    double lchi[2] = {0, 0};
+    auto chi = [&](int w, float q, double tau) {
+        if (q != lq[w]) { lq[w] = q; lchi[w] = 1.0 / (1.0 / std::sqrt(1.0 - cc * tau)).real(); }
+        return lchi[w];
+    };
+    for (size_t q = 0; q < n3; ++q) {
+        double tp = nm * zeta / (double)qp[q], tsv = nm * zeta / (double)qs[q];
+        double rb2 = mu[q], ra2 = (double)lam[q] + 2.0 * mu[q];
+        double chi_mu = chi(0, qs[q], tsv);
+        double chi_lam = chi(1, qp[q], tp);
+        double m2 = rb2 / (chi_mu * chi_mu);
+        mu[q] = (float)m2;
+        lam[q] = (float)(ra2 / (chi_lam * chi_lam) - 2 * m2);
+        qp[q] = (float)tp;
+        qs[q] = (float)tsv;
+    }
+    const float eps = 1.1920928955078125e-07f;
+    const size_t n2 = G.n2();
+    std::fill(kfs, kfs + n2, 0);
+    std::fill(kob, kob + n2, 0);
+    for (int j = 0; j <= ny + 2; ++j)
+        for (int i = 0; i <= nx + 2; ++i)
+            for (int k = 1; k <= nz - 1; ++k) {
+                if (std::fabs(mu[G.idx(k, i, j)]) < eps && std::fabs(mu[G.idx(k + 1, i, j)]) > eps) kob[G.idx2(i, j)] = k;
+                if (std::fabs(lam[G.idx(k, i, j)]) < eps && std::fabs(lam[G.idx(k + 1, i, j)]) > eps) kfs[G.idx2(i, j)] = k;
+            }
+    std::fill(kfs_top, kfs_top + n2, 0); std::fill(kfs_bot, kfs_bot + n2, 0);
+    std::fill(kob_top, kob_top + n2, 0); std::fill(kob_bot, kob_bot + n2, 0);
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            int a = 1 << 30, b = -(1 << 30), c = 1 << 30, d = -(1 << 30);
+            for (int jj = j - 2; jj <= j + 3; ++jj)
+                for (int ii = i - 2; ii <= i + 3; ++ii) {
+                    a = std::min(a, kfs[G.idx2(ii, jj)]); b = std::max(b, kfs[G.idx2(ii, jj)]);
+                    c = std::min(c, kob[G.idx2(ii, jj)]); d = std::max(d, kob[G.idx2(ii, jj)]);
+                }
+            kfs_top[G.idx2(i, j)] = std::max(a - 2, 1); kfs_bot[G.idx2(i, j)] = std::min(b + 2, nz);
+            kob_top[G.idx2(i, j)] = std::max(c - 2, 1); kob_bot[G.idx2(i, j)] = std::min(d + 2, nz);
+        }
+}
+
+// src/shared/m_fdtool.f90:307-336
+void sdr2moment(double strike, double dip, double rake, double* m6) {
+    const double r = PI / 180;
+    double sd = std::sin(dip * r), cd = std::cos(dip * r), s2d = std::sin(2 * dip * r), c2d = std::cos(2 * dip * r);
+    double sl = std::sin(rake * r), cl = std::cos(rake * r);
+    double sf = std::sin(strike * r), cf = std::cos(strike * r), s2f = std::sin(2 * strike * r), c2f = std::cos(2 * strike * r);
+    m6[0] = -(sd * cl * s2f + s2d * sl * sf * sf);   // xx
+    m6[1] = (sd * cl * s2f - s2d * sl * cf * cf);    // yy
+    m6[2] = (s2d * sl);                              // zz
+    m6[3] = -(cd * cl * sf - c2d * sl * cf);         // yz
+    m6[4] = -(cd * cl * cf + c2d * sl * sf);         // xz
+    m6[5] = (sd * cl * c2f + s2d * sl * s2f / 2);    // xy
+}
+
+int stf_code(const std::string& s) {
+    const char* names[] = {"boxcar", "triangle", "herrmann", "kupper", "cosine", "texp"};
+    for (int q = 0; q < 6; ++q) if (s == names[q]) return q;
+    if (s == "scosine") return 4;
+    return 3;
+}
+
+int x2i(double x, double beg, double d) { return (int)std::ceil((x - beg) / d); }
+
+void mkdirs(const std::string& d) {
+    std::string cur;
+    for (size_t p = 0; p <= d.size(); ++p) {
+        if (p == d.size() || d[p] == '/') {
+            if (!cur.empty()) mkdir(cur.c_str(), 0755);
+        }
+        if (p < d.size()) cur += d[p];
+    }
+}
+
+// SAC header + data (src/shared/m_sac.f90:267-449, header defaults :452-562)
+void write_sac(const std::string& fn, const Meta& m, const Station& st, const char* cmp, int idep, double cmpinc,
+               double cmpaz, const float* dat, int npts) {
+    float fh[70];
+    int ih[35], lh[5];
+    char kh[192];
+    for (auto& v : fh) v = -12345.0f;
+    for (auto& v : ih) v = -12345;
+    for (auto& v : lh) v = 0;
+    for (int q = 0; q < 24; ++q) std::memcpy(kh + 8 * q, "-12345  ", 8);
+    auto kset = [&](int word, int len, const std::string& s) {
+        std::string t = s.substr(0, len);
+        t.resize(len, ' ');
+        std::memcpy(kh + 4 * (word - 111), t.data(), len);
+    };
+    kset(113, 16, "-12345");  // kevnm is 16 characters
+    const Params& p = m.p;
+    double delta = p.ntdec_w * p.dt;
+    fh[0] = (float)((long long)(delta * 1e7)) / 1e7f;
+    fh[5] = (float)p.tbeg;
+    fh[7] = (float)m.otim;
+    fh[31] = (float)st.lat; fh[32] = (float)st.lon; fh[34] = (float)(st.z * 1000);
+    fh[35] = (float)m.evla; fh[36] = (float)m.evlo; fh[38] = (float)m.evdp;
+    fh[39] = m.M0 < 1.1920928955078125e-07 ? -12345.0f : (float)((std::log10(m.M0) - 9.1) * 2.0 / 3.0);
+    if (p.bf_mode) { fh[40] = (float)m.f3[0]; fh[41] = (float)m.f3[1]; fh[42] = (float)m.f3[2]; }
+    else {
+        fh[40] = (float)m.m6[0]; fh[41] = (float)m.m6[1]; fh[42] = (float)m.m6[2];
+        fh[43] = (float)m.m6[3]; fh[44] = (float)m.m6[4]; fh[45] = (float)m.m6[5];
+    }
+    fh[46] = (float)p.clon; fh[47] = (float)p.clat; fh[48] = (float)p.phi;
+    fh[50] = (float)std::sqrt((m.sx0 - st.x) * (m.sx0 - st.x) + (m.sy0 - st.y) * (m.sy0 - st.y));
+    fh[51] = (float)(std::atan2(st.y - m.sy0, st.x - m.sx0) * 180 / PI);
+    fh[52] = (float)(std::atan2(m.sy0 - st.y, m.sx0 - st.x) * 180 / PI);
+    fh[57] = (float)cmpaz; fh[58] = (float)cmpinc;
+    time_t tt = (time_t)m.exedate;
+    struct tm lt;
+    localtime_r(&tt, &lt);
+    ih[0] = lt.tm_year + 1900; ih[1] = lt.tm_yday + 1; ih[2] = lt.tm_hour; ih[3] = lt.tm_min; ih[4] = lt.tm_sec; ih[5] = 0;
+    ih[6] = 6;          // nvhdr
+    ih[9] = npts;       // npts
+    ih[15] = 1;         // iftype
+    ih[16] = idep;      // idep
+    lh[0] = 1;          // leven
+    lh[2] = 1;          // lovrok
+    kset(111, 8, st.name);
+    kset(113, 16, p.title.substr(0, 16));
+    kset(151, 8, cmp);
+    std::ofstream f(fn, std::ios::binary | std::ios::trunc);
+    if (!f) throw std::runtime_error("cannot write " + fn);
+    f.write((const char*)fh, sizeof fh);
+    f.write((const char*)ih, sizeof ih);
+    f.write((const char*)lh, sizeof lh);
+    f.write(kh, sizeof kh);
+    f.write((const char*)dat, (std::streamsize)npts * 4);
+}
+
+int prepare(const char* inf_path, swpc_sim** out, std::string* dry = nullptr) {
+    Inf inf(inf_path);
+    inf.strict = inf.b("strict_mode", false);
+    Params p;
+    if (inf.b("benchmark_mode", false)) throw std::runtime_error("benchmark_mode is not supported by this build");
+    p.title = inf.s("title", "swpc3d"); p.odir = inf.s("odir", "./out");
+    p.nx = inf.i("nx", 256); p.ny = inf.i("ny", 256); p.nz = inf.i("nz", 256); p.nt = inf.i("nt", 1000);
+    p.dx = inf.r("dx", 0.5); p.dy = inf.r("dy", 0.5); p.dz = inf.r("dz", 0.5); p.dt = inf.r("dt", 0.01);
+    p.na = inf.i("na", 20);
+    p.xbeg = inf.r("xbeg", -p.nx / 2 * p.dx); p.ybeg = inf.r("ybeg", -p.ny / 2 * p.dy); p.zbeg = inf.r("zbeg", -30 * p.dz);
+    p.tbeg = inf.r("tbeg", 0.0);
+    p.clon = inf.r("clon", 139.7604); p.clat = inf.r("clat", 35.7182); p.phi = inf.r("phi", 0.0);
+    p.abc_type = inf.s("abc_type", "pml");
+    if (p.abc_type != "pml" && p.abc_type != "cerjan") throw std::runtime_error("abc_type must be 'pml' or 'cerjan'");
+    p.fq_min = inf.r("fq_min", 0.05); p.fq_max = inf.r("fq_max", 5.0); p.fq_ref = inf.r("fq_ref", 1.0);
+    p.vmodel_type = inf.s("vmodel_type", "uni"); p.vcut = inf.r("vcut", 0.0);
+    p.munk = inf.b("munk_profile", false);
+    p.bf_mode = inf.b("bf_mode", false);
+    if (inf.b("pw_mode", false)) throw std::runtime_error("pw_mode is not supported by this build");
+    if (inf.b("green_mode", false)) throw std::runtime_error("green_mode is not supported by this build");
+    if (inf.b("stabilize_pml", false)) throw std::runtime_error("stabilize_pml is not supported by this build");
+    p.stftype = inf.s("stftype", "kupper"); p.stf_format = inf.s("stf_format", "xym0ij");
+    p.fn_stf = inf.s("fn_stf", ""); p.sdep_fit = inf.s("sdep_fit", "asis");
+    p.ntdec_w = inf.i("ntdec_w", 10); p.st_format = inf.s("st_format", "xy"); p.fn_stloc = inf.s("fn_stloc", "");
+    p.wav_format = inf.s("wav_format", "sac");
+    p.sw_v = inf.b("sw_wav_v", false); p.sw_u = inf.b("sw_wav_u", false);
+    p.sw_stress = inf.b("sw_wav_stress", false); p.sw_strain = inf.b("sw_wav_strain", false);
+    p.ntdec_r = inf.i("ntdec_r", 100);
+    p.xy_v = inf.b("xy_v%sw", false); p.xy_u = inf.b("xy_u%sw", false);
+    double zend = p.zbeg + p.nz * p.dz;
+    p.z0_xy = inf.r("z0_xy", std::max(std::min(10.0, zend), p.zbeg));
+    p.idec = inf.i("idec", 1); p.jdec = inf.i("jdec", 1); p.ntdec_s = inf.i("ntdec_s", 10);
+    for (const char* k : {"xy_ps%sw", "yz_ps%sw", "xz_ps%sw", "fs_ps%sw", "ob_ps%sw", "yz_v%sw", "xz_v%sw", "fs_v%sw",
+                          "ob_v%sw", "yz_u%sw", "xz_u%sw", "fs_u%sw", "ob_u%sw"})
+        if (inf.b(k, false)) std::fprintf(stderr, "swpc: snapshot %s is not produced by this build\n", k);
+    if (p.nt < 1) throw std::runtime_error("nt must be positive");
+
+    Grid G{p.nx, p.ny, p.nz};
+    std::vector<float> rho, lam, mu, tp, tsv;
+    double bd0 = 0;
+    vmodel(inf, p, G, rho, lam, mu, tp, tsv, bd0);
+    std::vector<int> kfs(G.n2()), kob(G.n2()), kft(G.n2()), kfb(G.n2()), kot(G.n2()), kobb(G.n2());
+    double ts[3];
+    medium_post(p.nx, p.ny, p.nz, p.na, p.fq_min, p.fq_max, p.fq_ref, rho.data(), lam.data(),
+                mu.data(), tp.data(), tsv.data(), kfs.data(), kob.data(), kft.data(), kfb.data(), kot.data(), kobb.data(), ts);
+
+    // sources (src/swpc_3d/m_source.f90:41-314, 468-774)
+    Meta meta;
+    meta.p = p;
+    meta.exedate = (long long)std::time(nullptr);
+    auto rows = table_rows(inf.path(p.fn_stf));
+    const std::string& f = p.stf_format;
+    struct S0 { double x, y, z, t0, tr, mo, m6[6], f3[3]; };
+    std::vector<S0> srcs;
+    for (size_t r = 0; r < rows.size(); ++r) {
+        auto t = split(rows[r]);
+        auto R = [&](size_t q) { if (q >= t.size()) throw std::runtime_error("short source line: " + rows[r]); return Inf::num(t[q]); };
+        S0 s{};
+        bool ll = f.size() >= 2 && f.compare(0, 2, "ll") == 0;
+        if (f == "psmeca") {
+            double lon = R(0), lat = R(1);
+            s.z = R(2);
+            double mzz = R(3), mxx = R(4), myy = R(5), mxz = R(6), myz = -R(7), mxy = -R(8);
+            int iex = (int)R(9);
+            g2c(lon, lat, p.clon, p.clat, p.phi, s.x, s.y);
+            double m0 = std::sqrt(mxx * mxx + myy * myy + mzz * mzz + 2 * (mxz * mxz + myz * myz + mxy * mxy)) / std::sqrt(2.0);
+            s.mo = m0 * std::pow(10.0, iex);
+            s.t0 = 0; s.tr = 2 * 1.05e-8 * std::pow(s.mo, 1.0 / 3.0);
+            s.mo *= 1e-7;
+            double m6[6] = {mxx, myy, mzz, myz, mxz, mxy};
+            for (int c = 0; c < 6; ++c) s.m6[c] = m6[c] / m0;
+        } else {
+            if (ll) { g2c(R(0), R(1), p.clon, p.clat, p.phi, s.x, s.y); }
+            else { s.x = R(0); s.y = R(1); }
+            s.z = R(2); s.t0 = R(3); s.tr = R(4);
+            if (p.bf_mode) {
+                if (!(f.compare(0, 2, "xy") == 0 || ll)) throw std::runtime_error("unknown body-force stf_format " + f);
+                s.f3[0] = R(5); s.f3[1] = R(6); s.f3[2] = R(7);
+            } else if (f == "xym0ij" || f == "llm0ij" || f == "xymwij" || f == "llmwij") {
+                s.mo = R(5);
+                if (f[2] == 'm' && f[3] == 'w') s.mo = std::pow(10.0, 1.5 * s.mo + 9.05);
+                for (int c = 0; c < 6; ++c) s.m6[c] = R(6 + c);
+            } else if (f == "xym0dc" || f == "llm0dc" || f == "xymwdc" || f == "llmwdc") {
+                s.mo = R(5);
+                if (f[2] == 'm' && f[3] == 'w') s.mo = std::pow(10.0, 1.5 * s.mo + 9.05);
+                sdr2moment(R(6) - p.phi, R(7), R(8), s.m6);
+            } else if (f == "xydsdc" || f == "lldsdc") {
+                double D = R(5), Sa = R(6);
+                sdr2moment(R(7) - p.phi, R(8), R(9), s.m6);
+                int is = x2i(s.x, p.xbeg, p.dx), js = x2i(s.y, p.ybeg, p.dy), ks = x2i(s.z, p.zbeg, p.dz);
+                s.mo = (is >= -2 && is <= p.nx + 3 && js >= -2 && js <= p.ny + 3 && ks >= -2 && ks <= p.nz + 3)
+                           ? 1e9 * mu[G.idx(ks, is, js)] * D * Sa : 0.0;
+            } else {
+                throw std::runtime_error("invalid source type " + f);
+            }
+        }
+        if (srcs.empty()) {
+            c2g(s.x, s.y, p.clon, p.clat, p.phi, meta.evlo, meta.evla);
+            meta.sx0 = s.x; meta.sy0 = s.y; meta.evdp = s.z; meta.otim = s.t0;
+            for (int c = 0; c < 6; ++c) meta.m6[c] = s.m6[c];
+            for (int c = 0; c < 3; ++c) meta.f3[c] = s.f3[c];
+        }
+        srcs.push_back(s);
+    }
+    if (srcs.empty()) throw std::runtime_error("no source grid in " + p.fn_stf);
+    double fcut = 0, M0 = 0;
+    for (auto& s : srcs) fcut = std::max(fcut, 1.0 / s.tr);
+    double UC = 1e-15;
+    if (p.bf_mode) {
+        for (auto& s : srcs) M0 += s.f3[0] * s.f3[0] + s.f3[1] * s.f3[1] + s.f3[2] * s.f3[2];
+        M0 = std::sqrt(M0);
+        UC *= 1e3;
+    } else {
+        for (auto& s : srcs) M0 += s.mo;
+    }
+    const double xend = p.xbeg + p.nx * p.dx, yend = p.ybeg + p.ny * p.dy;
+    std::vector<int> sijk;
+    std::vector<double> smo, smij, sf3, sprm;
+    for (auto& s : srcs) {
+        int is = x2i(s.x, p.xbeg, p.dx), js = x2i(s.y, p.ybeg, p.dy), ks = x2i(s.z, p.zbeg, p.dz);
+        if (p.sdep_fit.size() == 3 && p.sdep_fit.compare(0, 2, "bd") == 0 && p.sdep_fit[2] == '0') ks = x2i(bd0, p.zbeg, p.dz);
+        if (!(is >= -1 && is <= p.nx + 3 && js >= -1 && js <= p.ny + 3 && ks >= -1 && ks <= p.nz + 3)) continue;
+        if (!(p.xbeg <= s.x && s.x <= xend && p.ybeg <= s.y && s.y <= yend && p.zbeg <= s.z && s.z <= zend))
+            throw std::runtime_error("source outside the model space");
+        sijk.insert(sijk.end(), {is, js, ks});
+        smo.push_back(M0 > 0 ? s.mo / M0 : 0.0);
+        smij.insert(smij.end(), s.m6, s.m6 + 6);
+        for (int c = 0; c < 3; ++c) sf3.push_back(M0 > 0 ? s.f3[c] / M0 : 0.0);
+        sprm.insert(sprm.end(), {s.t0, s.tr});
+    }
+
+    // stations (src/swpc_3d/m_wav.f90:141-271)
+    int flags = (p.sw_v ? SWPC_WAV_V : 0) | (p.sw_u ? SWPC_WAV_U : 0) | (p.sw_stress ? SWPC_WAV_STRESS : 0) |
+                (p.sw_strain ? SWPC_WAV_STRAIN : 0);
+    if (flags) {
+        std::vector<std::string> srows;
+        try { srows = table_rows(inf.path(p.fn_stloc)); }
+        catch (...) { std::fprintf(stderr, "swpc: no station location file found\n"); }
+        for (auto& r : srows) {
+            auto t = split(r);
+            if (t.size() < 5) throw std::runtime_error("bad station line: " + r);
+            Station st;
+            if (p.st_format == "xy") {
+                st.x = Inf::num(t[0]); st.y = Inf::num(t[1]);
+                c2g(st.x, st.y, p.clon, p.clat, p.phi, st.lon, st.lat);
+            } else if (p.st_format == "ll") {
+                st.lon = Inf::num(t[0]); st.lat = Inf::num(t[1]);
+                g2c(st.lon, st.lat, p.clon, p.clat, p.phi, st.x, st.y);
+            } else throw std::runtime_error("unknown st_format " + p.st_format);
+            st.z = Inf::num(t[2]);
+            st.name = t[3].substr(0, 8);
+            std::string zsw = t[4].substr(0, 3);
+            st.i = x2i(st.x, p.xbeg, p.dx); st.j = x2i(st.y, p.ybeg, p.dy); st.k = x2i(st.z, p.zbeg, p.dz);
+            double x1 = p.xbeg + 0.5 * p.dx, xn = p.xbeg + (p.nx - 0.5) * p.dx;
+            double y1 = p.ybeg + 0.5 * p.dy, yn = p.ybeg + (p.ny - 0.5) * p.dy;
+            if (!(x1 < st.x && st.x < xn && y1 < st.y && st.y < yn && 1 < st.k && st.k < p.nz)) {
+                std::fprintf(stderr, "swpc: station %s is out of the region\n", st.name.c_str());
+                continue;
+            }
+            if (zsw == "fsb") st.k = kfs[G.idx2(st.i, st.j)] + 1;
+            else if (zsw == "obb") st.k = kob[G.idx2(st.i, st.j)] + 1;
+            else if (zsw == "oba") st.k = kob[G.idx2(st.i, st.j)] - 1;
+            else if (zsw == "bd0") st.k = x2i(bd0, p.zbeg, p.dz);
+            if (st.k > p.nz) st.k = p.nz - 1;
+            if (st.k < 1) st.k = 2;
+            meta.st.push_back(st);
+        }
+    }
+
+    if (dry) {  // set-up summary only, no device
+        char buf[512];
+        std::string src_s, st_s;
+        for (size_t q = 0; q < smo.size(); ++q)
+            src_s += (q ? ";" : "") + std::to_string(sijk[3 * q]) + "," + std::to_string(sijk[3 * q + 1]) + "," + std::to_string(sijk[3 * q + 2]);
+        for (size_t q = 0; q < meta.st.size(); ++q)
+            st_s += (q ? ";" : "") + std::to_string(meta.st[q].i) + "," + std::to_string(meta.st[q].j) + "," + std::to_string(meta.st[q].k);
+        std::snprintf(buf, sizeof buf, "{\"nx\": %d, \"ny\": %d, \"nz\": %d, \"nt\": %d, \"na\": %d, \"M0\": %.9g, \"UC\": %.9g, "
+                      "\"fcut\": %.9g, \"nsrc\": %d, \"nst\": %d, \"ts\": [%.9g, %.9g, %.9g], ",
+                      p.nx, p.ny, p.nz, p.nt, p.na, M0, UC, fcut, (int)smo.size(), (int)meta.st.size(), ts[0], ts[1], ts[2]);
+        *dry = std::string(buf) + "\"src\": \"" + src_s + "\", \"sta\": \"" + st_s + "\"}";
+        return 0;
+    }
+
+    swpc_dims d{};
+    d.nx = p.nx; d.ny = p.ny; d.nz = p.nz; d.nt = p.nt; d.na = p.na; d.nm = 3;
+    d.abc_type = p.abc_type == "pml" ? SWPC_ABC_PML : p.abc_type == "cerjan" ? SWPC_ABC_CERJAN : -1;
+    if (d.abc_type < 0) throw std::runtime_error("abc_type must be 'pml' or 'cerjan'");
+    std::string store = inf.s("gpu_store", "fp32");
+    d.store = store == "fp16" ? SWPC_STORE_FP16 : store == "bf16" ? SWPC_STORE_BF16 : SWPC_STORE_FP32;
+    d.dx = p.dx; d.dy = p.dy; d.dz = p.dz; d.dt = p.dt;
+    d.xbeg = p.xbeg; d.ybeg = p.ybeg; d.zbeg = p.zbeg; d.tbeg = p.tbeg;
+    d.fcut = fcut; d.M0 = M0; d.UC = UC; d.ntdec_r = p.ntdec_r;
+    meta.M0 = M0; meta.UC = UC;
+
+    swpc_sim* sim = nullptr;
+    int rc = swpc_gpu_create(&d, &sim);
+    if (rc) return rc;
+    auto bail = [&](int code) { swpc_gpu_destroy(sim); return code; };
+    if ((rc = swpc_gpu_upload_medium(sim, rho.data(), lam.data(), mu.data(), tp.data(), tsv.data(), kfs.data(), kob.data(),
+                                     kft.data(), kfb.data(), kot.data(), kobb.data(), ts)))
+        return bail(rc);
+    int ns = (int)smo.size();
+    if ((rc = swpc_gpu_set_sources(sim, ns, sijk.data(), smo.data(), smij.data(), sf3.data(), sprm.data(),
+                                   stf_code(p.stftype), p.bf_mode)))
+        return bail(rc);
+    std::vector<int> rijk;
+    for (auto& st : meta.st) rijk.insert(rijk.end(), {st.i, st.j, st.k});
+    if ((rc = swpc_gpu_set_receivers(sim, (int)meta.st.size(), rijk.data(), std::max(1, p.ntdec_w), flags)))
+        return bail(rc);
+    int kinds = (p.xy_v ? SWPC_SNAP_XY_V : 0) | (p.xy_u ? SWPC_SNAP_XY_U : 0);
+    if (kinds) {
+        int k0 = x2i(p.z0_xy, p.zbeg, p.dz);
+        if ((rc = swpc_gpu_set_snapshot(sim, kinds, std::max(1, std::min(p.nz, k0)), p.idec, p.jdec, p.ntdec_s)))
+            return bail(rc);
+    }
+    meta.flags = flags;
+    swpc_gpu_query(sim, &meta.ntw, nullptr, nullptr, nullptr, nullptr);
+    {
+        std::lock_guard<std::mutex> lk(g_meta_mu);
+        g_meta[sim] = meta;
+    }
+    *out = sim;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swpc_host_medium(int nx, int ny, int nz, int na, double fq_min, double fq_max, double fq_ref, float* rho, float* lam,
+                     float* mu, float* qp_taup, float* qs_taus, int* kfs, int* kob, int* kfs_top, int* kfs_bot,
+                     int* kob_top, int* kob_bot, double* ts) {
+    if (!rho || !lam || !mu || !qp_taup || !qs_taus || !kfs || !kob || !kfs_top || !kfs_bot || !kob_top || !kob_bot || !ts)
+        return swpc::set_err(SWPC_E_ARG, "null argument to swpc_host_medium");
+    if (nx <= 2 * na || ny <= 2 * na || nz <= na || na < 0) return swpc::set_err(SWPC_E_ARG, "bad grid / absorber size");
+    medium_post(nx, ny, nz, na, fq_min, fq_max, fq_ref, rho, lam, mu, qp_taup, qs_taus, kfs, kob, kfs_top, kfs_bot,
+                kob_top, kob_bot, ts);
+    return 0;
+}
+
+int swpc_host_prepare(const char* inf_path, swpc_sim** out) {
+    if (!inf_path || !out) return swpc::set_err(SWPC_E_ARG, "null argument");
+    *out = nullptr;
+    try {
+        return prepare(inf_path, out);
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
+}
+
+int swpc_host_check(const char* inf_path, char* summary, size_t n) {
+    if (!inf_path) return swpc::set_err(SWPC_E_ARG, "null argument");
+    try {
+        std::string s;
+        int rc = prepare(inf_path, nullptr, &s);
+        if (summary && n) {
+            size_t m = std::min(n - 1, s.size());
+            std::memcpy(summary, s.data(), m);
+            summary[m] = 0;
+        }
+        return rc ? rc : (int)s.size();
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
+}
+
+int swpc_host_nt(swpc_sim* sim) {
+    std::lock_guard<std::mutex> lk(g_meta_mu);
+    auto it = g_meta.find(sim);
+    return it == g_meta.end() ? 0 : it->second.p.nt;
+}
+
+int swpc_host_write_sac(swpc_sim* sim, const char* odir) {
+    Meta m;
+    {
+        std::lock_guard<std::mutex> lk(g_meta_mu);
+        auto it = g_meta.find(sim);
+        if (it == g_meta.end()) return swpc::set_err(SWPC_E_STATE, "simulation was not prepared by swpc_host_prepare");
+        m = it->second;
+    }
+    try {
+        std::string dir = (odir && *odir) ? std::string(odir) : m.p.odir;
+        mkdirs(dir + "/wav");
+        const int nst = (int)m.st.size(), ntw = m.ntw;
+        struct K { int kind, nc, idep; const char* names[6]; };
+        const K kinds[4] = {{SWPC_WAV_V, 3, 7, {"Vx", "Vy", "Vz"}}, {SWPC_WAV_U, 3, 6, {"Ux", "Uy", "Uz"}},
+                            {SWPC_WAV_STRESS, 6, 5, {"Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"}},
+                            {SWPC_WAV_STRAIN, 6, 5, {"Exx", "Eyy", "Ezz", "Eyz", "Exz", "Exy"}}};
+        for (const K& k : kinds) {
+            if (!(m.flags & k.kind)) continue;
+            std::vector<float> w((size_t)ntw * k.nc * nst);
+            int rc = swpc_gpu_fetch_waveforms(sim, k.kind, w.data());
+            if (rc) return rc;
+            for (int s = 0; s < nst; ++s)
+                for (int c = 0; c < k.nc; ++c) {
+                    double inc = -12345, az = -12345;
+                    if (k.nc == 3) { inc = 90.0; az = c == 0 ? 0.0 + m.p.phi : c == 1 ? 90.0 + m.p.phi : 0.0; }
+                    std::string fn = dir + "/wav/" + m.p.title + ".3d." + m.st[s].name + "." + k.names[c] + ".sac";
+                    write_sac(fn, m, m.st[s], k.names[c], k.idep, inc, az, &w[((size_t)s * k.nc + c) * ntw], ntw);
+                }
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
+}
+
+}  // extern "C"

@@ -51,7 +51,9 @@ struct Sim {
     bool bf_mode = false, medium_ready = false, diverged = false, profiling = false;
     int it_done = 0;
 
-    cudaEvent_t evs[12] = {};
+    struct Pending { int cls; cudaEvent_t a, b; };
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<Pending> pending;
     double prof_ms[6] = {0, 0, 0, 0, 0, 0};
     long long prof_n[6] = {0, 0, 0, 0, 0, 0};
 
@@ -69,6 +71,8 @@ struct Sim {
     int launch_step(bool timed);
     int ensure_graph();
     int check_divergence();
+    cudaEvent_t get_event();
+    int drain_events();
 };
 
 }  // namespace swpc

@@ -141,15 +141,18 @@ void Sim::fill_zargs(ZArgs& z) const {
 int Sim::launch_step(bool timed) {
     const dim3 blk(TBX, TBY);
     const dim3 grd((p.nxi + TBX - 1) / TBX, (p.nyi + TBY - 1) / TBY, (p.nzi + kchunk - 1) / kchunk);
-    auto ev0 = [&](int c) { if (timed) cudaEventRecord(evs[2 * c], stream); };
+    // timed: an event pair on the launching stream around each kernel, read
+    // back later by drain_events() so the launches are not serialised
+    cudaEvent_t e_a = nullptr;
+    auto ev0 = [&](int c) {
+        (void)c;
+        if (timed) { e_a = get_event(); cudaEventRecord(e_a, stream); }
+    };
     auto ev1 = [&](int c) {
         if (timed) {
-            cudaEventRecord(evs[2 * c + 1], stream);
-            cudaEventSynchronize(evs[2 * c + 1]);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, evs[2 * c], evs[2 * c + 1]);
-            prof_ms[c] += ms;
-            prof_n[c] += 1;
+            cudaEvent_t e_b = get_event();
+            cudaEventRecord(e_b, stream);
+            pending.push_back({c, e_a, e_b});
         }
     };
     if (vmax_args.ntdec_r > 0) { k_vmax<<<64, 256, 0, stream>>>(vmax_args); ++launches; }
@@ -194,6 +197,32 @@ int Sim::launch_step(bool timed) {
     k_advance<<<1, 1, 0, stream>>>(d_it); ++launches;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+cudaEvent_t Sim::get_event() {
+    if (!ev_pool.empty()) {
+        cudaEvent_t e = ev_pool.back();
+        ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+int Sim::drain_events() {
+    CK(cudaStreamSynchronize(stream));
+    for (auto& q : pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, q.a, q.b) == cudaSuccess) {
+            prof_ms[q.cls] += ms;
+            prof_n[q.cls] += 1;
+        }
+        ev_pool.push_back(q.a);
+        ev_pool.push_back(q.b);
+    }
+    pending.clear();
     return 0;
 }
 
@@ -422,6 +451,8 @@ int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out) {
 int swpc_gpu_profile(swpc_sim* sim, int enable) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    int rc = s->drain_events();
+    if (rc) return rc;
     s->profiling = enable != 0;
     for (int c = 0; c < 6; ++c) { s->prof_ms[c] = 0; s->prof_n[c] = 0; }
     return 0;
@@ -430,6 +461,8 @@ int swpc_gpu_profile(swpc_sim* sim, int enable) {
 int swpc_gpu_profile_read(swpc_sim* sim, double* ms, long long* n) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    int rc = s->drain_events();
+    if (rc) return rc;
     for (int c = 0; c < 6; ++c) {
         if (ms) ms[c] = s->prof_ms[c];
         if (n) n[c] = s->prof_n[c];
@@ -446,7 +479,8 @@ Sim::~Sim() {
     if (stream) cudaStreamSynchronize(stream);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (void* q : allocs) cudaFree(q);
-    for (auto& e : evs) if (e) cudaEventDestroy(e);
+    for (auto& q : pending) { ev_pool.push_back(q.a); ev_pool.push_back(q.b); }
+    for (auto& e : ev_pool) if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -464,7 +498,6 @@ int Sim::dalloc(void** ptr, size_t bytes) {
 
 int Sim::allocate() {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    for (auto& e : evs) CK(cudaEventCreate(&e));
     int rc;
     if ((rc = dalloc((void**)&V, p.nV * 4))) return rc;
     if ((rc = dalloc((void**)&S, p.nS * 4))) return rc;

@@ -45,7 +45,8 @@ EXPORTS = [
     "swpc_gpu_fetch_waveforms", "swpc_gpu_fetch_snapshot", "swpc_gpu_query", "swpc_gpu_vmax",
     "swpc_gpu_fetch_field", "swpc_gpu_profile", "swpc_gpu_profile_read", "swpc_gpu_stream",
     "swpc_gpu_launch_count", "swpc_gpu_destroy", "swpc_gpu_last_error", "swpc_host_prepare",
-    "swpc_host_write_sac",
+    "swpc_host_write_sac", "swpc_host_nt", "swpc_host_medium",
+    "swpc_host_check",
 ]
 
 
@@ -86,8 +87,9 @@ def lib(build=True):
     L.swpc_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.swpc_host_prepare.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_write_sac.argtypes = [vp, ctypes.c_char_p]
-    if hasattr(L, "swpc_host_nt"):
-        L.swpc_host_nt.argtypes = [vp]
+    L.swpc_host_nt.argtypes = [vp]
+    L.swpc_host_check.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+    L.swpc_host_medium.argtypes = [i, i, i, i, d, d, d] + [fp] * 5 + [ip] * 6 + [dp]
     _lib = L
     return L
 
@@ -118,6 +120,31 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     d.xbeg, d.ybeg, d.zbeg, d.tbeg = xbeg, ybeg, zbeg, tbeg
     d.fcut, d.M0, d.UC, d.ntdec_r = fcut, M0, UC, ntdec_r
     return d
+
+
+def host_medium(nx, ny, nz, na, fq_min, fq_max, fq_ref, rho, lam, mu, qp, qs):
+    """Medium post-processing of medium__setup in FP64 (swpc_host_medium).
+    Arrays are Fortran (k,i,j) halo arrays shaped (ny+6, nx+6, nz+6); rho,
+    lam, mu are modified in place and (taup, taus, maps..., ts) returned."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (rho, lam, mu, qp, qs)]
+    for a, b in zip(arrs[:3], (rho, lam, mu)):
+        if a is not b:
+            raise ValueError("rho, lam, mu must be contiguous float32 arrays (modified in place)")
+    maps = [np.zeros((ny + 6, nx + 6), np.int32) for _ in range(6)]
+    ts = np.zeros(3, np.float64)
+    _ck(lib().swpc_host_medium(nx, ny, nz, na, fq_min, fq_max, fq_ref, *[_ptr(a) for a in arrs],
+                               *[_ptr(m) for m in maps], _ptr(ts)))
+    return arrs[3], arrs[4], maps, ts
+
+
+def host_check(inf_path):
+    """Host set-up summary of an input.inf without a GPU (swpc_host_check)."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 20)
+    rc = lib().swpc_host_check(os.fsencode(os.path.abspath(inf_path)), buf, 1 << 20)
+    if rc < 0:
+        raise SwpcError(rc, last_error())
+    return json.loads(buf.value.decode())
 
 
 def required_bytes(dims):
@@ -224,6 +251,9 @@ class Simulation:
 
     def launch_count(self):
         return int(lib().swpc_gpu_launch_count(self._h))
+
+    def nt(self):
+        return int(lib().swpc_host_nt(self._h))
 
     def write_sac(self, odir=None):
         _ck(lib().swpc_host_write_sac(self._h, os.fsencode(odir) if odir else None))

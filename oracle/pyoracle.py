@@ -17,29 +17,44 @@ SRC = os.path.join(HERE, "swpc_oracle.cpp")
 # -ffp-contract=off and no fast-math keep the restatement's rounding
 # deterministic and close to the reference's scalar evaluation order.
 CXXFLAGS = ["-O2", "-fno-fast-math", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c++17"]
+# The timed CPU baseline uses the optimisation flags of the reference's
+# ubuntu-gfortran build (src/shared/makefile.arch:28: -O2 -ffast-math -fopenmp).
+LIB_FAST = os.path.join(BUILD, "liboracle_fast.so")
+CXXFLAGS_FAST = ["-O2", "-ffast-math", "-fopenmp", "-fPIC", "-shared", "-std=c++17"]
 
 MODES = {"fp32": 0, "mixed": 1, "fp64": 2}
 FIELDS = ["Vx", "Vy", "Vz", "Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"]
 MEDIA = ["rho", "lam", "mu", "taup", "taus", "kfs", "kob", "kfs_top", "kfs_bot", "kob_top", "kob_bot", "ts"]
 
 
-def build(force=False):
+def build(force=False, fast=False):
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        tmp = LIB + ".tmp"
-        subprocess.check_call(["g++", *CXXFLAGS, "-o", tmp, SRC])
-        os.replace(tmp, LIB)
-    return LIB
+    out, flags = (LIB_FAST, CXXFLAGS_FAST) if fast else (LIB, CXXFLAGS)
+    if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(SRC):
+        tmp = out + ".tmp"
+        subprocess.check_call(["g++", *flags, "-o", tmp, SRC])
+        os.replace(tmp, out)
+    return out
 
 
-_lib = None
+_libs = {}
+
+
+def use_fast_build():
+    """Route every Oracle created afterwards through the -ffast-math build
+    (timing only; the parity tests use the deterministic build)."""
+    global _fast
+    _fast = True
+
+
+_fast = False
 
 
 def lib():
-    global _lib
-    if _lib is None:
-        build()
-        L = ctypes.CDLL(LIB)
+    key = "fast" if _fast else "exact"
+    if key not in _libs:
+        path = build(fast=_fast)
+        L = ctypes.CDLL(path)
         vp = ctypes.c_void_p
         L.oracle_create.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(vp)]
         L.oracle_last_error.restype = ctypes.c_char_p
@@ -57,15 +72,15 @@ def lib():
         L.oracle_momentrate.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float]
         L.oracle_momentrate.restype = ctypes.c_float
         L.oracle_sdr2moment.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_void_p]
-        _lib = L
-    return _lib
+        _libs[key] = L
+    return _libs[key]
 
 
 class Oracle:
     """One oracle simulation built from an input.inf file."""
 
     def __init__(self, inf_path, mode="fp32", nthreads=0, medium=None):
-        L = lib()
+        L = self._L = lib()
         h = ctypes.c_void_p()
         vm = None
         if medium is not None:
@@ -81,7 +96,7 @@ class Oracle:
     def refresh(self):
         ints = np.zeros(16, np.int32)
         reals = np.zeros(16, np.float64)
-        lib().oracle_info(self.h, ints.ctypes.data, reals.ctypes.data)
+        self._L.oracle_info(self.h, ints.ctypes.data, reals.ctypes.data)
         (self.nx, self.ny, self.nz, self.nt, self.na, self.nst, self.ntw, self.nt_done,
          self.nxs, self.nys, self.k0_xy, self.nvmax, self.nsnap) = [int(v) for v in ints[:13]]
         self.M0, self.UC, self.fcut = [float(v) for v in reals[:3]]
@@ -89,25 +104,25 @@ class Oracle:
         self.ntdec_w, self.ntdec_r, self.bf_mode = int(ints[13]), int(ints[14]), bool(ints[15])
 
     def run(self, n):
-        if lib().oracle_run(self.h, int(n)) != 0:
-            raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+        if self._L.oracle_run(self.h, int(n)) != 0:
+            raise RuntimeError("oracle: " + self._L.oracle_last_error().decode())
         self.refresh()
 
     def waveforms(self, kind=0):
         ncmp = 3 if kind in (0, 1) else 6
         out = np.zeros((self.nst, ncmp, self.ntw), np.float32)  # Fortran (ntw,ncmp,nst)
-        lib().oracle_waveforms(self.h, kind, out.ctypes.data)
+        self._L.oracle_waveforms(self.h, kind, out.ctypes.data)
         return out
 
     def stations(self):
         out = np.zeros((self.nst, 3), np.int32)
-        lib().oracle_stations(self.h, out.ctypes.data)
+        self._L.oracle_stations(self.h, out.ctypes.data)
         return out
 
     def field(self, name):
         out = np.zeros((self.ny, self.nx, self.nz), np.float64)  # Fortran (nz,nx,ny)
-        if lib().oracle_field(self.h, FIELDS.index(name), out.ctypes.data) != 0:
-            raise RuntimeError(lib().oracle_last_error().decode())
+        if self._L.oracle_field(self.h, FIELDS.index(name), out.ctypes.data) != 0:
+            raise RuntimeError(self._L.oracle_last_error().decode())
         return out
 
     def medium(self, name):
@@ -118,33 +133,33 @@ class Oracle:
             out = np.zeros((self.ny + 6, self.nx + 6), np.float32)
         else:
             out = np.zeros(3, np.float32)
-        if lib().oracle_medium(self.h, w, out.ctypes.data) != 0:
-            raise RuntimeError(lib().oracle_last_error().decode())
+        if self._L.oracle_medium(self.h, w, out.ctypes.data) != 0:
+            raise RuntimeError(self._L.oracle_last_error().decode())
         return out if w < 5 or w == 11 else out.astype(np.int32)
 
     def vmax_log(self):
         out = np.zeros((self.nvmax, 4), np.float32)
-        lib().oracle_vmax(self.h, out.ctypes.data)
+        self._L.oracle_vmax(self.h, out.ctypes.data)
         return out
 
     def snap_xy_v(self):
         out = np.zeros(self.nsnap, np.float32)
-        lib().oracle_snap_xy_v(self.h, out.ctypes.data)
+        self._L.oracle_snap_xy_v(self.h, out.ctypes.data)
         return out.reshape(-1, 3, self.nys, self.nxs)
 
     def sources(self):
-        n = lib().oracle_sources(self.h, None, None)
+        n = self._L.oracle_sources(self.h, None, None)
         ijk = np.zeros((n, 3), np.int32)
         vals = np.zeros((n, 12), np.float64)
-        lib().oracle_sources(self.h, ijk.ctypes.data, vals.ctypes.data)
+        self._L.oracle_sources(self.h, ijk.ctypes.data, vals.ctypes.data)
         return ijk, vals
 
     def stf(self):
-        return lib().oracle_stf(self.h)
+        return self._L.oracle_stf(self.h)
 
     def close(self):
         if self.h:
-            lib().oracle_destroy(self.h)
+            self._L.oracle_destroy(self.h)
             self.h = None
 
     def __del__(self):
