@@ -160,11 +160,11 @@ def source_and_stations(w, med, seed):
     return src, mij, sta
 
 
-def build_sim(w, med, nt, store="fp32", ntdec_r=100):
+def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0):
     from openswpc_gb300 import gpu
     dims = gpu.make_dims(w["nx"], w["ny"], w["nz"], nt, w["dx"], w["dx"], w["dx"], w["dt"], na=20, store=store,
                          xbeg=-w["nx"] * w["dx"] / 2, ybeg=-w["ny"] * w["dx"] / 2, zbeg=med["zbeg"], fcut=1.0,
-                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r)
+                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant)
     sim = gpu.Simulation(dims)
     m = med["maps"]
     sim.upload_medium(med["rho"], med["lam"], med["mu"], med["taup"], med["taus"], m[0], m[1], m[2], m[3], m[4], m[5],
@@ -264,7 +264,7 @@ def run_gpu(args, w):
     t_setup = time.time()
     med = make_medium(w, seed)
     med["src"], med["mij"], med["sta"] = source_and_stations(w, med, seed)
-    sim = build_sim(w, med, w["nt"])
+    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant)
     stream = torch.cuda.ExternalStream(sim.stream())
     t_setup = time.time() - t_setup
 
@@ -332,7 +332,7 @@ def run_gpu(args, w):
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim2 = build_sim(w, med_p, args.steps)
+        sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant)
         sim2.run(1, args.steps)
         wav = sim2.waveforms()
         sim2.close()
@@ -389,6 +389,8 @@ def main():
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])
+    ap.add_argument("--variant", type=int, default=0, help="0: TMA-fed interior kernels, 1: plain smem sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1,0 +1,451 @@
+// kernels_tma.cuh -- TMA-fed z-sweep kernels for the viscoelastic interior.
+//
+// Each block owns a 32 x TY column tile and sweeps z.  One elected thread
+// streams whole plane tiles into shared-memory rings with
+// cp.async.bulk.tensor (4-D tensor maps over the row-interleaved [kz][jy][f][x]
+// groups: one copy brings every field of a group for the tile), completing on
+// one mbarrier per ring slot.  Several planes are in flight per block, so
+// the HBM pipe stays full without the register cost of software prefetch.
+// All threads compute from shared memory and store results with coalesced
+// 128-byte stores.  Every mbarrier wait is bounded; a wait that runs out sets
+// the error word, the block drains its own copies (again bounded) and returns.
+#pragma once
+#include <cuda.h>
+#include "kernels.cuh"
+
+namespace swpc {
+
+constexpr int TTY = 8;            // tile rows of the TMA kernels
+constexpr int WAIT_LIMIT = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int i = 0; i < WAIT_LIMIT; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Tensor maps and scalars of the TMA kernels.  The maps must stay 64-byte
+// aligned and are read from the kernel parameter space (__grid_constant__).
+struct TArgs {
+    CUtensorMap tmV;    // V group, box (40, 3, TTY+4, 1)
+    CUtensorMap tmS;    // S group, box (32, 6, TTY, 1)
+    CUtensorMap tmM;    // M group fields lam..taus, box (36, 4, TTY+1, 1)
+    CUtensorMap tmR;    // memory variables, box (32, 18, TTY, 1)
+    CUtensorMap tmSh;   // S group with halo, box (40, 6, TTY+4, 1)
+    CUtensorMap tmRho;  // M group field rho, box (36, 1, TTY+1, 1)
+    CUtensorMap tmVc;   // V group centre, box (32, 3, TTY, 1)
+    ZArgs z;
+    int* err;           // error word (bounded wait ran out)
+};
+
+// Every ring slot is a TMA destination and must start on a 128-byte
+// boundary: each slot is its own 128-byte-aligned struct, so its size is
+// padded to a multiple of 128 bytes.
+template <class T, int A, int B, int C>
+struct alignas(128) Slot3 { T d[A][B][C]; };
+template <class T, int A, int B>
+struct alignas(128) Slot2 { T d[A][B]; };
+
+template <class RT>
+struct StressSmem {
+    Slot3<RT, TTY, 18, 32> R[2];
+    Slot3<float, TTY, 6, 32> S[2];
+    Slot3<float, TTY + 1, 4, 36> M[3];
+    Slot3<float, TTY + 4, 3, 40> V[6];
+    alignas(8) uint64_t barRS[2], barM[3], barV[6];
+    int bad;
+};
+
+struct VelSmem {
+    Slot3<float, TTY + 4, 6, 40> S[8];
+    Slot2<float, TTY + 1, 36> M[3];
+    Slot3<float, TTY, 3, 32> V[4];
+    alignas(8) uint64_t barS[8], barM[3], barV[4];
+    int bad;
+};
+static_assert(sizeof(Slot3<float, TTY + 1, 4, 36>) % 128 == 0, "slot size");
+static_assert(sizeof(Slot2<float, TTY + 1, 36>) % 128 == 0, "slot size");
+static_assert(sizeof(Slot3<__half, TTY, 18, 32>) % 128 == 0, "slot size");
+static_assert(sizeof(Slot3<float, TTY + 4, 6, 40>) % 128 == 0, "slot size");
+
+// Start-up check of a TMA destination (128-byte boundary) and of the
+// innermost box coordinate (a multiple of 16 bytes); a block that fails it
+// issues no copy at all.
+__device__ __forceinline__ bool tma_ok(const void* dst, int x, int esize) {
+    return (smem_u32(dst) & 127u) == 0 && ((x * esize) & 15) == 0 && x >= 0;
+}
+
+__device__ __forceinline__ int pmod(int a, int n) { int r = a % n; return r < 0 ? r + n : r; }
+
+// ---------------------------------------------------------------------------
+// Interior stress update (m_kernel.f90:142-348), TMA pipeline.
+//   R+S ring: 2 planes (k, k+1 in flight)
+//   M ring:   3 planes (k, k+1 for mu(k+1), k+2 in flight)
+//   V ring:   6 planes (k-2 .. k+2 for the z stencil, k+3 in flight)
+// ---------------------------------------------------------------------------
+template <class RT>
+__global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constant__ TArgs ta) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    StressSmem<RT>& sm = *reinterpret_cast<StressSmem<RT>*>(smraw);
+    int& bad = sm.bad;
+    const ZArgs& a = ta.z;
+    const Geo& g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int xt = a.x0 + blockIdx.x * 32, yt = a.y0 + blockIdx.y * TTY;
+    const int ix = xt + tx, jy = yt + ty;
+    const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
+    const int kz0 = blockIdx.z * a.kchunk;
+    const int kz1 = min(kz0 + a.kchunk, a.kz_end);
+    if (kz0 >= kz1) return;
+
+    constexpr uint32_t BR = sizeof(RT) * TTY * 18 * 32, BS = 4 * TTY * 6 * 32;
+    constexpr uint32_t BM = 4 * (TTY + 1) * 4 * 36, BV = 4 * (TTY + 4) * 3 * 40;
+    int fills[11];  // producer bookkeeping: fills per slot (RS 0-1, M 2-4, V 5-10)
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) mbar_init(&sm.barRS[s], 1);
+        for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
+        for (int s = 0; s < 6; ++s) mbar_init(&sm.barV[s], 1);
+        fence_barrier_init();
+        bad = 0;
+    }
+    for (int s = 0; s < 11; ++s) fills[s] = 0;
+    const int gxS = xt + g.hx, gyS = yt + HYT;
+    if (tid == 0) {
+        bool ok = true;
+        for (int s = 0; s < 2; ++s) ok &= tma_ok(&sm.R[s], xt - a.x0, (int)sizeof(RT)) && tma_ok(&sm.S[s], gxS, 4);
+        for (int s = 0; s < 3; ++s) ok &= tma_ok(&sm.M[s], gxS, 4);
+        for (int s = 0; s < 6; ++s) ok &= tma_ok(&sm.V[s], gxS - 4, 4);
+        if (!ok) { bad = 1; atomicExch(ta.err, 2); }
+    }
+    __syncthreads();
+    if (bad) return;
+
+    auto issueRS = [&](int p) {
+        int s = pmod(p - kz0, 2);
+        mbar_expect_tx(&sm.barRS[s], BR + BS);
+        tma_load_4d(&sm.R[s], &ta.tmR, &sm.barRS[s], xt - a.x0, 0, yt - a.y0, p);
+        tma_load_4d(&sm.S[s], &ta.tmS, &sm.barRS[s], gxS, 0, gyS, p + HZT);
+        ++fills[s];
+    };
+    auto issueM = [&](int p) {
+        int s = pmod(p - kz0, 3);
+        mbar_expect_tx(&sm.barM[s], BM);
+        tma_load_4d(&sm.M[s], &ta.tmM, &sm.barM[s], gxS, 1, gyS, p + HZT);
+        ++fills[2 + s];
+    };
+    auto issueV = [&](int p) {
+        int s = pmod(p - (kz0 - 2), 6);
+        mbar_expect_tx(&sm.barV[s], BV);
+        tma_load_4d(&sm.V[s], &ta.tmV, &sm.barV[s], gxS - 4, 0, gyS - 2, p + HZT);
+        ++fills[5 + s];
+    };
+    if (tid == 0) {
+        for (int p = kz0; p <= min(kz0 + 1, kz1 - 1); ++p) issueRS(p);
+        for (int p = kz0; p <= min(kz0 + 2, kz1); ++p) issueM(p);
+        for (int p = kz0 - 2; p <= min(kz0 + 3, kz1 + 1); ++p) issueV(p);
+    }
+    auto parity = [&](int p, int p0, int n) { return (uint32_t)(((p - p0) / n) & 1); };
+
+    int4 band = make_int4(0, -1, 0, -1);
+    if (act) band = a.band[(size_t)(jy - a.y0) * a.nxi + (ix - a.x0)];
+    const float dt = a.c.dt;
+    const float eps = 1.1920928955078125e-07f;
+    const long long planeS = 6LL * g.pitch * g.nyp;
+    const long long bS = (long long)goff(g, 6, 0, ix, jy, 0);
+    const long long rrow = 18LL * a.rpitch, rplane = rrow * a.nyi;
+    const long long bR = (long long)(jy - a.y0) * rrow + (ix - a.x0);
+    float* __restrict__ Sg = a.S;
+    RT* __restrict__ Rg = (RT*)a.R;
+    const int P = g.pitch;
+
+    for (int k = kz0; k < kz1; ++k) {
+        bool ok = mbar_wait(&sm.barRS[pmod(k - kz0, 2)], parity(k, kz0, 2));
+        ok &= mbar_wait(&sm.barM[pmod(k - kz0, 3)], parity(k, kz0, 3));
+        ok &= mbar_wait(&sm.barM[pmod(k + 1 - kz0, 3)], parity(k + 1, kz0, 3));
+        for (int d = -2; d <= 2; ++d) ok &= mbar_wait(&sm.barV[pmod(k + d - kz0 + 2, 6)], parity(k + d, kz0 - 2, 6));
+        if (!ok) bad = 1;
+
+        const int sRS = pmod(k - kz0, 2), sM0 = pmod(k - kz0, 3), sM1 = pmod(k + 1 - kz0, 3);
+        const int sV[5] = {pmod(k - kz0, 6), pmod(k - kz0 + 1, 6), pmod(k - kz0 + 2, 6), pmod(k - kz0 + 3, 6), pmod(k - kz0 + 4, 6)};
+        if (act && ok) {
+            const int kk = k + 1;
+            const bool nb = in_band(kk, band);
+            const float e40x = nb ? a.c.e2x : a.c.e4x0, e41x = nb ? 0.f : a.c.e4x1;
+            const float e40y = nb ? a.c.e2y : a.c.e4y0, e41y = nb ? 0.f : a.c.e4y1;
+            const float e40z = nb ? a.c.e2z : a.c.e4z0, e41z = nb ? 0.f : a.c.e4z1;
+            const int lx = tx + 4, ly = ty + 2;
+            // V(k) plane tile: [y][c][x]
+            float (*Vk)[3][40] = sm.V[sV[2]].d;
+            auto X = [&](int dy, int dx) { return Vk[ly + dy][0][lx + dx]; };
+            auto Y = [&](int dy, int dx) { return Vk[ly + dy][1][lx + dx]; };
+            auto Z = [&](int dy, int dx) { return Vk[ly + dy][2][lx + dx]; };
+            auto zc = [&](int d, int c) { return sm.V[sV[d + 2]].d[ly][c][lx]; };  // own column at plane k+d
+
+            const float dxVx = (X(0, 0) - X(0, -1)) * e40x - (X(0, 1) - X(0, -2)) * e41x;
+            const float dyVy = (Y(0, 0) - Y(-1, 0)) * e40y - (Y(1, 0) - Y(-2, 0)) * e41y;
+            const float dzVz = (zc(0, 2) - zc(-1, 2)) * e40z - (zc(1, 2) - zc(-2, 2)) * e41z;
+            const float dxVy_dyVx = (Y(0, 1) - Y(0, 0)) * e40x - (Y(0, 2) - Y(0, -1)) * e41x
+                                  + (X(1, 0) - X(0, 0)) * e40y - (X(2, 0) - X(-1, 0)) * e41y;
+            const float dxVz_dzVx = (Z(0, 1) - Z(0, 0)) * e40x - (Z(0, 2) - Z(0, -1)) * e41x
+                                  + (zc(1, 0) - zc(0, 0)) * e40z - (zc(2, 0) - zc(-1, 0)) * e41z;
+            const float dyVz_dzVy = (Z(1, 0) - Z(0, 0)) * e40y - (Z(2, 0) - Z(-1, 0)) * e41y
+                                  + (zc(1, 1) - zc(0, 1)) * e40z - (zc(2, 1) - zc(-1, 1)) * e41z;
+
+            float (*M0)[4][36] = sm.M[sM0].d;
+            float (*M1)[4][36] = sm.M[sM1].d;
+            const float lam = M0[ty][0][tx], tp = M0[ty][2][tx], ts = M0[ty][3][tx];
+            const float m000 = M0[ty][1][tx], m100 = M1[ty][1][tx];
+            const float m010 = M0[ty][1][tx + 1], m110 = M1[ty][1][tx + 1];
+            const float m001 = M0[ty + 1][1][tx], m101 = M1[ty + 1][1][tx];
+            const float m011 = M0[ty + 1][1][tx + 1];
+
+            float r[18];
+#pragma unroll
+            for (int f = 0; f < 18; ++f) r[f] = St<RT>::ld(&sm.R[sRS].d[ty][f][tx]);
+            float (*Sk)[32] = sm.S[sRS].d[ty];
+            float sxx = Sk[0][tx], syy = Sk[1][tx], szz = Sk[2][tx], syz = Sk[3][tx], sxz = Sk[4][tx], sxy = Sk[5][tx];
+
+            const float mu2 = 2.f * m000, lam2mu = lam + mu2;
+            const float d3v3 = dxVx + dyVy + dzVz;
+            const float sx = dyVy + dzVz, sy = dxVx + dzVz, sz = dxVx + dyVy;
+            const float A = lam2mu * tp * d3v3;
+            const float Bx = A - mu2 * ts * sx, By = A - mu2 * ts * sy, Bz = A - mu2 * ts * sz;
+            float rxn = 0.f, ryn = 0.f, rzn = 0.f;
+#pragma unroll
+            for (int m = 0; m < NM; ++m) {
+                r[m] = a.c.c1[m] * r[m] - a.c.c2[m] * Bx * dt;
+                r[3 + m] = a.c.c1[m] * r[3 + m] - a.c.c2[m] * By * dt;
+                r[6 + m] = a.c.c1[m] * r[6 + m] - a.c.c2[m] * Bz * dt;
+                rxn += a.c.d1[m] * r[m];
+                ryn += a.c.d1[m] * r[3 + m];
+                rzn += a.c.d1[m] * r[6 + m];
+            }
+            const float tp1 = 1.f + tp * (1.f + a.c.d2), ts1 = 1.f + ts * (1.f + a.c.d2);
+            const float P2 = lam2mu * tp1 * d3v3;
+            sxx += (P2 - mu2 * ts1 * sx + rxn) * dt;
+            syy += (P2 - mu2 * ts1 * sy + ryn) * dt;
+            szz += (P2 - mu2 * ts1 * sz + rzn) * dt;
+            const float muxz = 4.f * m000 * m100 * m010 * m110 /
+                               (m000 * m100 * m010 + m000 * m100 * m110 + m000 * m010 * m110 + m100 * m010 * m110 + eps);
+            const float muxy = 4.f * m000 * m010 * m001 * m011 /
+                               (m000 * m010 * m001 + m000 * m010 * m011 + m000 * m001 * m011 + m010 * m001 * m011 + eps);
+            const float muyz = 4.f * m000 * m100 * m001 * m101 /
+                               (m000 * m100 * m001 + m000 * m100 * m101 + m000 * m001 * m101 + m100 * m001 * m101 + eps);
+            float ryzn = 0.f, rxzn = 0.f, rxyn = 0.f;
+            const float qyz = muyz * ts * dyVz_dzVy, qxz = muxz * ts * dxVz_dzVx, qxy = muxy * ts * dxVy_dyVx;
+#pragma unroll
+            for (int m = 0; m < NM; ++m) {
+                r[9 + m] = a.c.c1[m] * r[9 + m] - a.c.c2[m] * qyz * dt;
+                r[12 + m] = a.c.c1[m] * r[12 + m] - a.c.c2[m] * qxz * dt;
+                r[15 + m] = a.c.c1[m] * r[15 + m] - a.c.c2[m] * qxy * dt;
+                ryzn += a.c.d1[m] * r[9 + m];
+                rxzn += a.c.d1[m] * r[12 + m];
+                rxyn += a.c.d1[m] * r[15 + m];
+            }
+            syz += (muyz * ts1 * dyVz_dzVy + ryzn) * dt;
+            sxz += (muxz * ts1 * dxVz_dzVx + rxzn) * dt;
+            sxy += (muxy * ts1 * dxVy_dyVx + rxyn) * dt;
+            if (a.cer) {  // Cerjan sponge epilogue (m_absorb_c.f90:113-168)
+                const float gxc = a.cer[a.cer_off[0] + ix], gxb = a.cer[a.cer_off[1] + ix];
+                const float gyc = a.cer[a.cer_off[2] + jy], gyb = a.cer[a.cer_off[3] + jy];
+                const float gzc = a.cer[a.cer_off[4] + k], gzb = a.cer[a.cer_off[5] + k];
+                const float gcc = gxc * gyc * gzc;
+                sxx *= gcc; syy *= gcc; szz *= gcc;
+                syz = syz * gxc * gyb * gzb;
+                sxz = sxz * gxb * gyc * gzb;
+                sxy = sxy * gxb * gyb * gzc;
+            }
+            const long long oS = bS + k * planeS;
+            Sg[oS] = sxx; Sg[oS + P] = syy; Sg[oS + 2 * P] = szz;
+            Sg[oS + 3 * P] = syz; Sg[oS + 4 * P] = sxz; Sg[oS + 5 * P] = sxy;
+            const long long oR = bR + k * rplane;
+#pragma unroll
+            for (int f = 0; f < 18; ++f) St<RT>::st(Rg + oR + (long long)f * a.rpitch, r[f]);
+        }
+        __syncthreads();  // every thread is done with R/S(k), M(k), V(k-2)
+        if (bad) break;
+        if (tid == 0) {
+            fence_proxy_async();
+            if (k + 2 <= kz1 - 1) issueRS(k + 2);
+            if (k + 3 <= kz1) issueM(k + 3);
+            if (k + 4 <= kz1 + 1) issueV(k + 4);
+        }
+    }
+    if (bad) {
+        if (tid == 0) {
+            atomicExch(ta.err, 1);
+            // drain this block's copies still in flight (bounded)
+            for (int s = 0; s < 2; ++s) if (fills[s]) mbar_wait(&sm.barRS[s], (fills[s] - 1) & 1);
+            for (int s = 0; s < 3; ++s) if (fills[2 + s]) mbar_wait(&sm.barM[s], (fills[2 + s] - 1) & 1);
+            for (int s = 0; s < 6; ++s) if (fills[5 + s]) mbar_wait(&sm.barV[s], (fills[5 + s] - 1) & 1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Interior velocity update (m_kernel.f90:75-140), TMA pipeline.
+//   S ring:   8 planes (k-2 .. k+2 for the z stencil, k+3 .. k+5 in flight)
+//   rho ring: 3 planes (k, k+1, k+2 in flight)
+//   V ring:   4 planes (k, k+1 .. k+3 in flight)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__ TArgs ta) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    VelSmem& sm = *reinterpret_cast<VelSmem*>(smraw);
+    int& bad = sm.bad;
+    const ZArgs& a = ta.z;
+    const Geo& g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int xt = a.x0 + blockIdx.x * 32, yt = a.y0 + blockIdx.y * TTY;
+    const int ix = xt + tx, jy = yt + ty;
+    const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
+    const int kz0 = blockIdx.z * a.kchunk;
+    const int kz1 = min(kz0 + a.kchunk, a.kz_end);
+    if (kz0 >= kz1) return;
+
+    constexpr uint32_t BSH = 4 * (TTY + 4) * 6 * 40, BRHO = 4 * (TTY + 1) * 36, BVC = 4 * TTY * 3 * 32;
+    int fills[15];  // S 0-7, rho 8-10, V 11-14
+    if (tid == 0) {
+        for (int s = 0; s < 8; ++s) mbar_init(&sm.barS[s], 1);
+        for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
+        for (int s = 0; s < 4; ++s) mbar_init(&sm.barV[s], 1);
+        fence_barrier_init();
+        bad = 0;
+    }
+    for (int s = 0; s < 15; ++s) fills[s] = 0;
+    const int gx = xt + g.hx, gy = yt + HYT;
+    if (tid == 0) {
+        bool ok = true;
+        for (int s = 0; s < 8; ++s) ok &= tma_ok(&sm.S[s], gx - 4, 4);
+        for (int s = 0; s < 3; ++s) ok &= tma_ok(&sm.M[s], gx, 4);
+        for (int s = 0; s < 4; ++s) ok &= tma_ok(&sm.V[s], gx, 4);
+        if (!ok) { bad = 1; atomicExch(ta.err, 2); }
+    }
+    __syncthreads();
+    if (bad) return;
+    auto issueS = [&](int p) {
+        int s = pmod(p - (kz0 - 2), 8);
+        mbar_expect_tx(&sm.barS[s], BSH);
+        tma_load_4d(&sm.S[s], &ta.tmSh, &sm.barS[s], gx - 4, 0, gy - 2, p + HZT);
+        ++fills[s];
+    };
+    auto issueM = [&](int p) {
+        int s = pmod(p - kz0, 3);
+        mbar_expect_tx(&sm.barM[s], BRHO);
+        tma_load_4d(&sm.M[s], &ta.tmRho, &sm.barM[s], gx, 0, gy, p + HZT);
+        ++fills[8 + s];
+    };
+    auto issueV = [&](int p) {
+        int s = pmod(p - kz0, 4);
+        mbar_expect_tx(&sm.barV[s], BVC);
+        tma_load_4d(&sm.V[s], &ta.tmVc, &sm.barV[s], gx, 0, gy, p + HZT);
+        ++fills[11 + s];
+    };
+    if (tid == 0) {
+        for (int p = kz0 - 2; p <= min(kz0 + 5, kz1 + 1); ++p) issueS(p);
+        for (int p = kz0; p <= min(kz0 + 2, kz1); ++p) issueM(p);
+        for (int p = kz0; p <= min(kz0 + 3, kz1 - 1); ++p) issueV(p);
+    }
+    auto parity = [&](int p, int p0, int n) { return (uint32_t)(((p - p0) / n) & 1); };
+
+    int4 band = make_int4(0, -1, 0, -1);
+    if (act) band = a.band[(size_t)(jy - a.y0) * a.nxi + (ix - a.x0)];
+    const float dt = a.c.dt;
+    const long long planeV = 3LL * g.pitch * g.nyp;
+    const long long bV = (long long)goff(g, 3, 0, ix, jy, 0);
+    float* __restrict__ Vg = a.V;
+    const int P = g.pitch;
+
+    for (int k = kz0; k < kz1; ++k) {
+        bool ok = true;
+        for (int d = -2; d <= 2; ++d) ok &= mbar_wait(&sm.barS[pmod(k + d - kz0 + 2, 8)], parity(k + d, kz0 - 2, 8));
+        ok &= mbar_wait(&sm.barM[pmod(k - kz0, 3)], parity(k, kz0, 3));
+        ok &= mbar_wait(&sm.barM[pmod(k + 1 - kz0, 3)], parity(k + 1, kz0, 3));
+        ok &= mbar_wait(&sm.barV[pmod(k - kz0, 4)], parity(k, kz0, 4));
+        if (!ok) bad = 1;
+        if (act && ok) {
+            const int kk = k + 1;
+            const bool nb = in_band(kk, band);
+            const float e40x = nb ? a.c.e2x : a.c.e4x0, e41x = nb ? 0.f : a.c.e4x1;
+            const float e40y = nb ? a.c.e2y : a.c.e4y0, e41y = nb ? 0.f : a.c.e4y1;
+            const float e40z = nb ? a.c.e2z : a.c.e4z0, e41z = nb ? 0.f : a.c.e4z1;
+            const int lx = tx + 4, ly = ty + 2;
+            float (*Sk)[6][40] = sm.S[pmod(k - kz0 + 2, 8)].d;
+            // plane-k tile fields: 0 Sxx 1 Syy 2 Szz 3 Syz 4 Sxz 5 Sxy
+            auto T = [&](int f, int dy, int dx) { return Sk[ly + dy][f][lx + dx]; };
+            auto zc = [&](int d, int f) { return sm.S[pmod(k + d - kz0 + 2, 8)].d[ly][f][lx]; };
+            const float d3Sx3 = (T(0, 0, 1) - T(0, 0, 0)) * e40x - (T(0, 0, 2) - T(0, 0, -1)) * e41x
+                              + (T(5, 0, 0) - T(5, -1, 0)) * e40y - (T(5, 1, 0) - T(5, -2, 0)) * e41y
+                              + (zc(0, 4) - zc(-1, 4)) * e40z - (zc(1, 4) - zc(-2, 4)) * e41z;
+            const float d3Sy3 = (T(5, 0, 0) - T(5, 0, -1)) * e40x - (T(5, 0, 1) - T(5, 0, -2)) * e41x
+                              + (T(1, 1, 0) - T(1, 0, 0)) * e40y - (T(1, 2, 0) - T(1, -1, 0)) * e41y
+                              + (zc(0, 3) - zc(-1, 3)) * e40z - (zc(1, 3) - zc(-2, 3)) * e41z;
+            const float d3Sz3 = (T(4, 0, 0) - T(4, 0, -1)) * e40x - (T(4, 0, 1) - T(4, 0, -2)) * e41x
+                              + (T(3, 0, 0) - T(3, -1, 0)) * e40y - (T(3, 1, 0) - T(3, -2, 0)) * e41y
+                              + (zc(1, 2) - zc(0, 2)) * e40z - (zc(2, 2) - zc(-1, 2)) * e41z;
+            float (*R0)[36] = sm.M[pmod(k - kz0, 3)].d;
+            float (*R1)[36] = sm.M[pmod(k + 1 - kz0, 3)].d;
+            const float r0 = R0[ty][tx];
+            float (*Vk)[3][32] = sm.V[pmod(k - kz0, 4)].d;
+            float vx = Vk[ty][0][tx] + 2.f / (r0 + R0[ty][tx + 1]) * d3Sx3 * dt;
+            float vy = Vk[ty][1][tx] + 2.f / (r0 + R0[ty + 1][tx]) * d3Sy3 * dt;
+            float vz = Vk[ty][2][tx] + 2.f / (r0 + R1[ty][tx]) * d3Sz3 * dt;
+            if (a.cer) {  // Cerjan sponge epilogue (m_absorb_c.f90:170-198)
+                const float gxc = a.cer[a.cer_off[0] + ix], gxb = a.cer[a.cer_off[1] + ix];
+                const float gyc = a.cer[a.cer_off[2] + jy], gyb = a.cer[a.cer_off[3] + jy];
+                const float gzc = a.cer[a.cer_off[4] + k], gzb = a.cer[a.cer_off[5] + k];
+                vx = vx * gxb * gyc * gzc;
+                vy = vy * gxc * gyb * gzc;
+                vz = vz * gxc * gyc * gzb;
+            }
+            const long long oV = bV + k * planeV;
+            Vg[oV] = vx; Vg[oV + P] = vy; Vg[oV + 2 * P] = vz;
+        }
+        __syncthreads();  // every thread is done with S(k-2), rho(k), V(k)
+        if (bad) break;
+        if (tid == 0) {
+            fence_proxy_async();
+            if (k + 6 <= kz1 + 1) issueS(k + 6);
+            if (k + 3 <= kz1) issueM(k + 3);
+            if (k + 4 <= kz1 - 1) issueV(k + 4);
+        }
+    }
+    if (bad) {
+        if (tid == 0) {
+            atomicExch(ta.err, 1);
+            for (int s = 0; s < 8; ++s) if (fills[s]) mbar_wait(&sm.barS[s], (fills[s] - 1) & 1);
+            for (int s = 0; s < 3; ++s) if (fills[8 + s]) mbar_wait(&sm.barM[s], (fills[8 + s] - 1) & 1);
+            for (int s = 0; s < 4; ++s) if (fills[11 + s]) mbar_wait(&sm.barV[s], (fills[11 + s] - 1) & 1);
+        }
+    }
+}
+
+}  // namespace swpc

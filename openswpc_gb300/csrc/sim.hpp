@@ -6,6 +6,7 @@
 
 #include "../../include/swpc_gpu.h"
 #include "kernels.cuh"
+#include "kernels_tma.cuh"
 
 namespace swpc {
 
@@ -39,8 +40,12 @@ struct Sim {
     int cer_off[6] = {0, 0, 0, 0, 0, 0};
     int* d_it = nullptr;
     int* d_kob = nullptr;
+    int* d_err = nullptr;   // set by a kernel whose bounded wait ran out
     Coef coef{};
     int kchunk = 1, pml_blocks = 1;
+    int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
+    TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
+    size_t smem_stress = 0, smem_vel = 0;
 
     PArgs pml_args{};
     SrcArgs src_args{};
@@ -73,6 +78,7 @@ struct Sim {
     int check_divergence();
     cudaEvent_t get_event();
     int drain_events();
+    int build_tensor_maps();
 };
 
 }  // namespace swpc

@@ -167,10 +167,19 @@ int Sim::launch_step(bool timed) {
     }
     ZArgs z;
     fill_zargs(z);
+    targs.z = z;
+    const dim3 tblk(32, TTY);
+    const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + TTY - 1) / TTY, (p.nzi + kchunk - 1) / kchunk);
     ev0(0);
-    if (p.rbytes == 4) k_stress_interior<float><<<grd, blk, 0, stream>>>(z);
-    else if (dims.store == SWPC_STORE_FP16) k_stress_interior<__half><<<grd, blk, 0, stream>>>(z);
-    else k_stress_interior<__nv_bfloat16><<<grd, blk, 0, stream>>>(z);
+    if (variant == 0) {
+        if (p.rbytes == 4) k_stress_tma<float><<<tgrd, tblk, smem_stress, stream>>>(targs);
+        else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half><<<tgrd, tblk, smem_stress, stream>>>(targs);
+        else k_stress_tma<__nv_bfloat16><<<tgrd, tblk, smem_stress, stream>>>(targs);
+    } else {
+        if (p.rbytes == 4) k_stress_interior<float><<<grd, blk, 0, stream>>>(z);
+        else if (dims.store == SWPC_STORE_FP16) k_stress_interior<__half><<<grd, blk, 0, stream>>>(z);
+        else k_stress_interior<__nv_bfloat16><<<grd, blk, 0, stream>>>(z);
+    }
     ++launches;
     ev1(0);
     if (p.pml) {
@@ -184,7 +193,9 @@ int Sim::launch_step(bool timed) {
         ev1(5);
     }
     ev0(1);
-    k_vel_interior<<<grd, blk, 0, stream>>>(z); ++launches;
+    if (variant == 0) k_vel_tma<<<tgrd, tblk, smem_vel, stream>>>(targs);
+    else k_vel_interior<<<grd, blk, 0, stream>>>(z);
+    ++launches;
     ev1(1);
     if (p.pml) {
         ev0(3);
@@ -244,7 +255,74 @@ int Sim::ensure_graph() {
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// TMA tensor maps over the device groups (cuTensorMapEncodeTiled through the
+// runtime's driver entry point, so the library needs no -lcuda)
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)f;
+    });
+    return fn;
+}
+
+// 4-D map (x, field, y, z) over a row-interleaved group
+static int make_map(CUtensorMap* m, void* base, CUtensorMapDataType dt, int es, long long nx, int nf, long long ny,
+                    long long nz, int bx, int bf, int by) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_err(SWPC_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    cuuint64_t dims[4] = {(cuuint64_t)nx, (cuuint64_t)nf, (cuuint64_t)ny, (cuuint64_t)nz};
+    cuuint64_t strides[3] = {(cuuint64_t)(nx * es), (cuuint64_t)(nx * nf * es), (cuuint64_t)(nx * nf * ny * es)};
+    cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)bf, (cuuint32_t)by, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(m, dt, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_err(SWPC_E_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+    return 0;
+}
+
+int Sim::build_tensor_maps() {
+    const Geo& g = p.g;
+    const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    int rc;
+    if ((rc = make_map(&targs.tmV, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 40, 3, TTY + 4))) return rc;
+    if ((rc = make_map(&targs.tmS, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 32, 6, TTY))) return rc;
+    if ((rc = make_map(&targs.tmM, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 4, TTY + 1))) return rc;
+    if ((rc = make_map(&targs.tmSh, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 40, 6, TTY + 4))) return rc;
+    if ((rc = make_map(&targs.tmRho, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 1, TTY + 1))) return rc;
+    if ((rc = make_map(&targs.tmVc, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 32, 3, TTY))) return rc;
+    const CUtensorMapDataType RTy = dims.store == SWPC_STORE_FP32 ? F
+                                    : dims.store == SWPC_STORE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                    : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    if ((rc = make_map(&targs.tmR, R, RTy, p.rbytes, p.rpitch, 18, p.nyi, p.nzi, 32, 18, TTY))) return rc;
+    targs.err = d_err;
+    smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>);
+    smem_vel = sizeof(VelSmem);
+    CK(cudaFuncSetAttribute(k_stress_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(StressSmem<float>)));
+    CK(cudaFuncSetAttribute(k_stress_tma<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(StressSmem<__half>)));
+    CK(cudaFuncSetAttribute(k_stress_tma<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sizeof(StressSmem<__nv_bfloat16>)));
+    CK(cudaFuncSetAttribute(k_vel_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(VelSmem)));
+    return 0;
+}
+
 int Sim::check_divergence() {
+    if (d_err) {
+        int e = 0;
+        CK(cudaMemcpyAsync(&e, d_err, 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (e) return set_err(SWPC_E_TIMEOUT, "a bounded wait on a shared-memory pipeline barrier ran out");
+    }
     if (vmax_args.ntdec_r <= 0 || !rep_host.size()) return 0;
     CK(cudaMemcpyAsync(rep_host.data(), vmax_args.rep, rep_host.size() * 4, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
@@ -521,6 +599,9 @@ int Sim::allocate() {
     pml_blocks = (int)std::min<long long>((p.npml + 255) / 256, 64LL * nsm);
     if (pml_blocks < 1) pml_blocks = 1;
     graph_steps = 8;
+    if ((rc = dalloc((void**)&d_err, 16))) return rc;
+    variant = dims.reserved[0] == 1 ? 1 : 0;
+    if ((rc = build_tensor_maps())) return rc;
     return 0;
 }
 

@@ -111,7 +111,9 @@ def _ptr(a):
 
 
 def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xbeg=0.0, ybeg=0.0, zbeg=0.0,
-              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0):
+              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0):
+    """swpc_dims for swpc_gpu_create.  variant 0 selects the TMA-fed interior
+    kernels, 1 the shared-memory sweep without TMA (kept for comparison)."""
     d = Dims()
     d.nx, d.ny, d.nz, d.nt, d.na, d.nm = nx, ny, nz, nt, na, 3
     d.abc_type = 0 if abc == "pml" else 1
@@ -119,6 +121,7 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     d.dx, d.dy, d.dz, d.dt = dx, dy, dz, dt
     d.xbeg, d.ybeg, d.zbeg, d.tbeg = xbeg, ybeg, zbeg, tbeg
     d.fcut, d.M0, d.UC, d.ntdec_r = fcut, M0, UC, ntdec_r
+    d.reserved[0] = int(variant)
     return d
 
 

@@ -13,14 +13,14 @@ def misfit(a, b):
     return float(np.linalg.norm((a - b).ravel()) / (nb if nb > 0 else 1.0))
 
 
-def sim_from_oracle(o, store="fp32", nt=None, abc=None, ntdec_r=0, snapshot=None):
+def sim_from_oracle(o, store="fp32", nt=None, abc=None, ntdec_r=0, snapshot=None, variant=0):
     """GPU simulation fed with the oracle's medium, surface maps, relaxation
     times, sources and stations (so both sides see identical inputs)."""
     nt = o.nt if nt is None else nt
     na = o.na
     dims = gpu.make_dims(o.nx, o.ny, o.nz, nt, o.dx, o.dy, o.dz, o.dt, na=na,
                          abc=abc or "pml", store=store, xbeg=o.xbeg, ybeg=o.ybeg, zbeg=o.zbeg, tbeg=o.tbeg,
-                         fcut=o.fcut, M0=o.M0, UC=o.UC, ntdec_r=ntdec_r)
+                         fcut=o.fcut, M0=o.M0, UC=o.UC, ntdec_r=ntdec_r, variant=variant)
     s = gpu.Simulation(dims)
     med = [o.medium(n) for n in ("rho", "lam", "mu", "taup", "taus")]
     maps = [o.medium(n) for n in ("kfs", "kob", "kfs_top", "kfs_bot", "kob_top", "kob_bot")]

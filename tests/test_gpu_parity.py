@@ -21,9 +21,10 @@ def small_inf(tmp_path_factory):
 
 
 @pytest.mark.gpu
-def test_fields_after_few_steps(small_inf):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fields_after_few_steps(small_inf, variant):
     o = pyoracle.Oracle(small_inf, "fp32")
-    s = sim_from_oracle(o)
+    s = sim_from_oracle(o, variant=variant)
     # 40 steps: the source (rise time 1 s, dt 0.02 s) is still injecting
     o.run(40)
     s.run(1, 40)
@@ -35,9 +36,10 @@ def test_fields_after_few_steps(small_inf):
 
 
 @pytest.mark.gpu
-def test_waveforms_match_oracle(small_inf):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_waveforms_match_oracle(small_inf, variant):
     o = pyoracle.Oracle(small_inf, "fp32")
-    s = sim_from_oracle(o)
+    s = sim_from_oracle(o, variant=variant)
     o.run(240)
     s.run(1, 240)
     w_gpu = s.waveforms()
