@@ -135,6 +135,18 @@ int swpc_gpu_vmax(swpc_sim* sim, float out[3]);
  * double: which = 0..8 for Vx Vy Vz Sxx Syy Szz Syz Sxz Sxy. */
 int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out);
 
+/* The same read-back for callers that cannot allocate device memory (a host
+ * whose device is fully committed under an HBM budget, or whose allocator
+ * forbids side allocations).  No counterpart in the reference.  It calls no
+ * cudaMalloc/cudaFree: the gather goes through a fixed 32 MiB scratch array
+ * in the library image that every GPU loading the library holds until exit.
+ * Grids above SWPC_STATIC_FIELD_MAX points are rejected with SWPC_E_ARG.  The
+ * first call on a device looks the array up for that device; make it before
+ * any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU (from different threads or streams) race. */
+#define SWPC_STATIC_FIELD_MAX (4 * 1024 * 1024)
+int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out);
+
 /* Optional per-kernel timing with CUDA events on the simulation's stream:
  * enable = 1 records every launch of the interior and PML kernels (graph
  * replay is bypassed while enabled).  ms[0..5] = accumulated milliseconds of

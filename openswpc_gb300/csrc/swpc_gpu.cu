@@ -526,6 +526,63 @@ int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out) {
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Field read-back without any device allocation.
+//
+// swpc_gpu_fetch_field gathers a field into a temporary device buffer that it
+// allocates and frees on every call.  Some callers cannot allow that: a host
+// that has committed the whole device to resident wavefields under an HBM
+// budget (the temporary allocation would fail on a full device, or would
+// break the budget's accounting), and frameworks whose own allocator owns all
+// device memory and forbids side allocations.  For them the gather goes
+// through this fixed scratch array instead.  It lives in the library image:
+// every GPU that loads the library holds its 32 MiB until the process exits.
+// Fields larger than SWPC_STATIC_FIELD_MAX points are rejected.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_field_scratch[SWPC_STATIC_FIELD_MAX];
+
+// Device address of g_field_scratch, looked up once per device.  In host code
+// the symbol name is only a host-side stand-in, never a device address.
+static int static_scratch(double** out) {
+    static std::mutex mu;
+    static void* addr[128] = {};
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return set_err(SWPC_E_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_field_scratch);
+        if (e != cudaSuccess || !p)
+            return set_err(SWPC_E_CUDA, std::string("cudaGetSymbolAddress(g_field_scratch): ") + cudaGetErrorString(e));
+        addr[dev] = p;
+    }
+    *out = (double*)addr[dev];
+    return 0;
+}
+
+extern "C" int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out || which < 0 || which > 8) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_fetch_field_static");
+    const Geo& g = s->p.g;
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    if (n > (size_t)SWPC_STATIC_FIELD_MAX)
+        return set_err(SWPC_E_ARG, "grid of " + std::to_string(n) + " points exceeds the static read-back limit of " +
+                                       std::to_string((long long)SWPC_STATIC_FIELD_MAX) + " points; use swpc_gpu_fetch_field");
+    double* d = nullptr;
+    int rc = static_scratch(&d);
+    if (rc) return rc;
+    // every one of the n elements copied back is written by the gather first,
+    // so the array needs no clearing
+    if (which < 3) k_gather_d<<<1024, 256, 0, s->stream>>>(s->V, d, g, 3, which);
+    else k_gather_d<<<1024, 256, 0, s->stream>>>(s->S, d, g, 6, which - 3);
+    ++s->launches;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
 int swpc_gpu_profile(swpc_sim* sim, int enable) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s) return set_err(SWPC_E_ARG, "null simulation");

@@ -19,6 +19,7 @@ SWPC_SNAP_XY_V, SWPC_SNAP_XY_U = 1, 2
 STORE = {"fp32": 0, "fp16": 1, "bf16": 2}
 STF = {"boxcar": 0, "triangle": 1, "herrmann": 2, "kupper": 3, "cosine": 4, "scosine": 4, "texp": 5}
 FIELDS = ["Vx", "Vy", "Vz", "Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"]
+STATIC_FIELD_MAX = 4 * 1024 * 1024  # SWPC_STATIC_FIELD_MAX of include/swpc_gpu.h
 
 
 class SwpcError(RuntimeError):
@@ -46,7 +47,7 @@ EXPORTS = [
     "swpc_gpu_fetch_field", "swpc_gpu_profile", "swpc_gpu_profile_read", "swpc_gpu_stream",
     "swpc_gpu_launch_count", "swpc_gpu_destroy", "swpc_gpu_last_error", "swpc_host_prepare",
     "swpc_host_write_sac", "swpc_host_nt", "swpc_host_medium",
-    "swpc_host_check",
+    "swpc_host_check", "swpc_gpu_fetch_field_static",
 ]
 
 
@@ -77,6 +78,7 @@ def lib(build=True):
     L.swpc_gpu_query.argtypes = [vp, ip, ip, ip, ip, ip]
     L.swpc_gpu_vmax.argtypes = [vp, fp]
     L.swpc_gpu_fetch_field.argtypes = [vp, i, dp]
+    L.swpc_gpu_fetch_field_static.argtypes = [vp, i, dp]
     L.swpc_gpu_profile.argtypes = [vp, i]
     L.swpc_gpu_profile_read.argtypes = [vp, dp, ip]
     L.swpc_gpu_stream.argtypes = [vp]
@@ -233,6 +235,16 @@ class Simulation:
             raise SwpcError(-1, "field() needs the dims the simulation was created with")
         out = np.zeros((d.ny, d.nx, d.nz), np.float64)
         _ck(lib().swpc_gpu_fetch_field(self._h, FIELDS.index(name), out.ctypes.data))
+        return out
+
+    def field_static(self, name):
+        """field() through the library's fixed scratch array: no device
+        allocation, grids up to STATIC_FIELD_MAX points."""
+        d = self.dims
+        if d is None:
+            raise SwpcError(-1, "field_static() needs the dims the simulation was created with")
+        out = np.zeros((d.ny, d.nx, d.nz), np.float64)
+        _ck(lib().swpc_gpu_fetch_field_static(self._h, FIELDS.index(name), out.ctypes.data))
         return out
 
     def vmax(self):
