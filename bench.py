@@ -57,6 +57,17 @@ B_INT, B_PML = 236, 228
 KERNEL_BYTES = {"stress_interior": 220, "vel_interior": 52, "stress_pml": 140, "vel_pml": 124}
 
 
+def byte_model(store):
+    """(interior B/pt, PML B/pt, per-kernel B/pt) for a storage precision:
+    16-bit storage halves the 18 memory-variable words (36 RMW words,
+    144 B -> 72 B per interior point); the PML shell and the medium stay FP32."""
+    if store == "fp32":
+        return B_INT, B_PML, dict(KERNEL_BYTES)
+    kb = dict(KERNEL_BYTES)
+    kb["stress_interior"] -= 72
+    return B_INT - 72, B_PML, kb
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -160,11 +171,11 @@ def source_and_stations(w, med, seed):
     return src, mij, sta
 
 
-def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0):
+def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None):
     from openswpc_gb300 import gpu
     dims = gpu.make_dims(w["nx"], w["ny"], w["nz"], nt, w["dx"], w["dx"], w["dx"], w["dt"], na=20, store=store,
                          xbeg=-w["nx"] * w["dx"] / 2, ybeg=-w["ny"] * w["dx"] / 2, zbeg=med["zbeg"], fcut=1.0,
-                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant)
+                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant, concurrent=concurrent)
     sim = gpu.Simulation(dims)
     m = med["maps"]
     sim.upload_medium(med["rho"], med["lam"], med["mu"], med["taup"], med["taus"], m[0], m[1], m[2], m[3], m[4], m[5],
@@ -264,7 +275,7 @@ def run_gpu(args, w):
     t_setup = time.time()
     med = make_medium(w, seed)
     med["src"], med["mij"], med["sta"] = source_and_stations(w, med, seed)
-    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant)
+    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant, concurrent=args.pml_overlap)
     stream = torch.cuda.ExternalStream(sim.stream())
     t_setup = time.time() - t_setup
 
@@ -298,11 +309,12 @@ def run_gpu(args, w):
     npt = w["nx"] * w["ny"] * w["nz"]
     value = world * npt * args.steps / (ms_max / 1e3)
     n_int, n_pml = counts(w)
-    step_bytes = B_INT * n_int + B_PML * n_pml
+    b_int, b_pml, kbytes = byte_model(args.store)
+    step_bytes = b_int * n_int + b_pml * n_pml
     names = ["stress_interior", "vel_interior", "stress_pml", "vel_pml"]
     kavg = {nm: float(kms[q] / max(kn[q], 1)) for q, nm in enumerate(names)}
     units = {"stress_interior": n_int, "vel_interior": n_int, "stress_pml": n_pml, "vel_pml": n_pml}
-    kern = {nm: {"ms": kavg[nm], "GBps": KERNEL_BYTES[nm] * units[nm] / (kavg[nm] / 1e3) / 1e9 if kavg[nm] > 0 else None,
+    kern = {nm: {"ms": kavg[nm], "GBps": kbytes[nm] * units[nm] / (kavg[nm] / 1e3) / 1e9 if kavg[nm] > 0 else None,
                  "share": float(kms[q] / max(kms[:4].sum(), 1e-12))} for q, nm in enumerate(names)}
     top = "stress_interior"
     achieved = kern[top]["GBps"]
@@ -332,7 +344,7 @@ def run_gpu(args, w):
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant)
+        sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant, concurrent=args.pml_overlap)
         sim2.run(1, args.steps)
         wav = sim2.waveforms()
         sim2.close()
@@ -358,14 +370,15 @@ def run_gpu(args, w):
             "config": {"workload": "large single source %dx%dx%d" % (w["nx"], w["ny"], w["nz"]),
                        "dx_km": w["dx"], "dt_s": w["dt"], "nt": w["nt"], "nm": 3, "na": 20, "receivers": w["nst"],
                        "snapshot": "xy_v every %d steps" % w["ntdec_s"], "parallelism": "replicas x%d" % world,
+                       "store": args.store,
                        "l2": "inputs larger than L2 (%.0f GB working set), no flush" % (gpu.required_bytes(
                            gpu.make_dims(w["nx"], w["ny"], w["nz"], w["nt"], w["dx"], w["dx"], w["dx"], w["dt"])) / 1e9)},
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
                                   "peak": peak, "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak,
-                                  "model": "236 B/interior pt + 228 B/PML pt per step"},
+                                  "model": "%d B/interior pt + %d B/PML pt per step" % (b_int, b_pml)},
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "traffic": traffic,
-                         "bytes_per_point": KERNEL_BYTES[top], "peak_source": peak_kind},
+                         "bytes_per_point": kbytes[top], "peak_source": peak_kind},
             "kernels": kern,
             "clocks": clocks,
             "gpu_launches": launches,
@@ -380,20 +393,98 @@ def run_gpu(args, w):
     return 0
 
 
+def batch_inputs(n, seed, nt, root):
+    """The batched many-instance workload: n simulations, each axis drawn
+    uniformly from {96, 128, ..., 256}, dt = 0.02 s, seeded 3-5 layer media,
+    a 50/50 mix of single forces and double couples, 8 receivers each."""
+    from openswpc_gb300 import configs
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice(np.arange(96, 257, 32), size=(n, 3))
+    infs = []
+    for q, (nx, ny, nz) in enumerate(sizes):
+        d = os.path.join(root, "m%03d" % q)
+        infs.append(configs.write_layered(d, int(nx), int(ny), int(nz), seed + q, nt=nt, n_station=8))
+    return infs, sizes
+
+
+def run_batch(args):
+    """Batched form: solves/s of n simulations advanced together versus the
+    same simulations run one after another on the plain path.  Both are
+    timed over K steps (CUDA events) and scaled to the full nt = 1500
+    (steps cost the same throughout a run)."""
+    from openswpc_gb300 import autotune, gpu
+    import torch
+    gpu.lib()
+    n, nt_full = args.nsim, 1500
+    with tempfile.TemporaryDirectory() as root:
+        infs, sizes = batch_inputs(n, 20261203, nt_full, root)
+        sims = [gpu.Simulation.from_inf(f) for f in infs]
+        pts = [int(np.prod(s)) for s in sizes]
+        t0 = time.time()
+        rec = autotune.tune(sims, steps=3)
+        t_tune = time.time() - t0
+        b = gpu.Batch(sims)
+        st = torch.cuda.ExternalStream(b.stream())
+        b.run(args.warmup)
+        b.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = b.launch_count()
+        e0.record(st)
+        b.run(args.steps)
+        e1.record(st)
+        e1.synchronize()
+        ms_batch = e0.elapsed_time(e1) / args.steps
+        launches = b.launch_count() - n0
+        b.close()
+        # the same members one after another, each on its own plain path
+        ms_seq = 0.0
+        for s in sims:
+            s.reset()
+            s.set_zchunk(0)
+            s.run(1, args.warmup)
+            s.sync()
+            stq = torch.cuda.ExternalStream(s.stream())
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(stq)
+            s.run(args.warmup + 1, args.warmup + args.steps)
+            a1.record(stq)
+            a1.synchronize()
+            ms_seq += a0.elapsed_time(a1) / args.steps
+        for s in sims:
+            s.close()
+    solves_batch = n / (nt_full * ms_batch / 1e3)
+    solves_seq = n / (nt_full * ms_seq / 1e3)
+    line = {"metric": "batched solves/s", "value": solves_batch, "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched many-instance: %d simulations, axes in {96..256}, nt=%d" % (n, nt_full),
+                       "points_total": int(sum(pts)), "zchunk": rec["zchunk"]},
+            "sequential_solves_per_s": solves_seq, "speedup_vs_sequential": solves_batch / solves_seq,
+            "grid_pt_updates_per_s": sum(pts) / (ms_batch / 1e3), "autotune": rec, "autotune_s": t_tune,
+            "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--nsim", type=int, default=64, help="members of the batched workload")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])
     ap.add_argument("--variant", type=int, default=0, help="0: TMA-fed interior kernels, 1: plain smem sweep")
+    ap.add_argument("--pml-overlap", type=lambda v: {"auto": None, "on": True, "off": False}[v], default=None,
+                    help="auto|on|off: run the PML kernels beside the interior ones")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "batch":
+        return run_batch(args)
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)

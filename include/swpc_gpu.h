@@ -163,6 +163,37 @@ long long swpc_gpu_launch_count(swpc_sim* sim);
 
 int swpc_gpu_destroy(swpc_sim* sim);
 
+/* The dims the simulation was created with. */
+int swpc_gpu_get_dims(swpc_sim* sim, swpc_dims* out);
+
+/* Return the simulation to its initial state (all wavefields, memory
+ * variables, PML auxiliaries, receiver and snapshot buffers zero; next step
+ * is it = 1) while keeping medium, sources, receivers and snapshot set-up.
+ * Used by the autotuner, which times steps on the real simulations. */
+int swpc_gpu_reset(swpc_sim* sim);
+
+/* z-sweep depth (planes per block) of the interior kernels; 0 restores the
+ * automatic choice.  The autotuner (openswpc_gb300/autotune.py) sets it. */
+int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk);
+int swpc_gpu_get_zchunk(swpc_sim* sim);
+
+/* ------------------------------------------------------------------------
+ * Batched form: n independent simulations (same storage precision, medium
+ * uploaded) advanced together, one fused launch per phase of the time step,
+ * replayed through a CUDA graph.  No counterpart in the reference, which runs
+ * one simulation per process; it replaces running the reference once per
+ * input file (e.g. the Green's-function runs of example/green/).  Each
+ * member continues from its own next step; members keep their own receivers,
+ * snapshots and divergence checks.  Destroying the batch leaves the members.
+ * ---------------------------------------------------------------------- */
+typedef struct swpc_batch swpc_batch;
+int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out);
+int swpc_batch_run(swpc_batch* batch, int nsteps);
+int swpc_batch_sync(swpc_batch* batch);
+void* swpc_batch_stream(swpc_batch* batch);
+long long swpc_batch_launch_count(swpc_batch* batch);
+int swpc_batch_destroy(swpc_batch* batch);
+
 /* Copy the last error message into buf; returns its length. */
 int swpc_gpu_last_error(char* buf, size_t n);
 
@@ -176,6 +207,21 @@ int swpc_gpu_last_error(char* buf, size_t n);
  * Relative file names in input.inf are resolved against the directory of
  * inf_path. */
 int swpc_host_prepare(const char* inf_path, swpc_sim** out);
+
+/* Two-phase form of swpc_host_prepare, for callers that decide when a
+ * simulation may take device memory (the serving loop below):
+ * swpc_host_load runs the whole host set-up (medium, sources, stations) and
+ * touches no GPU; swpc_host_request_bytes gives the device bytes the
+ * simulation will hold; swpc_host_materialize creates and uploads it (the
+ * request can be materialised more than once); swpc_host_request_free
+ * releases the host copy.  Together they equal swpc_host_prepare
+ * (src/swpc_3d/main.f90:48-117). */
+typedef struct swpc_request swpc_request;
+int swpc_host_load(const char* inf_path, swpc_request** out);
+long long swpc_host_request_bytes(const swpc_request* req);
+int swpc_host_request_dims(const swpc_request* req, swpc_dims* out);
+int swpc_host_materialize(const swpc_request* req, swpc_sim** out);
+int swpc_host_request_free(swpc_request* req);
 
 /* Run the whole host set-up of swpc_host_prepare without touching a GPU and
  * write a JSON summary (grid, M0, fcut, relaxation times, source and station
@@ -200,6 +246,57 @@ int swpc_host_medium(int nx, int ny, int nz, int na, double fq_min, double fq_ma
 /* Write the receiver traces as SAC files named
  * odir/wav/<title>.3d.<station>.<cmp>.sac (m_wav.f90:782-792). */
 int swpc_host_write_sac(swpc_sim* sim, const char* odir);
+
+/* ------------------------------------------------------------------------
+ * Serving form: a request loop with continuous batching.  No counterpart in
+ * the reference (one simulation per mpiexec).  Requests are input.inf paths;
+ * host threads run their set-up as they arrive, a request takes device memory
+ * only once the admitted simulations leave room for it inside hbm_budget
+ * (first come, first served), and every admitted simulation is advanced by
+ * one batched launch sequence per quantum of time steps.  Between quanta the
+ * finished simulations hand back their receiver traces and free their memory,
+ * and the requests that became ready join the batch, so new work overlaps
+ * the work already on the GPU.  Wavefields stay resident from admission to
+ * completion.  All functions are thread-safe.
+ * ---------------------------------------------------------------------- */
+typedef struct swpc_server swpc_server;
+typedef struct {
+    double hbm_budget;  /* device bytes the admitted simulations may hold (0: 80% of free memory) */
+    int max_active;     /* most simulations advanced together (0: 128) */
+    int quantum;        /* time steps between scheduling points (0: 50) */
+    int prep_threads;   /* host threads running request set-up (0: 4) */
+    int write_sac;      /* 1: also write each request's SAC files into its odir */
+    int reserved[8];
+} swpc_serve_config;
+
+enum { SWPC_REQ_QUEUED = 0, SWPC_REQ_LOADING = 1, SWPC_REQ_WAITING = 2, SWPC_REQ_RUNNING = 3, SWPC_REQ_DONE = 4 };
+
+int swpc_serve_create(const swpc_serve_config* cfg, swpc_server** out);
+/* Queue one input.inf; *id identifies the request from then on. */
+int swpc_serve_submit(swpc_server* srv, const char* inf_path, long long* id);
+/* State of a request: SWPC_REQ_* or the negative error code it failed with. */
+int swpc_serve_state(swpc_server* srv, long long id);
+/* Block until the request is done or failed, or timeout_s passes (< 0: no
+ * limit); returns its state. */
+int swpc_serve_wait(swpc_server* srv, long long id, double timeout_s);
+/* Receiver traces of a finished request, laid out as swpc_gpu_fetch_waveforms
+ * lays them out ((nst, ncmp, ntw)); with buf null only *nst and *ntw are set.
+ * n_floats is the room in buf. */
+int swpc_serve_result(swpc_server* srv, long long id, int kind, float* buf, size_t n_floats, int* nst, int* ntw);
+/* Error message of a failed request; returns its length. */
+int swpc_serve_error(swpc_server* srv, long long id, char* buf, size_t n);
+/* Server-clock seconds at submission, admission (device memory granted),
+ * first time step and completion. */
+int swpc_serve_times(swpc_server* srv, long long id, double* t4);
+/* Forget a finished request and its traces. */
+int swpc_serve_release(swpc_server* srv, long long id);
+/* Block until every submitted request is done or failed. */
+int swpc_serve_drain(swpc_server* srv);
+/* st[0..9]: done, failed, running, waiting or loading, queued, device bytes
+ * granted, peak device bytes granted, quanta run, batch rebuilds, grid-point
+ * updates performed. */
+int swpc_serve_stats(swpc_server* srv, double* st);
+int swpc_serve_destroy(swpc_server* srv);
 
 #ifdef __cplusplus
 }

@@ -21,7 +21,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
 
 CU_SOURCES = ["swpc_gpu.cu"]
-CXX_SOURCES = ["host.cpp"]
+CXX_SOURCES = ["host.cpp", "serve.cpp"]
 
 
 def _nvcc():
@@ -73,7 +73,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     drv_src = os.path.join(CSRC, "driver_main.cpp")
     if os.path.exists(drv_src):

@@ -95,11 +95,13 @@ def write_plain_small(d, seed=DEFAULT_SEED, nt=1000, **over):
     return os.path.join(d, "input.inf")
 
 
-def write_layered(d, nx, ny, nz, seed, nt=1500, dx=0.5, dt=0.02, n_station=8, body_force=None, **over):
+def write_layered(d, nx, ny, nz, seed, nt=1500, dx=0.5, dt=0.02, n_station=8, body_force=None,
+                  src_depth_max=None, **over):
     """One member of the batched many-instance workload: a seeded 3-5 layer
     medium (Vp 4.5-7.5 km/s sorted with depth, Vs = Vp/1.73,
     rho = 1.74 Vp^0.25, Qp = 600, Qs = 300), a single force or a double
-    couple, and receivers at the free surface."""
+    couple, and receivers at the free surface.  `src_depth_max` (km) caps the
+    source depth, so that short runs record the direct waves."""
     os.makedirs(d, exist_ok=True)
     rng = np.random.default_rng(seed)
     nlay = int(rng.integers(3, 6))
@@ -110,7 +112,7 @@ def write_layered(d, nx, ny, nz, seed, nt=1500, dx=0.5, dt=0.02, n_station=8, bo
     rows = [(float(z), float(1.74 * vp ** 0.25), float(vp), float(vp / 1.73), 600.0, 300.0) for z, vp in zip(depths, vps)]
     if body_force is None:
         body_force = bool(rng.integers(0, 2))
-    xbeg, ybeg, zbeg = -nx * dx / 2, -ny * dx / 2, -1.5 * dx / 0.5 * 0.5
+    xbeg, ybeg = -nx * dx / 2, -ny * dx / 2
     keys = base_keys(nx=nx, ny=ny, nz=nz, nt=nt, dx=dx, dy=dx, dz=dx, dt=dt, xbeg=xbeg, ybeg=ybeg,
                      zbeg=-3 * dx, bf_mode=body_force, stf_format="xy" if body_force else "xym0dc", **over)
     write_inf(os.path.join(d, "input.inf"), keys)
@@ -118,7 +120,10 @@ def write_layered(d, nx, ny, nz, seed, nt=1500, dx=0.5, dt=0.02, n_station=8, bo
     margin = (keys["na"] + 4) * dx
     sx = float(rng.uniform(xbeg + margin, -xbeg - margin))
     sy = float(rng.uniform(ybeg + margin, -ybeg - margin))
-    sz = float(rng.uniform(3 * dx, zmax - (keys["na"] + 6) * dx))
+    zlim = zmax - (keys["na"] + 6) * dx
+    if src_depth_max is not None:
+        zlim = min(zlim, src_depth_max)
+    sz = float(rng.uniform(3 * dx, zlim))
     with open(os.path.join(d, "source.dat"), "w") as f:
         if body_force:
             v = rng.normal(size=3)

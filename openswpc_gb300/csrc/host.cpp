@@ -503,7 +503,24 @@ void write_sac(const std::string& fn, const Meta& m, const Station& st, const ch
     f.write((const char*)dat, (std::streamsize)npts * 4);
 }
 
-int prepare(const char* inf_path, swpc_sim** out, std::string* dry = nullptr) {
+// Everything the host set-up derives from one input.inf, held until the
+// simulation is put on a device: the medium, the source and receiver grid
+// indices and the device dimensions.
+struct Prepared {
+    Meta meta;
+    swpc_dims d{};
+    std::vector<float> rho, lam, mu, tp, tsv;
+    std::vector<int> kfs, kob, kft, kfb, kot, kobb;
+    double ts[3] = {0, 0, 0};
+    std::vector<int> sijk, rijk;
+    std::vector<double> smo, smij, sf3, sprm;
+    int stf = 0, bf_mode = 0, flags = 0, ntdec_w = 1, kinds = 0, k0 = 1, idec = 1, jdec = 1, ntdec_s = 10;
+};
+
+// Host half of the set-up (src/swpc_3d/main.f90:48-117 without the device):
+// parse, build the medium, locate sources and stations.  With `dry` set,
+// only a JSON summary is produced.
+int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     Inf inf(inf_path);
     inf.strict = inf.b("strict_mode", false);
     Params p;
@@ -686,7 +703,8 @@ int prepare(const char* inf_path, swpc_sim** out, std::string* dry = nullptr) {
         return 0;
     }
 
-    swpc_dims d{};
+    swpc_dims& d = P.d;
+    d = swpc_dims{};
     d.nx = p.nx; d.ny = p.ny; d.nz = p.nz; d.nt = p.nt; d.na = p.na; d.nm = 3;
     d.abc_type = p.abc_type == "pml" ? SWPC_ABC_PML : p.abc_type == "cerjan" ? SWPC_ABC_CERJAN : -1;
     if (d.abc_type < 0) throw std::runtime_error("abc_type must be 'pml' or 'cerjan'");
@@ -696,36 +714,60 @@ int prepare(const char* inf_path, swpc_sim** out, std::string* dry = nullptr) {
     d.xbeg = p.xbeg; d.ybeg = p.ybeg; d.zbeg = p.zbeg; d.tbeg = p.tbeg;
     d.fcut = fcut; d.M0 = M0; d.UC = UC; d.ntdec_r = p.ntdec_r;
     meta.M0 = M0; meta.UC = UC;
+    meta.flags = flags;
 
+    P.rho = std::move(rho); P.lam = std::move(lam); P.mu = std::move(mu); P.tp = std::move(tp); P.tsv = std::move(tsv);
+    P.kfs = std::move(kfs); P.kob = std::move(kob); P.kft = std::move(kft); P.kfb = std::move(kfb);
+    P.kot = std::move(kot); P.kobb = std::move(kobb);
+    for (int m = 0; m < 3; ++m) P.ts[m] = ts[m];
+    P.sijk = std::move(sijk); P.smo = std::move(smo); P.smij = std::move(smij); P.sf3 = std::move(sf3);
+    P.sprm = std::move(sprm);
+    P.stf = stf_code(p.stftype);
+    P.bf_mode = p.bf_mode;
+    P.rijk.clear();
+    for (auto& st : meta.st) P.rijk.insert(P.rijk.end(), {st.i, st.j, st.k});
+    P.flags = flags;
+    P.ntdec_w = std::max(1, p.ntdec_w);
+    P.kinds = (p.xy_v ? SWPC_SNAP_XY_V : 0) | (p.xy_u ? SWPC_SNAP_XY_U : 0);
+    P.k0 = std::max(1, std::min(p.nz, x2i(p.z0_xy, p.zbeg, p.dz)));
+    P.idec = p.idec; P.jdec = p.jdec; P.ntdec_s = p.ntdec_s;
+    P.meta = std::move(meta);
+    return 0;
+}
+
+// Device half of the set-up: create the simulation, upload the medium,
+// sources, receivers and snapshot plan.
+int materialize(const Prepared& P, swpc_sim** out) {
     swpc_sim* sim = nullptr;
-    int rc = swpc_gpu_create(&d, &sim);
+    int rc = swpc_gpu_create(&P.d, &sim);
     if (rc) return rc;
     auto bail = [&](int code) { swpc_gpu_destroy(sim); return code; };
-    if ((rc = swpc_gpu_upload_medium(sim, rho.data(), lam.data(), mu.data(), tp.data(), tsv.data(), kfs.data(), kob.data(),
-                                     kft.data(), kfb.data(), kot.data(), kobb.data(), ts)))
+    if ((rc = swpc_gpu_upload_medium(sim, P.rho.data(), P.lam.data(), P.mu.data(), P.tp.data(), P.tsv.data(),
+                                     P.kfs.data(), P.kob.data(), P.kft.data(), P.kfb.data(), P.kot.data(),
+                                     P.kobb.data(), P.ts)))
         return bail(rc);
-    int ns = (int)smo.size();
-    if ((rc = swpc_gpu_set_sources(sim, ns, sijk.data(), smo.data(), smij.data(), sf3.data(), sprm.data(),
-                                   stf_code(p.stftype), p.bf_mode)))
+    if ((rc = swpc_gpu_set_sources(sim, (int)P.smo.size(), P.sijk.data(), P.smo.data(), P.smij.data(), P.sf3.data(),
+                                   P.sprm.data(), P.stf, P.bf_mode)))
         return bail(rc);
-    std::vector<int> rijk;
-    for (auto& st : meta.st) rijk.insert(rijk.end(), {st.i, st.j, st.k});
-    if ((rc = swpc_gpu_set_receivers(sim, (int)meta.st.size(), rijk.data(), std::max(1, p.ntdec_w), flags)))
+    if ((rc = swpc_gpu_set_receivers(sim, (int)P.meta.st.size(), P.rijk.data(), P.ntdec_w, P.flags)))
         return bail(rc);
-    int kinds = (p.xy_v ? SWPC_SNAP_XY_V : 0) | (p.xy_u ? SWPC_SNAP_XY_U : 0);
-    if (kinds) {
-        int k0 = x2i(p.z0_xy, p.zbeg, p.dz);
-        if ((rc = swpc_gpu_set_snapshot(sim, kinds, std::max(1, std::min(p.nz, k0)), p.idec, p.jdec, p.ntdec_s)))
-            return bail(rc);
-    }
-    meta.flags = flags;
+    if (P.kinds && (rc = swpc_gpu_set_snapshot(sim, P.kinds, P.k0, P.idec, P.jdec, P.ntdec_s)))
+        return bail(rc);
+    Meta meta = P.meta;
     swpc_gpu_query(sim, &meta.ntw, nullptr, nullptr, nullptr, nullptr);
     {
         std::lock_guard<std::mutex> lk(g_meta_mu);
-        g_meta[sim] = meta;
+        g_meta[sim] = std::move(meta);
     }
     *out = sim;
     return 0;
+}
+
+int prepare(const char* inf_path, swpc_sim** out, std::string* dry = nullptr) {
+    Prepared P;
+    int rc = load(inf_path, P, dry);
+    if (rc || dry) return rc;
+    return materialize(P, out);
 }
 
 }  // namespace
@@ -751,6 +793,52 @@ int swpc_host_prepare(const char* inf_path, swpc_sim** out) {
     } catch (const std::exception& e) {
         return swpc::set_err(SWPC_E_IO, e.what());
     }
+}
+
+struct swpc_request {
+    Prepared P;
+};
+
+int swpc_host_load(const char* inf_path, swpc_request** out) {
+    if (!inf_path || !out) return swpc::set_err(SWPC_E_ARG, "null argument");
+    *out = nullptr;
+    try {
+        auto* r = new swpc_request();
+        int rc = load(inf_path, r->P);
+        if (rc) { delete r; return rc; }
+        *out = r;
+        return 0;
+    } catch (const std::bad_alloc&) {
+        return swpc::set_err(SWPC_E_NOMEM, "host memory exhausted while loading " + std::string(inf_path));
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
+}
+
+long long swpc_host_request_bytes(const swpc_request* req) {
+    if (!req) return swpc::set_err(SWPC_E_ARG, "null request");
+    return (long long)swpc_gpu_required_bytes(&req->P.d);
+}
+
+int swpc_host_request_dims(const swpc_request* req, swpc_dims* out) {
+    if (!req || !out) return swpc::set_err(SWPC_E_ARG, "null argument");
+    *out = req->P.d;
+    return 0;
+}
+
+int swpc_host_materialize(const swpc_request* req, swpc_sim** out) {
+    if (!req || !out) return swpc::set_err(SWPC_E_ARG, "null argument");
+    *out = nullptr;
+    try {
+        return materialize(req->P, out);
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
+}
+
+int swpc_host_request_free(swpc_request* req) {
+    delete req;
+    return 0;
 }
 
 int swpc_host_check(const char* inf_path, char* summary, size_t n) {

@@ -408,7 +408,9 @@ struct PmlBox {
     int x0, y0, z0, nx, ny, nz;
     int pitch;           // ADE row pitch
     long long off;       // offset of this box in the ADE buffers (elements)
-    long long first;     // first linear point index of this box
+    long long first;     // first point of this box in the shell (points are counted box by box)
+    // launch tiling: 32 x TBY column tiles, each sweeping a chunk of zc planes
+    int tiles_x, tiles_y, zc, nzc, first_block;
 };
 
 struct PArgs {
@@ -426,39 +428,51 @@ struct PArgs {
     float r20x, r20y, r20z, dt;
 };
 
-__device__ __forceinline__ int find_box(const PArgs& a, long long p) {
-    int b = 0;
-#pragma unroll
-    for (int q = 1; q < 5; ++q)
-        if (q < a.nbox && p >= a.box[q].first) b = q;
-    return b;
-}
-
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
-__global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) {
+// Shell point p -> (box, x, y, z): points are numbered box by box, x fastest.
+// The per-box count fits in 32 bits, so the decomposition is two 32-bit
+// divisions by the box extents.
+struct PmlPt {
+    int b, lx, ly, lz;
+};
+__device__ __forceinline__ PmlPt pml_point(const PArgs& a, long long p) {
+    PmlPt r;
+    r.b = 0;
+#pragma unroll
+    for (int q = 1; q < 5; ++q)
+        if (q < a.nbox && p >= a.box[q].first) r.b = q;
+    const PmlBox& B = a.box[r.b];
+    const unsigned q = (unsigned)(p - B.first);
+    const unsigned t = q / (unsigned)B.nx;
+    r.lx = (int)(q - t * (unsigned)B.nx);
+    r.lz = (int)(t / (unsigned)B.ny);
+    r.ly = (int)(t - (unsigned)r.lz * (unsigned)B.ny);
+    return r;
+}
+
+// PML stress update (m_absorb_p.f90:429-531) at shell point p.
+__device__ __forceinline__ void stress_pml_pt(const PArgs& a, const long long p) {
+    if (p >= a.npts) return;
+    const PmlPt c = pml_point(a, p);
+    const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
     const float eps = 1.1920928955078125e-07f;
     const int P = g.pitch;
-    const size_t rowV = (size_t)3 * P, planeV = rowV * g.nyp;
-    const size_t rowM = (size_t)5 * P;
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.npts; p += (long long)gridDim.x * blockDim.x) {
-        const int b = find_box(a, p);
-        const PmlBox& B = a.box[b];
-        long long q = p - B.first;
-        const int lx = (int)(q % B.nx);
-        q /= B.nx;
-        const int ly = (int)(q % B.ny);
-        const int lz = (int)(q / B.ny);
-        const int ix = B.x0 + lx, jy = B.y0 + ly, kz = B.z0 + lz;
-        const size_t oV = goff(g, 3, 0, ix, jy, kz);
-        const size_t oM = goff(g, 5, 0, ix, jy, kz);
-        const size_t oS = goff(g, 6, 0, ix, jy, kz);
-        const size_t oA = (size_t)B.off + ((size_t)(lz * B.ny + ly) * 9) * B.pitch + lx;
-        const float* __restrict__ V = a.V;
-        const float* __restrict__ M = a.M;
-        const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
-        const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
+    const long long rowV = 3LL * P, planeV = rowV * g.nyp;
+    const long long rowM = 5LL * P, planeM = rowM * g.nyp;
+    const int ix = B.x0 + c.lx, jy = B.y0 + c.ly, kz = B.z0 + c.lz;
+    const long long oV = (long long)goff(g, 3, 0, ix, jy, kz);
+    const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
+    const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
+    const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
+    const float* __restrict__ V = a.V;
+    const float* __restrict__ M = a.M;
+    float* __restrict__ S = a.S;
+    const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
+    const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
+    const int AP = B.pitch;
+    {
         const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
         const float vx = V[oV], vy = V[oV + P], vz = V[oV + 2 * P];
         // normal part (m_absorb_p.f90:453-474)
@@ -469,12 +483,10 @@ __global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) {
         const float lam2mu = lamv + 2.f * muv;
         const float lamR = lam2mu - 2.f * muv;
         float* A = a.adeV + oA;
-        const int AP = B.pitch;
         const float aVx = A[0], aVy = A[AP], aVz = A[2 * AP];
         const float dxa = gxc.x * dxVx + gxc.y * aVx;
         const float dya = gyc.x * dyVy + gyc.y * aVy;
         const float dza = gzc.x * dzVz + gzc.y * aVz;
-        float* S = a.S;
         S[oS] += (lam2mu * dxa + lamR * (dya + dza)) * a.dt;
         S[oS + P] += (lam2mu * dya + lamR * (dxa + dza)) * a.dt;
         S[oS + 2 * P] += (lam2mu * dza + lamR * (dxa + dya)) * a.dt;
@@ -488,7 +500,6 @@ __global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) {
         const float dyVz = (V[oV + 2 * P + rowV] - vz) * a.r20y;
         const float dzVx = (V[oV + planeV] - vx) * a.r20z;
         const float dzVy = (V[oV + P + planeV] - vy) * a.r20z;
-        const size_t planeM = rowM * g.nyp;
         const float m000 = muv, m100 = M[oM + 2 * P + planeM], m010 = M[oM + 2 * P + 1], m110 = M[oM + 2 * P + planeM + 1];
         const float m001 = M[oM + 2 * P + rowM], m011 = M[oM + 2 * P + rowM + 1], m101 = M[oM + 2 * P + planeM + rowM];
         const float muxz = 4.f * m000 * m100 * m010 * m110 /
@@ -510,28 +521,27 @@ __global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_vel_pml(const PArgs a) {
+// PML velocity update (m_absorb_p.f90:246-317) at shell point p.
+__device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
+    if (p >= a.npts) return;
+    const PmlPt c = pml_point(a, p);
+    const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
     const int P = g.pitch;
-    const size_t rowS = (size_t)6 * P, planeS = rowS * g.nyp;
-    const size_t rowM = (size_t)5 * P, planeM = rowM * g.nyp;
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.npts; p += (long long)gridDim.x * blockDim.x) {
-        const int b = find_box(a, p);
-        const PmlBox& B = a.box[b];
-        long long q = p - B.first;
-        const int lx = (int)(q % B.nx);
-        q /= B.nx;
-        const int ly = (int)(q % B.ny);
-        const int lz = (int)(q / B.ny);
-        const int ix = B.x0 + lx, jy = B.y0 + ly, kz = B.z0 + lz;
-        const size_t oV = goff(g, 3, 0, ix, jy, kz);
-        const size_t oM = goff(g, 5, 0, ix, jy, kz);
-        const size_t oS = goff(g, 6, 0, ix, jy, kz);
-        const size_t oA = (size_t)B.off + ((size_t)(lz * B.ny + ly) * 9) * B.pitch + lx;
-        const float* __restrict__ S = a.S;
-        const float* __restrict__ M = a.M;
-        const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
-        const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
+    const long long rowS = 6LL * P, planeS = rowS * g.nyp;
+    const long long rowM = 5LL * P, planeM = rowM * g.nyp;
+    const int ix = B.x0 + c.lx, jy = B.y0 + c.ly, kz = B.z0 + c.lz;
+    const long long oV = (long long)goff(g, 3, 0, ix, jy, kz);
+    const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
+    const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
+    const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
+    const float* __restrict__ S = a.S;
+    const float* __restrict__ M = a.M;
+    float* __restrict__ V = a.V;
+    const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
+    const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
+    const int AP = B.pitch;
+    {
         const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
         // m_absorb_p.f90:265-305
         const float sxx = S[oS], syy = S[oS + P], szz = S[oS + 2 * P];
@@ -550,10 +560,8 @@ __global__ void __launch_bounds__(256) k_vel_pml(const PArgs a) {
         const float by = 2.f / (r0 + M[oM + rowM]);
         const float bz = 2.f / (r0 + M[oM + planeM]);
         float* A = a.adeS + oA;
-        const int AP = B.pitch;
         const float axSxx = A[0], aySxy = A[AP], azSxz = A[2 * AP], axSxy = A[3 * AP], aySyy = A[4 * AP];
         const float azSyz = A[5 * AP], axSxz = A[6 * AP], aySyz = A[7 * AP], azSzz = A[8 * AP];
-        float* V = a.V;
         V[oV] += bx * (gxe.x * dxSxx + gyc.x * dySxy + gzc.x * dzSxz + gxe.y * axSxx + gyc.y * aySxy + gzc.y * azSxz) * a.dt;
         V[oV + P] += by * (gxc.x * dxSxy + gye.x * dySyy + gzc.x * dzSyz + gxc.y * axSxy + gye.y * aySyy + gzc.y * azSyz) * a.dt;
         V[oV + 2 * P] += bz * (gxc.x * dxSxz + gyc.x * dySyz + gze.x * dzSzz + gxc.y * axSxz + gyc.y * aySyz + gze.y * azSzz) * a.dt;
@@ -567,6 +575,19 @@ __global__ void __launch_bounds__(256) k_vel_pml(const PArgs a) {
         A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
         A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
     }
+}
+
+// one thread per shell point; batched: block b covers points
+// [256 e.y, 256 e.y + 256) of simulation e.x, e = blocks[b]
+__global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * 256LL + threadIdx.x); }
+__global__ void __launch_bounds__(256) k_vel_pml(const PArgs a) { vel_pml_pt(a, blockIdx.x * 256LL + threadIdx.x); }
+__global__ void __launch_bounds__(256) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+    const int2 e = blocks[blockIdx.x];
+    stress_pml_pt(all[e.x], e.y * 256LL + threadIdx.x);
+}
+__global__ void __launch_bounds__(256) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+    const int2 e = blocks[blockIdx.x];
+    vel_pml_pt(all[e.x], e.y * 256LL + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -611,6 +632,7 @@ struct SrcArgs {
     const float* fxyz;   // 3n
     const float* prm;    // 2n
     int n, stf;
+    int bf;              // 1: body forces (velocity), 0: moment tensors (stress)
     float tbeg, dt, dt_dxyz;
     const int* it;       // device step counter
 };
@@ -620,9 +642,8 @@ struct SrcArgs {
 __device__ __forceinline__ bool in_xy(const Geo& g, int ix, int jy) { return ix >= 0 && ix < g.nx && jy >= 0 && jy < g.ny; }
 
 // m_source.f90:776-848
-__global__ void k_stressglut(const SrcArgs a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n) return;
+__device__ __forceinline__ void stressglut_one(const SrcArgs& a, const int s) {
+    if (s >= a.n || a.bf) return;
     const int it = *a.it;
     const float t = a.tbeg + ((float)it - 0.5f) * a.dt;
     const float st = momentrate(t, a.stf, a.prm[2 * s], a.prm[2 * s + 1]);
@@ -643,9 +664,8 @@ __global__ void k_stressglut(const SrcArgs a) {
 }
 
 // m_source.f90:850-898
-__global__ void k_bodyforce(const SrcArgs a) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n) return;
+__device__ __forceinline__ void bodyforce_one(const SrcArgs& a, const int s) {
+    if (s >= a.n || !a.bf) return;
     const int it = *a.it;
     const float st = momentrate(a.tbeg + (float)it * a.dt, a.stf, a.prm[2 * s], a.prm[2 * s + 1]);
     const int i = a.ijk[3 * s], j = a.ijk[3 * s + 1], k = a.ijk[3 * s + 2];
@@ -663,6 +683,11 @@ __global__ void k_bodyforce(const SrcArgs a) {
     add(2, i, j, k, 2.f / (r0 + rho(i, j, k + 1)), f[2]);
     add(2, i, j, k - 1, 2.f / (r0 + rho(i, j, k - 1)), f[2]);
 }
+
+__global__ void k_stressglut(const SrcArgs a) { stressglut_one(a, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_bodyforce(const SrcArgs a) { bodyforce_one(a, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_stressglut_batch(const SrcArgs* __restrict__ all) { stressglut_one(all[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_bodyforce_batch(const SrcArgs* __restrict__ all) { bodyforce_one(all[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x); }
 
 struct TapArgs {
     Geo g;
@@ -682,8 +707,7 @@ struct TapArgs {
 };
 
 // m_wav.f90:397-625: taps of the *previous* step's velocity/stress
-__global__ void k_taps(const TapArgs a) {
-    int n = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void taps_one(const TapArgs& a, const int n) {
     if (n >= a.n) return;
     const int it = *a.it;
     const Geo& g = a.g;
@@ -754,6 +778,9 @@ __global__ void k_taps(const TapArgs a) {
     }
 }
 
+__global__ void k_taps(const TapArgs a) { taps_one(a, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_taps_batch(const TapArgs* __restrict__ all) { taps_one(all[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x); }
+
 struct SnapArgs {
     Geo g;
     const float* V;
@@ -767,10 +794,8 @@ struct SnapArgs {
 };
 
 // m_snap.f90:1587-1653 (xy_v) and 1963-2025 (xy_u)
-__global__ void k_snap_xy(const SnapArgs a) {
-    const int ii = blockIdx.x * blockDim.x + threadIdx.x;
-    const int jj = blockIdx.y;
-    if (ii >= a.nxs || jj >= a.nys) return;
+__device__ __forceinline__ void snap_one(const SnapArgs& a, const int ii, const int jj) {
+    if (!a.kinds || ii >= a.nxs || jj >= a.nys) return;
     const int it = *a.it;
     const int i = (ii + 1) * a.idec - a.idec / 2 - 1;
     const int j = (jj + 1) * a.jdec - a.jdec / 2 - 1;
@@ -790,6 +815,11 @@ __global__ void k_snap_xy(const SnapArgs a) {
         for (int c = 0; c < 3; ++c) a.xy_u[(size_t)fr * 3 * pl + c * pl + q] = (float)a.uacc[q + c * pl];
 }
 
+__global__ void k_snap_xy(const SnapArgs a) { snap_one(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y); }
+__global__ void k_snap_xy_batch(const SnapArgs* __restrict__ all) {
+    snap_one(all[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
 struct VmaxArgs {
     Geo g;
     const float* V;
@@ -801,7 +831,7 @@ struct VmaxArgs {
 };
 
 // m_kernel.f90:350-374 (+ the NaN check the report's divergence test implies)
-__global__ void k_vmax(const VmaxArgs a) {
+__device__ __forceinline__ void vmax_block(const VmaxArgs& a) {
     const int it = *a.it;
     if (a.ntdec_r <= 0 || it % a.ntdec_r != 0) return;
     const int r = it / a.ntdec_r - 1;
@@ -827,8 +857,15 @@ __global__ void k_vmax(const VmaxArgs a) {
     }
 }
 
+__global__ void k_vmax(const VmaxArgs a) { vmax_block(a); }
+__global__ void k_vmax_batch(const VmaxArgs* __restrict__ all) { vmax_block(all[blockIdx.y]); }
+
 __global__ void k_set_it(int* it, int v) { *it = v; }
 __global__ void k_advance(int* it) { *it += 1; }
+__global__ void k_advance_batch(int* const* __restrict__ its, int n) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) *its[q] += 1;
+}
 
 // Fortran (k,i,j) halo array -> one field of a device group (upload)
 __global__ void k_scatter_f(const float* src, float* dst, Geo g, int nf, int f, int store_kind, void* dst16) {

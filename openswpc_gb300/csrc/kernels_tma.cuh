@@ -104,7 +104,30 @@ __device__ __forceinline__ bool tma_ok(const void* dst, int x, int esize) {
     return (smem_u32(dst) & 127u) == 0 && ((x * esize) & 15) == 0 && x >= 0;
 }
 
-__device__ __forceinline__ int pmod(int a, int n) { int r = a % n; return r < 0 ? r + n : r; }
+// Position of a plane in a ring of N slots that is filled in plane order:
+// the slot and the parity of the fill it belongs to.
+template <int N>
+struct RingPos {
+    int slot;
+    uint32_t par;
+    __device__ __forceinline__ void advance() {
+        if (++slot == N) { slot = 0; par ^= 1u; }
+    }
+};
+
+// Producer bookkeeping for the bounded drain: bit s of `used` marks a slot
+// that has been filled, bit s of `last` the parity of its latest fill.
+struct FillLog {
+    uint32_t used = 0, last = 0;
+    __device__ __forceinline__ void note(int s, uint32_t par) {
+        used |= 1u << s;
+        last = (last & ~(1u << s)) | (par << s);
+    }
+    __device__ __forceinline__ void drain(uint64_t* bars, int n) const {
+        for (int s = 0; s < n; ++s)
+            if (used & (1u << s)) mbar_wait(&bars[s], (last >> s) & 1u);
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Interior stress update (m_kernel.f90:142-348), TMA pipeline.
@@ -112,24 +135,27 @@ __device__ __forceinline__ int pmod(int a, int n) { int r = a % n; return r < 0 
 //   M ring:   3 planes (k, k+1 for mu(k+1), k+2 in flight)
 //   V ring:   6 planes (k-2 .. k+2 for the z stencil, k+3 in flight)
 // ---------------------------------------------------------------------------
+// One 32 x TTY column tile and z chunk (bx, by, bz) of one simulation; `ta`
+// lives in kernel parameter space (single simulation) or in global memory
+// (batched launch).
 template <class RT>
-__global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constant__ TArgs ta) {
+__device__ __forceinline__ void stress_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
     extern __shared__ __align__(128) unsigned char smraw[];
     StressSmem<RT>& sm = *reinterpret_cast<StressSmem<RT>*>(smraw);
     int& bad = sm.bad;
     const ZArgs& a = ta.z;
+    const Coef cf = a.c;
     const Geo& g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int xt = a.x0 + blockIdx.x * 32, yt = a.y0 + blockIdx.y * TTY;
+    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TTY;
     const int ix = xt + tx, jy = yt + ty;
     const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
-    const int kz0 = blockIdx.z * a.kchunk;
+    const int kz0 = bz * a.kchunk;
     const int kz1 = min(kz0 + a.kchunk, a.kz_end);
     if (kz0 >= kz1) return;
 
     constexpr uint32_t BR = sizeof(RT) * TTY * 18 * 32, BS = 4 * TTY * 6 * 32;
     constexpr uint32_t BM = 4 * (TTY + 1) * 4 * 36, BV = 4 * (TTY + 4) * 3 * 40;
-    int fills[11];  // producer bookkeeping: fills per slot (RS 0-1, M 2-4, V 5-10)
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) mbar_init(&sm.barRS[s], 1);
         for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
@@ -137,7 +163,6 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
         fence_barrier_init();
         bad = 0;
     }
-    for (int s = 0; s < 11; ++s) fills[s] = 0;
     const int gxS = xt + g.hx, gyS = yt + HYT;
     if (tid == 0) {
         bool ok = true;
@@ -149,35 +174,46 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
     __syncthreads();
     if (bad) return;
 
-    auto issueRS = [&](int p) {
-        int s = pmod(p - kz0, 2);
+    // producer (thread 0): next plane and ring position of every stream
+    int nRS = kz0, nM = kz0, nV = kz0 - 2;
+    RingPos<2> pRS{0, 0u};
+    RingPos<3> pM{0, 0u};
+    RingPos<6> pV{0, 0u};
+    FillLog lRS, lM, lV;
+    auto issueRS = [&]() {
+        const int s = pRS.slot;
         mbar_expect_tx(&sm.barRS[s], BR + BS);
-        tma_load_4d(&sm.R[s], &ta.tmR, &sm.barRS[s], xt - a.x0, 0, yt - a.y0, p);
-        tma_load_4d(&sm.S[s], &ta.tmS, &sm.barRS[s], gxS, 0, gyS, p + HZT);
-        ++fills[s];
+        tma_load_4d(&sm.R[s], &ta.tmR, &sm.barRS[s], xt - a.x0, 0, yt - a.y0, nRS);
+        tma_load_4d(&sm.S[s], &ta.tmS, &sm.barRS[s], gxS, 0, gyS, nRS + HZT);
+        lRS.note(s, pRS.par);
+        pRS.advance();
+        ++nRS;
     };
-    auto issueM = [&](int p) {
-        int s = pmod(p - kz0, 3);
+    auto issueM = [&]() {
+        const int s = pM.slot;
         mbar_expect_tx(&sm.barM[s], BM);
-        tma_load_4d(&sm.M[s], &ta.tmM, &sm.barM[s], gxS, 1, gyS, p + HZT);
-        ++fills[2 + s];
+        tma_load_4d(&sm.M[s], &ta.tmM, &sm.barM[s], gxS, 1, gyS, nM + HZT);
+        lM.note(s, pM.par);
+        pM.advance();
+        ++nM;
     };
-    auto issueV = [&](int p) {
-        int s = pmod(p - (kz0 - 2), 6);
+    auto issueV = [&]() {
+        const int s = pV.slot;
         mbar_expect_tx(&sm.barV[s], BV);
-        tma_load_4d(&sm.V[s], &ta.tmV, &sm.barV[s], gxS - 4, 0, gyS - 2, p + HZT);
-        ++fills[5 + s];
+        tma_load_4d(&sm.V[s], &ta.tmV, &sm.barV[s], gxS - 4, 0, gyS - 2, nV + HZT);
+        lV.note(s, pV.par);
+        pV.advance();
+        ++nV;
     };
     if (tid == 0) {
-        for (int p = kz0; p <= min(kz0 + 1, kz1 - 1); ++p) issueRS(p);
-        for (int p = kz0; p <= min(kz0 + 2, kz1); ++p) issueM(p);
-        for (int p = kz0 - 2; p <= min(kz0 + 3, kz1 + 1); ++p) issueV(p);
+        while (nRS <= min(kz0 + 1, kz1 - 1)) issueRS();
+        while (nM <= min(kz0 + 2, kz1)) issueM();
+        while (nV <= min(kz0 + 3, kz1 + 1)) issueV();
     }
-    auto parity = [&](int p, int p0, int n) { return (uint32_t)(((p - p0) / n) & 1); };
 
     int4 band = make_int4(0, -1, 0, -1);
     if (act) band = a.band[(size_t)(jy - a.y0) * a.nxi + (ix - a.x0)];
-    const float dt = a.c.dt;
+    const float dt = cf.dt;
     const float eps = 1.1920928955078125e-07f;
     const long long planeS = 6LL * g.pitch * g.nyp;
     const long long bS = (long long)goff(g, 6, 0, ix, jy, 0);
@@ -187,21 +223,28 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
     RT* __restrict__ Rg = (RT*)a.R;
     const int P = g.pitch;
 
-    for (int k = kz0; k < kz1; ++k) {
-        bool ok = mbar_wait(&sm.barRS[pmod(k - kz0, 2)], parity(k, kz0, 2));
-        ok &= mbar_wait(&sm.barM[pmod(k - kz0, 3)], parity(k, kz0, 3));
-        ok &= mbar_wait(&sm.barM[pmod(k + 1 - kz0, 3)], parity(k + 1, kz0, 3));
-        for (int d = -2; d <= 2; ++d) ok &= mbar_wait(&sm.barV[pmod(k + d - kz0 + 2, 6)], parity(k + d, kz0 - 2, 6));
-        if (!ok) bad = 1;
+    // consumer ring positions: R+S of plane k, M of plane k+1, V of plane k+2;
+    // the slots of M(k) and of V(k-2 .. k+1) ride along
+    RingPos<2> cRS{0, 0u};
+    RingPos<3> cM1{1, 0u};
+    RingPos<6> cV2{4, 0u};
+    int sM0 = 0, sV[5] = {0, 1, 2, 3, 4};
+    bool ok = mbar_wait(&sm.barM[0], 0u);
+    for (int q = 0; q < 4; ++q) ok &= mbar_wait(&sm.barV[q], 0u);
 
-        const int sRS = pmod(k - kz0, 2), sM0 = pmod(k - kz0, 3), sM1 = pmod(k + 1 - kz0, 3);
-        const int sV[5] = {pmod(k - kz0, 6), pmod(k - kz0 + 1, 6), pmod(k - kz0 + 2, 6), pmod(k - kz0 + 3, 6), pmod(k - kz0 + 4, 6)};
+    for (int k = kz0; k < kz1; ++k) {
+        ok &= mbar_wait(&sm.barRS[cRS.slot], cRS.par);
+        ok &= mbar_wait(&sm.barM[cM1.slot], cM1.par);
+        ok &= mbar_wait(&sm.barV[cV2.slot], cV2.par);
+        if (!ok) bad = 1;
+        const int sRS = cRS.slot, sM1 = cM1.slot;
+        sV[4] = cV2.slot;
         if (act && ok) {
             const int kk = k + 1;
             const bool nb = in_band(kk, band);
-            const float e40x = nb ? a.c.e2x : a.c.e4x0, e41x = nb ? 0.f : a.c.e4x1;
-            const float e40y = nb ? a.c.e2y : a.c.e4y0, e41y = nb ? 0.f : a.c.e4y1;
-            const float e40z = nb ? a.c.e2z : a.c.e4z0, e41z = nb ? 0.f : a.c.e4z1;
+            const float e40x = nb ? cf.e2x : cf.e4x0, e41x = nb ? 0.f : cf.e4x1;
+            const float e40y = nb ? cf.e2y : cf.e4y0, e41y = nb ? 0.f : cf.e4y1;
+            const float e40z = nb ? cf.e2z : cf.e4z0, e41z = nb ? 0.f : cf.e4z1;
             const int lx = tx + 4, ly = ty + 2;
             // V(k) plane tile: [y][c][x]
             float (*Vk)[3][40] = sm.V[sV[2]].d;
@@ -242,14 +285,14 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
             float rxn = 0.f, ryn = 0.f, rzn = 0.f;
 #pragma unroll
             for (int m = 0; m < NM; ++m) {
-                r[m] = a.c.c1[m] * r[m] - a.c.c2[m] * Bx * dt;
-                r[3 + m] = a.c.c1[m] * r[3 + m] - a.c.c2[m] * By * dt;
-                r[6 + m] = a.c.c1[m] * r[6 + m] - a.c.c2[m] * Bz * dt;
-                rxn += a.c.d1[m] * r[m];
-                ryn += a.c.d1[m] * r[3 + m];
-                rzn += a.c.d1[m] * r[6 + m];
+                r[m] = cf.c1[m] * r[m] - cf.c2[m] * Bx * dt;
+                r[3 + m] = cf.c1[m] * r[3 + m] - cf.c2[m] * By * dt;
+                r[6 + m] = cf.c1[m] * r[6 + m] - cf.c2[m] * Bz * dt;
+                rxn += cf.d1[m] * r[m];
+                ryn += cf.d1[m] * r[3 + m];
+                rzn += cf.d1[m] * r[6 + m];
             }
-            const float tp1 = 1.f + tp * (1.f + a.c.d2), ts1 = 1.f + ts * (1.f + a.c.d2);
+            const float tp1 = 1.f + tp * (1.f + cf.d2), ts1 = 1.f + ts * (1.f + cf.d2);
             const float P2 = lam2mu * tp1 * d3v3;
             sxx += (P2 - mu2 * ts1 * sx + rxn) * dt;
             syy += (P2 - mu2 * ts1 * sy + ryn) * dt;
@@ -264,12 +307,12 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
             const float qyz = muyz * ts * dyVz_dzVy, qxz = muxz * ts * dxVz_dzVx, qxy = muxy * ts * dxVy_dyVx;
 #pragma unroll
             for (int m = 0; m < NM; ++m) {
-                r[9 + m] = a.c.c1[m] * r[9 + m] - a.c.c2[m] * qyz * dt;
-                r[12 + m] = a.c.c1[m] * r[12 + m] - a.c.c2[m] * qxz * dt;
-                r[15 + m] = a.c.c1[m] * r[15 + m] - a.c.c2[m] * qxy * dt;
-                ryzn += a.c.d1[m] * r[9 + m];
-                rxzn += a.c.d1[m] * r[12 + m];
-                rxyn += a.c.d1[m] * r[15 + m];
+                r[9 + m] = cf.c1[m] * r[9 + m] - cf.c2[m] * qyz * dt;
+                r[12 + m] = cf.c1[m] * r[12 + m] - cf.c2[m] * qxz * dt;
+                r[15 + m] = cf.c1[m] * r[15 + m] - cf.c2[m] * qxy * dt;
+                ryzn += cf.d1[m] * r[9 + m];
+                rxzn += cf.d1[m] * r[12 + m];
+                rxyn += cf.d1[m] * r[15 + m];
             }
             syz += (muyz * ts1 * dyVz_dzVy + ryzn) * dt;
             sxz += (muxz * ts1 * dxVz_dzVx + rxzn) * dt;
@@ -295,19 +338,22 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
         if (bad) break;
         if (tid == 0) {
             fence_proxy_async();
-            if (k + 2 <= kz1 - 1) issueRS(k + 2);
-            if (k + 3 <= kz1) issueM(k + 3);
-            if (k + 4 <= kz1 + 1) issueV(k + 4);
+            if (nRS <= kz1 - 1) issueRS();
+            if (nM <= kz1) issueM();
+            if (nV <= kz1 + 1) issueV();
         }
+        cRS.advance();
+        sM0 = sM1;
+        cM1.advance();
+        for (int q = 0; q < 4; ++q) sV[q] = sV[q + 1];
+        cV2.advance();
     }
-    if (bad) {
-        if (tid == 0) {
-            atomicExch(ta.err, 1);
-            // drain this block's copies still in flight (bounded)
-            for (int s = 0; s < 2; ++s) if (fills[s]) mbar_wait(&sm.barRS[s], (fills[s] - 1) & 1);
-            for (int s = 0; s < 3; ++s) if (fills[2 + s]) mbar_wait(&sm.barM[s], (fills[2 + s] - 1) & 1);
-            for (int s = 0; s < 6; ++s) if (fills[5 + s]) mbar_wait(&sm.barV[s], (fills[5 + s] - 1) & 1);
-        }
+    if (bad && tid == 0) {
+        atomicExch(ta.err, 1);
+        // drain this block's copies still in flight (bounded)
+        lRS.drain(sm.barRS, 2);
+        lM.drain(sm.barM, 3);
+        lV.drain(sm.barV, 6);
     }
 }
 
@@ -317,22 +363,22 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constan
 //   rho ring: 3 planes (k, k+1, k+2 in flight)
 //   V ring:   4 planes (k, k+1 .. k+3 in flight)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__ TArgs ta) {
+__device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
     extern __shared__ __align__(128) unsigned char smraw[];
     VelSmem& sm = *reinterpret_cast<VelSmem*>(smraw);
     int& bad = sm.bad;
     const ZArgs& a = ta.z;
+    const Coef cf = a.c;
     const Geo& g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int xt = a.x0 + blockIdx.x * 32, yt = a.y0 + blockIdx.y * TTY;
+    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TTY;
     const int ix = xt + tx, jy = yt + ty;
     const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
-    const int kz0 = blockIdx.z * a.kchunk;
+    const int kz0 = bz * a.kchunk;
     const int kz1 = min(kz0 + a.kchunk, a.kz_end);
     if (kz0 >= kz1) return;
 
     constexpr uint32_t BSH = 4 * (TTY + 4) * 6 * 40, BRHO = 4 * (TTY + 1) * 36, BVC = 4 * TTY * 3 * 32;
-    int fills[15];  // S 0-7, rho 8-10, V 11-14
     if (tid == 0) {
         for (int s = 0; s < 8; ++s) mbar_init(&sm.barS[s], 1);
         for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
@@ -340,7 +386,6 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__
         fence_barrier_init();
         bad = 0;
     }
-    for (int s = 0; s < 15; ++s) fills[s] = 0;
     const int gx = xt + g.hx, gy = yt + HYT;
     if (tid == 0) {
         bool ok = true;
@@ -351,57 +396,77 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__
     }
     __syncthreads();
     if (bad) return;
-    auto issueS = [&](int p) {
-        int s = pmod(p - (kz0 - 2), 8);
+
+    int nS = kz0 - 2, nM = kz0, nV = kz0;
+    RingPos<8> pS{0, 0u};
+    RingPos<3> pM{0, 0u};
+    RingPos<4> pV{0, 0u};
+    FillLog lS, lM, lV;
+    auto issueS = [&]() {
+        const int s = pS.slot;
         mbar_expect_tx(&sm.barS[s], BSH);
-        tma_load_4d(&sm.S[s], &ta.tmSh, &sm.barS[s], gx - 4, 0, gy - 2, p + HZT);
-        ++fills[s];
+        tma_load_4d(&sm.S[s], &ta.tmSh, &sm.barS[s], gx - 4, 0, gy - 2, nS + HZT);
+        lS.note(s, pS.par);
+        pS.advance();
+        ++nS;
     };
-    auto issueM = [&](int p) {
-        int s = pmod(p - kz0, 3);
+    auto issueM = [&]() {
+        const int s = pM.slot;
         mbar_expect_tx(&sm.barM[s], BRHO);
-        tma_load_4d(&sm.M[s], &ta.tmRho, &sm.barM[s], gx, 0, gy, p + HZT);
-        ++fills[8 + s];
+        tma_load_4d(&sm.M[s], &ta.tmRho, &sm.barM[s], gx, 0, gy, nM + HZT);
+        lM.note(s, pM.par);
+        pM.advance();
+        ++nM;
     };
-    auto issueV = [&](int p) {
-        int s = pmod(p - kz0, 4);
+    auto issueV = [&]() {
+        const int s = pV.slot;
         mbar_expect_tx(&sm.barV[s], BVC);
-        tma_load_4d(&sm.V[s], &ta.tmVc, &sm.barV[s], gx, 0, gy, p + HZT);
-        ++fills[11 + s];
+        tma_load_4d(&sm.V[s], &ta.tmVc, &sm.barV[s], gx, 0, gy, nV + HZT);
+        lV.note(s, pV.par);
+        pV.advance();
+        ++nV;
     };
     if (tid == 0) {
-        for (int p = kz0 - 2; p <= min(kz0 + 5, kz1 + 1); ++p) issueS(p);
-        for (int p = kz0; p <= min(kz0 + 2, kz1); ++p) issueM(p);
-        for (int p = kz0; p <= min(kz0 + 3, kz1 - 1); ++p) issueV(p);
+        while (nS <= min(kz0 + 5, kz1 + 1)) issueS();
+        while (nM <= min(kz0 + 2, kz1)) issueM();
+        while (nV <= min(kz0 + 3, kz1 - 1)) issueV();
     }
-    auto parity = [&](int p, int p0, int n) { return (uint32_t)(((p - p0) / n) & 1); };
 
     int4 band = make_int4(0, -1, 0, -1);
     if (act) band = a.band[(size_t)(jy - a.y0) * a.nxi + (ix - a.x0)];
-    const float dt = a.c.dt;
+    const float dt = cf.dt;
     const long long planeV = 3LL * g.pitch * g.nyp;
     const long long bV = (long long)goff(g, 3, 0, ix, jy, 0);
     float* __restrict__ Vg = a.V;
     const int P = g.pitch;
 
+    // consumer positions: S of plane k+2 (slots of k-2 .. k+1 ride along),
+    // rho of plane k+1 (slot of rho(k) rides along), V of plane k
+    RingPos<8> cS2{4, 0u};
+    RingPos<3> cM1{1, 0u};
+    RingPos<4> cV{0, 0u};
+    int sS[5] = {0, 1, 2, 3, 4}, sM0 = 0;
+    bool ok = mbar_wait(&sm.barM[0], 0u);
+    for (int q = 0; q < 4; ++q) ok &= mbar_wait(&sm.barS[q], 0u);
+
     for (int k = kz0; k < kz1; ++k) {
-        bool ok = true;
-        for (int d = -2; d <= 2; ++d) ok &= mbar_wait(&sm.barS[pmod(k + d - kz0 + 2, 8)], parity(k + d, kz0 - 2, 8));
-        ok &= mbar_wait(&sm.barM[pmod(k - kz0, 3)], parity(k, kz0, 3));
-        ok &= mbar_wait(&sm.barM[pmod(k + 1 - kz0, 3)], parity(k + 1, kz0, 3));
-        ok &= mbar_wait(&sm.barV[pmod(k - kz0, 4)], parity(k, kz0, 4));
+        ok &= mbar_wait(&sm.barS[cS2.slot], cS2.par);
+        ok &= mbar_wait(&sm.barM[cM1.slot], cM1.par);
+        ok &= mbar_wait(&sm.barV[cV.slot], cV.par);
         if (!ok) bad = 1;
+        sS[4] = cS2.slot;
+        const int sM1 = cM1.slot;
         if (act && ok) {
             const int kk = k + 1;
             const bool nb = in_band(kk, band);
-            const float e40x = nb ? a.c.e2x : a.c.e4x0, e41x = nb ? 0.f : a.c.e4x1;
-            const float e40y = nb ? a.c.e2y : a.c.e4y0, e41y = nb ? 0.f : a.c.e4y1;
-            const float e40z = nb ? a.c.e2z : a.c.e4z0, e41z = nb ? 0.f : a.c.e4z1;
+            const float e40x = nb ? cf.e2x : cf.e4x0, e41x = nb ? 0.f : cf.e4x1;
+            const float e40y = nb ? cf.e2y : cf.e4y0, e41y = nb ? 0.f : cf.e4y1;
+            const float e40z = nb ? cf.e2z : cf.e4z0, e41z = nb ? 0.f : cf.e4z1;
             const int lx = tx + 4, ly = ty + 2;
-            float (*Sk)[6][40] = sm.S[pmod(k - kz0 + 2, 8)].d;
+            float (*Sk)[6][40] = sm.S[sS[2]].d;
             // plane-k tile fields: 0 Sxx 1 Syy 2 Szz 3 Syz 4 Sxz 5 Sxy
             auto T = [&](int f, int dy, int dx) { return Sk[ly + dy][f][lx + dx]; };
-            auto zc = [&](int d, int f) { return sm.S[pmod(k + d - kz0 + 2, 8)].d[ly][f][lx]; };
+            auto zc = [&](int d, int f) { return sm.S[sS[d + 2]].d[ly][f][lx]; };
             const float d3Sx3 = (T(0, 0, 1) - T(0, 0, 0)) * e40x - (T(0, 0, 2) - T(0, 0, -1)) * e41x
                               + (T(5, 0, 0) - T(5, -1, 0)) * e40y - (T(5, 1, 0) - T(5, -2, 0)) * e41y
                               + (zc(0, 4) - zc(-1, 4)) * e40z - (zc(1, 4) - zc(-2, 4)) * e41z;
@@ -411,10 +476,10 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__
             const float d3Sz3 = (T(4, 0, 0) - T(4, 0, -1)) * e40x - (T(4, 0, 1) - T(4, 0, -2)) * e41x
                               + (T(3, 0, 0) - T(3, -1, 0)) * e40y - (T(3, 1, 0) - T(3, -2, 0)) * e41y
                               + (zc(1, 2) - zc(0, 2)) * e40z - (zc(2, 2) - zc(-1, 2)) * e41z;
-            float (*R0)[36] = sm.M[pmod(k - kz0, 3)].d;
-            float (*R1)[36] = sm.M[pmod(k + 1 - kz0, 3)].d;
+            float (*R0)[36] = sm.M[sM0].d;
+            float (*R1)[36] = sm.M[sM1].d;
             const float r0 = R0[ty][tx];
-            float (*Vk)[3][32] = sm.V[pmod(k - kz0, 4)].d;
+            float (*Vk)[3][32] = sm.V[cV.slot].d;
             float vx = Vk[ty][0][tx] + 2.f / (r0 + R0[ty][tx + 1]) * d3Sx3 * dt;
             float vy = Vk[ty][1][tx] + 2.f / (r0 + R0[ty + 1][tx]) * d3Sy3 * dt;
             float vz = Vk[ty][2][tx] + 2.f / (r0 + R1[ty][tx]) * d3Sz3 * dt;
@@ -433,19 +498,62 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__
         if (bad) break;
         if (tid == 0) {
             fence_proxy_async();
-            if (k + 6 <= kz1 + 1) issueS(k + 6);
-            if (k + 3 <= kz1) issueM(k + 3);
-            if (k + 4 <= kz1 - 1) issueV(k + 4);
+            if (nS <= kz1 + 1) issueS();
+            if (nM <= kz1) issueM();
+            if (nV <= kz1 - 1) issueV();
         }
+        for (int q = 0; q < 4; ++q) sS[q] = sS[q + 1];
+        cS2.advance();
+        sM0 = sM1;
+        cM1.advance();
+        cV.advance();
     }
-    if (bad) {
-        if (tid == 0) {
-            atomicExch(ta.err, 1);
-            for (int s = 0; s < 8; ++s) if (fills[s]) mbar_wait(&sm.barS[s], (fills[s] - 1) & 1);
-            for (int s = 0; s < 3; ++s) if (fills[8 + s]) mbar_wait(&sm.barM[s], (fills[8 + s] - 1) & 1);
-            for (int s = 0; s < 4; ++s) if (fills[11 + s]) mbar_wait(&sm.barV[s], (fills[11 + s] - 1) & 1);
-        }
+    if (bad && tid == 0) {
+        atomicExch(ta.err, 1);
+        lS.drain(sm.barS, 8);
+        lM.drain(sm.barM, 3);
+        lV.drain(sm.barV, 4);
     }
+}
+
+template <class RT>
+__global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constant__ TArgs ta) {
+    stress_tma_tile<RT>(ta, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+__global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__ TArgs ta) {
+    vel_tma_tile(ta, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Batched launches: block b works on tile (e.y, e.z, e.w) of simulation e.x,
+// with e = blocks[b]; every simulation's tensor maps live in `all` (global
+// memory, 128-byte aligned).
+// The tables were written by host copies, so the issuing thread makes the
+// tensor maps visible to the TMA unit with a system-scope tensormap-proxy
+// acquire fence before the first copy.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap* m) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)m) : "memory");
+}
+__device__ __forceinline__ void tmaps_acquire(const TArgs& t) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        tmap_acquire(&t.tmV);
+        tmap_acquire(&t.tmS);
+        tmap_acquire(&t.tmM);
+        tmap_acquire(&t.tmR);
+        tmap_acquire(&t.tmSh);
+        tmap_acquire(&t.tmRho);
+        tmap_acquire(&t.tmVc);
+    }
+}
+template <class RT>
+__global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
+    const int4 e = blocks[blockIdx.x];
+    tmaps_acquire(all[e.x]);
+    stress_tma_tile<RT>(all[e.x], e.y, e.z, e.w);
+}
+__global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
+    const int4 e = blocks[blockIdx.x];
+    tmaps_acquire(all[e.x]);
+    vel_tma_tile(all[e.x], e.y, e.z, e.w);
 }
 
 }  // namespace swpc

@@ -21,12 +21,16 @@ struct Plan {
     long long nV, nS, nM, nR, nade, npml, bytes;
     PmlBox box[5];
     int nbox;
+    int pml_blocks;
 };
 
 struct Sim {
     swpc_dims dims;
     Plan p;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // PML shell kernels, joined back into `stream` every phase
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
+    bool concurrent = true;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_steps = 8;
     long long launches = 0, launches_per_graph = 0;
@@ -42,7 +46,7 @@ struct Sim {
     int* d_kob = nullptr;
     int* d_err = nullptr;   // set by a kernel whose bounded wait ran out
     Coef coef{};
-    int kchunk = 1, pml_blocks = 1;
+    int kchunk = 1, kchunk_auto = 1;
     int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
     size_t smem_stress = 0, smem_vel = 0;

@@ -67,6 +67,7 @@ static int plan(const swpc_dims* d, Plan& p) {
     // PML shell boxes
     p.nbox = 0;
     p.nade = 0;
+    p.pml_blocks = 0;
     long long first = 0;
     if (p.pml) {
         const int na = d->na, nx = d->nx, ny = d->ny, nz = d->nz;
@@ -79,6 +80,12 @@ static int plan(const swpc_dims* d, Plan& p) {
             B.pitch = (int)rup(B.nx, 32);
             B.off = p.nade;
             B.first = first;
+            B.tiles_x = (B.nx + 31) / 32;
+            B.tiles_y = (B.ny + TBY - 1) / TBY;
+            B.zc = std::min(B.nz, 32);
+            B.nzc = (B.nz + B.zc - 1) / B.zc;
+            B.first_block = p.pml_blocks;
+            p.pml_blocks += B.tiles_x * B.tiles_y * B.nzc;
             p.nade += 9LL * B.pitch * B.ny * B.nz;
             first += (long long)B.nx * B.ny * B.nz;
         }
@@ -143,23 +150,26 @@ int Sim::launch_step(bool timed) {
     const dim3 grd((p.nxi + TBX - 1) / TBX, (p.nyi + TBY - 1) / TBY, (p.nzi + kchunk - 1) / kchunk);
     // timed: an event pair on the launching stream around each kernel, read
     // back later by drain_events() so the launches are not serialised
-    cudaEvent_t e_a = nullptr;
-    auto ev0 = [&](int c) {
-        (void)c;
-        if (timed) { e_a = get_event(); cudaEventRecord(e_a, stream); }
+    cudaEvent_t e_a[6] = {};
+    auto ev0 = [&](int c, cudaStream_t st) {
+        if (timed) { e_a[c] = get_event(); cudaEventRecord(e_a[c], st); }
     };
-    auto ev1 = [&](int c) {
+    auto ev1 = [&](int c, cudaStream_t st) {
         if (timed) {
             cudaEvent_t e_b = get_event();
-            cudaEventRecord(e_b, stream);
-            pending.push_back({c, e_a, e_b});
+            cudaEventRecord(e_b, st);
+            pending.push_back({c, e_a[c], e_b});
         }
     };
+    // the PML shell kernels run beside the interior kernels on a second
+    // stream (two branches of the captured graph); they touch disjoint points
+    const bool two = p.pml && concurrent;
+    cudaStream_t sp = two ? stream2 : stream;
     if (vmax_args.ntdec_r > 0) { k_vmax<<<64, 256, 0, stream>>>(vmax_args); ++launches; }
     if (tap_args.n > 0) {
-        ev0(4);
+        ev0(4, stream);
         k_taps<<<(tap_args.n + 127) / 128, 128, 0, stream>>>(tap_args); ++launches;
-        ev1(4);
+        ev1(4, stream);
     }
     if (snap_args.kinds) {
         dim3 sg((snap_args.nxs + 127) / 128, snap_args.nys);
@@ -170,7 +180,17 @@ int Sim::launch_step(bool timed) {
     targs.z = z;
     const dim3 tblk(32, TTY);
     const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + TTY - 1) / TTY, (p.nzi + kchunk - 1) / kchunk);
-    ev0(0);
+    if (two) {
+        cudaEventRecord(ev_fork, stream);
+        cudaStreamWaitEvent(stream2, ev_fork, 0);
+    }
+    if (p.pml) {
+        ev0(2, sp);
+        k_stress_pml<<<(unsigned)((p.npml + 255) / 256), 256, 0, sp>>>(pml_args); ++launches;
+        ev1(2, sp);
+        if (two) cudaEventRecord(ev_join, stream2);
+    }
+    ev0(0, stream);
     if (variant == 0) {
         if (p.rbytes == 4) k_stress_tma<float><<<tgrd, tblk, smem_stress, stream>>>(targs);
         else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half><<<tgrd, tblk, smem_stress, stream>>>(targs);
@@ -181,27 +201,29 @@ int Sim::launch_step(bool timed) {
         else k_stress_interior<__nv_bfloat16><<<grd, blk, 0, stream>>>(z);
     }
     ++launches;
-    ev1(0);
-    if (p.pml) {
-        ev0(2);
-        k_stress_pml<<<pml_blocks, 256, 0, stream>>>(pml_args); ++launches;
-        ev1(2);
-    }
+    ev1(0, stream);
+    if (two) cudaStreamWaitEvent(stream, ev_join, 0);
     if (src_args.n > 0 && !bf_mode) {
-        ev0(5);
+        ev0(5, stream);
         k_stressglut<<<(src_args.n + 127) / 128, 128, 0, stream>>>(src_args); ++launches;
-        ev1(5);
+        ev1(5, stream);
     }
-    ev0(1);
+    if (two) {
+        cudaEventRecord(ev_fork2, stream);
+        cudaStreamWaitEvent(stream2, ev_fork2, 0);
+    }
+    if (p.pml) {
+        ev0(3, sp);
+        k_vel_pml<<<(unsigned)((p.npml + 255) / 256), 256, 0, sp>>>(pml_args); ++launches;
+        ev1(3, sp);
+        if (two) cudaEventRecord(ev_join2, stream2);
+    }
+    ev0(1, stream);
     if (variant == 0) k_vel_tma<<<tgrd, tblk, smem_vel, stream>>>(targs);
     else k_vel_interior<<<grd, blk, 0, stream>>>(z);
     ++launches;
-    ev1(1);
-    if (p.pml) {
-        ev0(3);
-        k_vel_pml<<<pml_blocks, 256, 0, stream>>>(pml_args); ++launches;
-        ev1(3);
-    }
+    ev1(1, stream);
+    if (two) cudaStreamWaitEvent(stream, ev_join2, 0);
     if (src_args.n > 0 && bf_mode) {
         k_bodyforce<<<(src_args.n + 127) / 128, 128, 0, stream>>>(src_args); ++launches;
     }
@@ -279,6 +301,10 @@ static EncodeTiledFn encode_fn() {
 // 4-D map (x, field, y, z) over a row-interleaved group
 static int make_map(CUtensorMap* m, void* base, CUtensorMapDataType dt, int es, long long nx, int nf, long long ny,
                     long long nz, int bx, int bf, int by) {
+    // L2 fetch granularity: each box row is one 128-byte line (FP32) or half
+    // of one (16-bit); promoting to 256 bytes would double the DRAM reads of
+    // rows whose neighbour tile is not read at the same time
+    const CUtensorMapL2promotion promo = bx * es >= 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B : CU_TENSOR_MAP_L2_PROMOTION_NONE;
     EncodeTiledFn fn = encode_fn();
     if (!fn) return set_err(SWPC_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     cuuint64_t dims[4] = {(cuuint64_t)nx, (cuuint64_t)nf, (cuuint64_t)ny, (cuuint64_t)nz};
@@ -286,7 +312,7 @@ static int make_map(CUtensorMap* m, void* base, CUtensorMapDataType dt, int es, 
     cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)bf, (cuuint32_t)by, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = fn(m, dt, 4, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    promo, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_err(SWPC_E_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
     return 0;
 }
@@ -313,6 +339,13 @@ int Sim::build_tensor_maps() {
     CK(cudaFuncSetAttribute(k_stress_tma<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sizeof(StressSmem<__nv_bfloat16>)));
     CK(cudaFuncSetAttribute(k_vel_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(VelSmem)));
+    CK(cudaFuncSetAttribute(k_stress_tma_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sizeof(StressSmem<float>)));
+    CK(cudaFuncSetAttribute(k_stress_tma_batch<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sizeof(StressSmem<__half>)));
+    CK(cudaFuncSetAttribute(k_stress_tma_batch<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sizeof(StressSmem<__nv_bfloat16>)));
+    CK(cudaFuncSetAttribute(k_vel_tma_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(VelSmem)));
     return 0;
 }
 
@@ -583,6 +616,46 @@ extern "C" int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out
     return 0;
 }
 
+int swpc_gpu_get_dims(swpc_sim* sim, swpc_dims* out) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out) return set_err(SWPC_E_ARG, "null argument");
+    *out = s->dims;
+    return 0;
+}
+
+int swpc_gpu_reset(swpc_sim* sim) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemsetAsync(s->V, 0, s->p.nV * 4, s->stream));
+    CK(cudaMemsetAsync(s->S, 0, s->p.nS * 4, s->stream));
+    CK(cudaMemsetAsync(s->R, 0, s->p.nR * s->p.rbytes, s->stream));
+    if (s->adeV) CK(cudaMemsetAsync(s->adeV, 0, s->p.nade * 4, s->stream));
+    if (s->adeS) CK(cudaMemsetAsync(s->adeS, 0, s->p.nade * 4, s->stream));
+    const TapArgs& t = s->tap_args;
+    if (t.n > 0) {
+        const size_t w3 = (size_t)t.ntw * 3 * t.n * 4, w6 = (size_t)t.ntw * 6 * t.n * 4;
+        if (t.wav_v) CK(cudaMemsetAsync(t.wav_v, 0, w3, s->stream));
+        if (t.wav_u) CK(cudaMemsetAsync(t.wav_u, 0, w3, s->stream));
+        if (t.wav_s) CK(cudaMemsetAsync(t.wav_s, 0, w6, s->stream));
+        if (t.wav_e) CK(cudaMemsetAsync(t.wav_e, 0, w6, s->stream));
+        if (t.acc) CK(cudaMemsetAsync(t.acc, 0, (size_t)9 * t.n * 8, s->stream));
+    }
+    const SnapArgs& a = s->snap_args;
+    if (a.kinds) {
+        const size_t fr = (size_t)a.maxframes * 3 * a.nxs * a.nys * 4;
+        if (a.xy_v) CK(cudaMemsetAsync(a.xy_v, 0, fr, s->stream));
+        if (a.xy_u) CK(cudaMemsetAsync(a.xy_u, 0, fr, s->stream));
+        if (a.uacc) CK(cudaMemsetAsync(a.uacc, 0, (size_t)3 * a.nxs * a.nys * 8, s->stream));
+    }
+    if (s->vmax_args.rep) CK(cudaMemsetAsync(s->vmax_args.rep, 0, (size_t)s->vmax_args.nrep * 12, s->stream));
+    CK(cudaMemsetAsync(s->d_err, 0, 4, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    s->it_done = 0;
+    s->diverged = false;
+    return 0;
+}
+
 int swpc_gpu_profile(swpc_sim* sim, int enable) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s) return set_err(SWPC_E_ARG, "null simulation");
@@ -616,6 +689,8 @@ Sim::~Sim() {
     for (void* q : allocs) cudaFree(q);
     for (auto& q : pending) { ev_pool.push_back(q.a); ev_pool.push_back(q.b); }
     for (auto& e : ev_pool) if (e) cudaEventDestroy(e);
+    if (stream2) { cudaStreamSynchronize(stream2); cudaStreamDestroy(stream2); }
+    for (cudaEvent_t e : {ev_fork, ev_join, ev_fork2, ev_join2}) if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -633,6 +708,11 @@ int Sim::dalloc(void** ptr, size_t bytes) {
 
 int Sim::allocate() {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_fork2, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_join2, cudaEventDisableTiming));
     int rc;
     if ((rc = dalloc((void**)&V, p.nV * 4))) return rc;
     if ((rc = dalloc((void**)&S, p.nS * 4))) return rc;
@@ -653,11 +733,17 @@ int Sim::allocate() {
     long long want = 8LL * nsm;
     int nchunk = (int)std::max(1LL, std::min((long long)(p.nzi / 8), (want + cols - 1) / cols));
     kchunk = (p.nzi + nchunk - 1) / nchunk;
-    pml_blocks = (int)std::min<long long>((p.npml + 255) / 256, 64LL * nsm);
-    if (pml_blocks < 1) pml_blocks = 1;
+    kchunk_auto = kchunk;
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
     variant = dims.reserved[0] == 1 ? 1 : 0;
+    // PML shell beside the interior: pays off only when the interior launch
+    // cannot fill the GPU by itself (measured: 128x128x64 0.134 vs 0.16 ms per
+    // step; 1024x1024x512 27.9 serial vs 28.3 ms concurrent)
+    {
+        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + TTY - 1) / TTY) * ((p.nzi + kchunk - 1) / kchunk);
+        concurrent = dims.reserved[1] == 2 || (dims.reserved[1] == 0 && tiles < 4LL * nsm);
+    }
     if ((rc = build_tensor_maps())) return rc;
     return 0;
 }
@@ -776,6 +862,7 @@ int Sim::set_sources(int n, const int* ijk, const double* mo, const double* mij,
     a.n = n; a.stf = stftype;
     a.tbeg = (float)dims.tbeg; a.dt = (float)dims.dt;
     a.dt_dxyz = (float)(dims.dt / (dims.dx * dims.dy * dims.dz));
+    a.bf = bf ? 1 : 0;
     bf_mode = bf;
     if (n == 0) return 0;
     std::vector<int> q(3 * (size_t)n);
@@ -866,3 +953,231 @@ int Sim::set_snapshot(int kinds, int k0, int idec, int jdec, int ntdec_s) {
     if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Batched form: many independent simulations advanced by one fused launch per
+// phase of the time step (stress interior + PML shell, sources, velocity
+// interior + PML shell, taps), captured as a CUDA graph.  Every launch walks a
+// block table that spans all members, so small grids that would leave most of
+// the GPU idle alone fill it together.
+// ---------------------------------------------------------------------------
+struct Batch {
+    std::vector<Sim*> sims;
+    cudaStream_t stream = nullptr, stream2 = nullptr;
+    cudaEvent_t ev[4] = {};
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 8;
+    int rbytes = 4, store = 0;
+    std::vector<void*> allocs;
+    TArgs* d_targs = nullptr;
+    PArgs* d_pargs = nullptr;
+    SrcArgs* d_src = nullptr;
+    TapArgs* d_tap = nullptr;
+    SnapArgs* d_snap = nullptr;
+    VmaxArgs* d_vmax = nullptr;
+    int** d_its = nullptr;
+    int4* d_tblocks = nullptr;
+    int2* d_pblocks = nullptr;
+    int n_tblocks = 0, n_pblocks = 0, max_nst = 0, max_src = 0, max_nxs = 0, max_nys = 0;
+    bool any_vmax = false, any_snap = false, any_bf = false, any_mt = false;
+    size_t smem_stress = 0, smem_vel = 0;
+    long long launches = 0, launches_per_graph = 0;
+    ~Batch() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* q : allocs) cudaFree(q);
+        for (auto e : ev) if (e) cudaEventDestroy(e);
+        if (stream2) cudaStreamDestroy(stream2);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    template <class T>
+    int upload(T** dst, const std::vector<T>& v) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(16, v.size() * sizeof(T)));
+        if (e != cudaSuccess) return set_err(SWPC_E_NOMEM, std::string("batch table: ") + cudaGetErrorString(e));
+        allocs.push_back(q);
+        if (!v.empty()) CK(cudaMemcpy(q, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        *dst = (T*)q;
+        return 0;
+    }
+    int launch_step() {
+        const int n = (int)sims.size();
+        if (any_vmax) { k_vmax_batch<<<dim3(64, n), 256, 0, stream>>>(d_vmax); ++launches; }
+        if (max_nst) { k_taps_batch<<<dim3((max_nst + 127) / 128, n), 128, 0, stream>>>(d_tap); ++launches; }
+        if (any_snap) { k_snap_xy_batch<<<dim3((max_nxs + 127) / 128, max_nys, n), 128, 0, stream>>>(d_snap); ++launches; }
+        const dim3 tblk(32, TTY);
+        if (n_pblocks) {
+            cudaEventRecord(ev[0], stream);
+            cudaStreamWaitEvent(stream2, ev[0], 0);
+            k_stress_pml_batch<<<n_pblocks, 256, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
+            cudaEventRecord(ev[1], stream2);
+        }
+        if (rbytes == 4) k_stress_tma_batch<float><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+        else if (store == SWPC_STORE_FP16) k_stress_tma_batch<__half><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+        else k_stress_tma_batch<__nv_bfloat16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+        ++launches;
+        if (n_pblocks) cudaStreamWaitEvent(stream, ev[1], 0);
+        if (any_mt) { k_stressglut_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
+        if (n_pblocks) {
+            cudaEventRecord(ev[2], stream);
+            cudaStreamWaitEvent(stream2, ev[2], 0);
+            k_vel_pml_batch<<<n_pblocks, 256, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
+            cudaEventRecord(ev[3], stream2);
+        }
+        k_vel_tma_batch<<<n_tblocks, tblk, smem_vel, stream>>>(d_targs, d_tblocks); ++launches;
+        if (n_pblocks) cudaStreamWaitEvent(stream, ev[3], 0);
+        if (any_bf) { k_bodyforce_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
+        k_advance_batch<<<(n + 127) / 128, 128, 0, stream>>>(d_its, n); ++launches;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+        return 0;
+    }
+};
+
+extern "C" {
+
+int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || kchunk < 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_zchunk");
+    if (kchunk == 0) kchunk = s->kchunk_auto;
+    s->kchunk = std::max(1, std::min(kchunk, s->p.nzi));
+    if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+    return 0;
+}
+
+int swpc_gpu_get_zchunk(swpc_sim* sim) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    return s ? s->kchunk : set_err(SWPC_E_ARG, "null simulation");
+}
+
+int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
+    if (!sims || n <= 0 || !out) return set_err(SWPC_E_ARG, "bad arguments to swpc_batch_create");
+    *out = nullptr;
+    Batch* b = new Batch();
+    auto fail = [&](int rc) { delete b; return rc; };
+    for (int q = 0; q < n; ++q) {
+        Sim* s = reinterpret_cast<Sim*>(sims[q]);
+        if (!s || !s->medium_ready) return fail(set_err(SWPC_E_STATE, "every member must have its medium uploaded"));
+        if (s->variant != 0) return fail(set_err(SWPC_E_ARG, "batched members must use the TMA interior kernels"));
+        if (q && s->dims.store != b->store) return fail(set_err(SWPC_E_ARG, "batched members must share one storage precision"));
+        for (int r = 0; r < q; ++r)
+            if (b->sims[r] == s) return fail(set_err(SWPC_E_ARG, "a simulation appears twice in the batch"));
+        b->store = s->dims.store;
+        b->rbytes = s->p.rbytes;
+        b->sims.push_back(s);
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(set_err(SWPC_E_CUDA, "stream creation failed"));
+    for (auto& e : b->ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(set_err(SWPC_E_CUDA, "event creation failed"));
+    std::vector<TArgs> ta(n);
+    std::vector<PArgs> pa(n);
+    std::vector<SrcArgs> sa(n);
+    std::vector<TapArgs> tp(n);
+    std::vector<SnapArgs> sn(n);
+    std::vector<VmaxArgs> vm(n);
+    std::vector<int*> its(n);
+    std::vector<int4> tb;
+    std::vector<int2> pb;
+    for (int q = 0; q < n; ++q) {
+        Sim* s = b->sims[q];
+        CK(cudaStreamSynchronize(s->stream));
+        ZArgs z;
+        s->fill_zargs(z);
+        ta[q] = s->targs;
+        ta[q].z = z;
+        pa[q] = s->pml_args;
+        if (!s->p.pml) pa[q].npts = 0;
+        sa[q] = s->src_args;
+        tp[q] = s->tap_args;
+        sn[q] = s->snap_args;
+        vm[q] = s->vmax_args;
+        its[q] = s->d_it;
+        const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + TTY - 1) / TTY, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
+        for (int bz = 0; bz < gz; ++bz)
+            for (int by = 0; by < gy; ++by)
+                for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
+        if (s->p.pml)
+            for (long long bk = 0; bk < (s->p.npml + 255) / 256; ++bk) pb.push_back(make_int2(q, (int)bk));
+        b->max_nst = std::max(b->max_nst, s->tap_args.n);
+        b->max_src = std::max(b->max_src, s->src_args.n);
+        if (s->src_args.n > 0) { if (s->bf_mode) b->any_bf = true; else b->any_mt = true; }
+        if (s->vmax_args.ntdec_r > 0) b->any_vmax = true;
+        if (s->snap_args.kinds) {
+            b->any_snap = true;
+            b->max_nxs = std::max(b->max_nxs, s->snap_args.nxs);
+            b->max_nys = std::max(b->max_nys, s->snap_args.nys);
+        }
+    }
+    int rc;
+    if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_pargs, pa)) || (rc = b->upload(&b->d_src, sa)) ||
+        (rc = b->upload(&b->d_tap, tp)) || (rc = b->upload(&b->d_snap, sn)) || (rc = b->upload(&b->d_vmax, vm)) ||
+        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_pblocks, pb)))
+        return fail(rc);
+    if (((uintptr_t)b->d_targs & 127) != 0) return fail(set_err(SWPC_E_CUDA, "tensor-map table is not 128-byte aligned"));
+    b->n_tblocks = (int)tb.size();
+    b->n_pblocks = (int)pb.size();
+    b->smem_stress = b->sims[0]->smem_stress;
+    b->smem_vel = b->sims[0]->smem_vel;
+    *out = reinterpret_cast<swpc_batch*>(b);
+    return 0;
+}
+
+int swpc_batch_run(swpc_batch* batch, int nsteps) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    if (!b || nsteps < 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_batch_run");
+    // every member continues from its own next step; the members' own
+    // streams are drained first so their state is current
+    for (Sim* s : b->sims) {
+        if (s->diverged) return set_err(SWPC_E_DIVERGED, "a batch member has diverged");
+        CK(cudaStreamSynchronize(s->stream));
+        k_set_it<<<1, 1, 0, b->stream>>>(s->d_it, s->it_done + 1);
+        ++b->launches;
+    }
+    int n = nsteps, rc = 0;
+    if (n >= b->graph_steps && !b->graph) {
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        long long l0 = b->launches;
+        for (int q = 0; q < b->graph_steps && rc == 0; ++q) rc = b->launch_step();
+        cudaGraph_t gr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &gr);
+        if (rc) return rc;
+        if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+        b->launches_per_graph = b->launches - l0;
+        b->launches = l0;
+    }
+    while (b->graph && n >= b->graph_steps) {
+        CK(cudaGraphLaunch(b->graph, b->stream));
+        b->launches += b->launches_per_graph;
+        n -= b->graph_steps;
+    }
+    for (int q = 0; q < n && rc == 0; ++q) rc = b->launch_step();
+    for (Sim* s : b->sims) s->it_done += nsteps;
+    return rc;
+}
+
+int swpc_batch_sync(swpc_batch* batch) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    if (!b) return set_err(SWPC_E_ARG, "null batch");
+    CK(cudaStreamSynchronize(b->stream));
+    for (Sim* s : b->sims) {
+        int rc = s->check_divergence();
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+void* swpc_batch_stream(swpc_batch* batch) { return batch ? (void*)reinterpret_cast<Batch*>(batch)->stream : nullptr; }
+
+long long swpc_batch_launch_count(swpc_batch* batch) { return batch ? reinterpret_cast<Batch*>(batch)->launches : -1; }
+
+int swpc_batch_destroy(swpc_batch* batch) {
+    delete reinterpret_cast<Batch*>(batch);
+    return 0;
+}
+
+}  // extern "C"

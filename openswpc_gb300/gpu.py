@@ -47,8 +47,22 @@ EXPORTS = [
     "swpc_gpu_fetch_field", "swpc_gpu_profile", "swpc_gpu_profile_read", "swpc_gpu_stream",
     "swpc_gpu_launch_count", "swpc_gpu_destroy", "swpc_gpu_last_error", "swpc_host_prepare",
     "swpc_host_write_sac", "swpc_host_nt", "swpc_host_medium",
-    "swpc_host_check", "swpc_gpu_fetch_field_static",
+    "swpc_host_check", "swpc_gpu_fetch_field_static", "swpc_gpu_reset", "swpc_gpu_get_dims", "swpc_gpu_set_zchunk",
+    "swpc_gpu_get_zchunk", "swpc_batch_create", "swpc_batch_run", "swpc_batch_sync", "swpc_batch_stream",
+    "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes",
+    "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
+    "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
+    "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
 ]
+
+
+class ServeConfig(ctypes.Structure):
+    """swpc_serve_config of include/swpc_gpu.h."""
+    _fields_ = [("hbm_budget", ctypes.c_double), ("max_active", ctypes.c_int), ("quantum", ctypes.c_int),
+                ("prep_threads", ctypes.c_int), ("write_sac", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+REQ_QUEUED, REQ_LOADING, REQ_WAITING, REQ_RUNNING, REQ_DONE = range(5)
 
 
 def lib(build=True):
@@ -92,6 +106,35 @@ def lib(build=True):
     L.swpc_host_nt.argtypes = [vp]
     L.swpc_host_check.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
     L.swpc_host_medium.argtypes = [i, i, i, i, d, d, d] + [fp] * 5 + [ip] * 6 + [dp]
+    L.swpc_gpu_reset.argtypes = [vp]
+    L.swpc_gpu_get_dims.argtypes = [vp, ctypes.POINTER(Dims)]
+    L.swpc_gpu_set_zchunk.argtypes = [vp, i]
+    L.swpc_gpu_get_zchunk.argtypes = [vp]
+    L.swpc_batch_create.argtypes = [ctypes.c_void_p, i, ctypes.POINTER(vp)]
+    L.swpc_batch_run.argtypes = [vp, i]
+    L.swpc_batch_sync.argtypes = [vp]
+    L.swpc_batch_stream.argtypes = [vp]
+    L.swpc_batch_stream.restype = vp
+    L.swpc_batch_launch_count.argtypes = [vp]
+    L.swpc_batch_launch_count.restype = ctypes.c_longlong
+    L.swpc_batch_destroy.argtypes = [vp]
+    L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
+    L.swpc_host_request_bytes.argtypes = [vp]
+    L.swpc_host_request_bytes.restype = ctypes.c_longlong
+    L.swpc_host_request_dims.argtypes = [vp, ctypes.POINTER(Dims)]
+    L.swpc_host_materialize.argtypes = [vp, ctypes.POINTER(vp)]
+    L.swpc_host_request_free.argtypes = [vp]
+    L.swpc_serve_create.argtypes = [ctypes.POINTER(ServeConfig), ctypes.POINTER(vp)]
+    L.swpc_serve_submit.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]
+    L.swpc_serve_state.argtypes = [vp, ctypes.c_longlong]
+    L.swpc_serve_wait.argtypes = [vp, ctypes.c_longlong, d]
+    L.swpc_serve_result.argtypes = [vp, ctypes.c_longlong, i, fp, ctypes.c_size_t, ip, ip]
+    L.swpc_serve_error.argtypes = [vp, ctypes.c_longlong, ctypes.c_char_p, ctypes.c_size_t]
+    L.swpc_serve_times.argtypes = [vp, ctypes.c_longlong, dp]
+    L.swpc_serve_release.argtypes = [vp, ctypes.c_longlong]
+    L.swpc_serve_drain.argtypes = [vp]
+    L.swpc_serve_stats.argtypes = [vp, dp]
+    L.swpc_serve_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -113,9 +156,11 @@ def _ptr(a):
 
 
 def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xbeg=0.0, ybeg=0.0, zbeg=0.0,
-              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0):
+              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0, concurrent=None):
     """swpc_dims for swpc_gpu_create.  variant 0 selects the TMA-fed interior
-    kernels, 1 the shared-memory sweep without TMA (kept for comparison)."""
+    kernels, 1 the shared-memory sweep without TMA (kept for comparison);
+    concurrent runs the PML shell kernels beside the interior kernels on a
+    second stream (True/False; None lets the library choose by grid size)."""
     d = Dims()
     d.nx, d.ny, d.nz, d.nt, d.na, d.nm = nx, ny, nz, nt, na, 3
     d.abc_type = 0 if abc == "pml" else 1
@@ -124,6 +169,7 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     d.xbeg, d.ybeg, d.zbeg, d.tbeg = xbeg, ybeg, zbeg, tbeg
     d.fcut, d.M0, d.UC, d.ntdec_r = fcut, M0, UC, ntdec_r
     d.reserved[0] = int(variant)
+    d.reserved[1] = 0 if concurrent is None else (2 if concurrent else 1)
     return d
 
 
@@ -163,6 +209,8 @@ class Simulation:
         self._h = ctypes.c_void_p()
         if handle is not None:
             self._h = handle
+            dims = Dims()
+            _ck(lib().swpc_gpu_get_dims(self._h, ctypes.byref(dims)))
         else:
             _ck(lib().swpc_gpu_create(ctypes.byref(dims), ctypes.byref(self._h)))
         self.dims = dims
@@ -270,12 +318,173 @@ class Simulation:
     def nt(self):
         return int(lib().swpc_host_nt(self._h))
 
+    def reset(self):
+        _ck(lib().swpc_gpu_reset(self._h))
+
+    def set_zchunk(self, kchunk):
+        _ck(lib().swpc_gpu_set_zchunk(self._h, int(kchunk)))
+
+    def zchunk(self):
+        return int(lib().swpc_gpu_get_zchunk(self._h))
+
     def write_sac(self, odir=None):
         _ck(lib().swpc_host_write_sac(self._h, os.fsencode(odir) if odir else None))
 
     def close(self):
         if self._h:
             lib().swpc_gpu_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several simulations advanced together by fused launches
+    (swpc_batch_*).  The members stay owned by the caller."""
+
+    def __init__(self, sims):
+        self.sims = list(sims)
+        arr = (ctypes.c_void_p * len(self.sims))(*[s.handle.value for s in self.sims])
+        self._h = ctypes.c_void_p()
+        _ck(lib().swpc_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(self.sims), ctypes.byref(self._h)))
+
+    def run(self, nsteps):
+        _ck(lib().swpc_batch_run(self._h, int(nsteps)))
+
+    def sync(self):
+        _ck(lib().swpc_batch_sync(self._h))
+
+    def stream(self):
+        return lib().swpc_batch_stream(self._h)
+
+    def launch_count(self):
+        return int(lib().swpc_batch_launch_count(self._h))
+
+    def close(self):
+        if self._h:
+            lib().swpc_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Request:
+    """Host half of the set-up of one input.inf (swpc_host_load): medium,
+    sources and stations in host memory, no device touched."""
+
+    def __init__(self, inf_path):
+        self._h = ctypes.c_void_p()
+        _ck(lib().swpc_host_load(os.fsencode(os.path.abspath(inf_path)), ctypes.byref(self._h)))
+
+    @property
+    def device_bytes(self):
+        n = lib().swpc_host_request_bytes(self._h)
+        if n < 0:
+            raise SwpcError(int(n), last_error())
+        return int(n)
+
+    @property
+    def dims(self):
+        d = Dims()
+        _ck(lib().swpc_host_request_dims(self._h, ctypes.byref(d)))
+        return d
+
+    def materialize(self):
+        """Create the simulation on the current device and upload it."""
+        h = ctypes.c_void_p()
+        _ck(lib().swpc_host_materialize(self._h, ctypes.byref(h)))
+        return Simulation(handle=h)
+
+    def close(self):
+        if self._h:
+            lib().swpc_host_request_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop with continuous batching (swpc_serve_*): submit input.inf
+    paths at any time; admitted requests share fused launches on the GPU."""
+
+    def __init__(self, hbm_budget=0.0, max_active=0, quantum=0, prep_threads=0, write_sac=False):
+        cfg = ServeConfig(hbm_budget=float(hbm_budget), max_active=int(max_active), quantum=int(quantum),
+                          prep_threads=int(prep_threads), write_sac=int(bool(write_sac)))
+        self._h = ctypes.c_void_p()
+        _ck(lib().swpc_serve_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+
+    def submit(self, inf_path):
+        rid = ctypes.c_longlong()
+        _ck(lib().swpc_serve_submit(self._h, os.fsencode(os.path.abspath(inf_path)), ctypes.byref(rid)))
+        return int(rid.value)
+
+    def state(self, rid):
+        return int(lib().swpc_serve_state(self._h, rid))
+
+    def wait(self, rid, timeout=-1.0):
+        st = int(lib().swpc_serve_wait(self._h, rid, float(timeout)))
+        if st < 0:
+            raise SwpcError(st, self.error(rid))
+        return st
+
+    def error(self, rid):
+        buf = ctypes.create_string_buffer(2048)
+        lib().swpc_serve_error(self._h, rid, buf, 2048)
+        return buf.value.decode(errors="replace")
+
+    def result(self, rid, kind=SWPC_WAV_V):
+        nst, ntw = ctypes.c_int(), ctypes.c_int()
+        _ck(lib().swpc_serve_result(self._h, rid, int(kind), None, 0, ctypes.byref(nst), ctypes.byref(ntw)))
+        nc = 3 if kind in (SWPC_WAV_V, SWPC_WAV_U) else 6
+        out = np.zeros((nst.value, nc, ntw.value), np.float32)
+        _ck(lib().swpc_serve_result(self._h, rid, int(kind), out.ctypes.data, out.size, None, None))
+        return out
+
+    def times(self, rid):
+        t = np.zeros(4)
+        _ck(lib().swpc_serve_times(self._h, rid, t.ctypes.data))
+        return dict(submitted=t[0], admitted=t[1], started=t[2], finished=t[3])
+
+    def release(self, rid):
+        _ck(lib().swpc_serve_release(self._h, rid))
+
+    def drain(self):
+        _ck(lib().swpc_serve_drain(self._h))
+
+    def stats(self):
+        st = np.zeros(10)
+        _ck(lib().swpc_serve_stats(self._h, st.ctypes.data))
+        keys = ("done", "failed", "running", "waiting", "queued", "bytes_granted", "peak_bytes", "quanta",
+                "rebuilds", "updates")
+        return dict(zip(keys, st.tolist()))
+
+    def close(self):
+        if self._h:
+            lib().swpc_serve_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __enter__(self):

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def header_functions():
     src = open(os.path.join(ROOT, "include", "swpc_gpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(swpc_(?:gpu|host)_\w+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(swpc_(?:gpu|host|batch|serve)_\w+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_symbol():
@@ -48,6 +48,21 @@ def test_host_setup_matches_oracle(tmp_path):
     assert src == [tuple(r) for r in o.sources()[0]]
     sta = [tuple(int(v) for v in s.split(",")) for s in h["sta"].split(";")]
     assert sta == [tuple(r) for r in o.stations()]
+
+
+def test_two_phase_load_needs_no_gpu(tmp_path):
+    """swpc_host_load runs the whole host set-up without a device and knows
+    the device bytes the simulation will take before it is created."""
+    inf = configs.write_plain_small(str(tmp_path), nt=50)
+    r = gpu.Request(inf)
+    d = r.dims
+    h = gpu.host_check(inf)
+    assert (d.nx, d.ny, d.nz, d.nt, d.na) == (h["nx"], h["ny"], h["nz"], h["nt"], h["na"])
+    assert abs(d.M0 - h["M0"]) <= 1e-9 * h["M0"]
+    assert r.device_bytes == gpu.required_bytes(d)
+    r.close()
+    with pytest.raises(gpu.SwpcError):
+        gpu.Request(os.path.join(str(tmp_path), "missing.inf"))
 
 
 def test_host_medium_matches_oracle(tmp_path):
