@@ -466,14 +466,152 @@ def run_batch(args):
     return 0
 
 
+def serve_inputs(n, seed, nt, root, tail=0.1):
+    """Requests of the serving workload: the batched generator, with a
+    fraction `tail` of the requests replaced by 512 x 512 x 256 grids."""
+    from openswpc_gb300 import configs
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice(np.arange(96, 257, 32), size=(n, 3))
+    big = rng.random(n) < tail
+    sizes[big] = (512, 512, 256)
+    infs = []
+    for q, (nx, ny, nz) in enumerate(sizes):
+        d = os.path.join(root, "r%04d" % q)
+        infs.append(configs.write_layered(d, int(nx), int(ny), int(nz), seed + q, nt=nt, n_station=8))
+    return infs, sizes
+
+
+def run_serve(args):
+    """Serving form: Poisson arrivals at each rate of --rates submitted to the
+    continuous-batching server (swpc_serve_*), latency = completion minus
+    arrival; then the same requests one after another on the plain path
+    (host set-up + run + trace read-back each), which also gives every
+    request's result alone for the misfit check."""
+    from openswpc_gb300 import gpu
+    gpu.lib()
+    rates = [float(r) for r in args.rates.split(",")]
+    out = {"metric": "served solves/s and latency", "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    with tempfile.TemporaryDirectory() as root:
+        infs, sizes = serve_inputs(args.requests, 20261203, args.nt, root)
+        pts = [int(np.prod(s)) for s in sizes]
+        # sequential plain path: each request alone, end to end
+        alone = []
+        t0 = time.perf_counter()
+        for f in infs:
+            s = gpu.Simulation.from_inf(f)
+            s.run(1, args.nt)
+            s.sync()
+            alone.append(s.waveforms())
+            s.close()
+        t_seq = time.perf_counter() - t0
+        per_rate = []
+        worst = 0.0
+        for lam in rates:
+            rng = np.random.default_rng(int(lam * 1000) + 7)
+            gaps = rng.exponential(1.0 / lam, size=len(infs))
+            with gpu.Server(hbm_budget=args.budget_gb * 1e9, quantum=args.quantum, prep_threads=8) as srv:
+                ids = []
+                tstart = time.perf_counter()
+                tnext = tstart
+                for f, g in zip(infs, gaps):
+                    tnext += g
+                    dly = tnext - time.perf_counter()
+                    if dly > 0:
+                        time.sleep(dly)
+                    ids.append(srv.submit(f))
+                for rid in ids:
+                    srv.wait(rid)
+                t_all = time.perf_counter() - tstart
+                lat = []
+                for rid, w in zip(ids, alone):
+                    t = srv.times(rid)
+                    lat.append(t["finished"] - t["submitted"])
+                    got = srv.result(rid)
+                    den = float(np.linalg.norm(w))
+                    worst = max(worst, float(np.linalg.norm(got - w)) / den if den > 0 else 0.0)
+                    srv.release(rid)
+                st = srv.stats()
+            lat = np.array(lat)
+            per_rate.append({"rate_per_s": lam, "solves_per_s": len(ids) / t_all, "wall_s": t_all,
+                             "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
+                             "p99_s": float(np.percentile(lat, 99)), "peak_device_gb": st["peak_bytes"] / 1e9,
+                             "quanta": int(st["quanta"]), "batch_rebuilds": int(st["rebuilds"]),
+                             "grid_pt_updates_per_s": st["updates"] / t_all})
+    best = max(per_rate, key=lambda r: r["solves_per_s"])
+    out.update({"value": best["solves_per_s"], "rates": per_rate,
+                "sequential_solves_per_s": len(infs) / t_seq, "sequential_wall_s": t_seq,
+                "speedup_vs_sequential": best["solves_per_s"] / (len(infs) / t_seq),
+                "misfit_vs_alone_max": worst,
+                "config": {"workload": "serving: Poisson arrivals, %d requests per rate, axes in {96..256} with 10%% "
+                                       "512x512x256, nt=%d" % (len(infs), args.nt),
+                           "hbm_budget_gb": args.budget_gb, "quantum_steps": args.quantum,
+                           "points_total": int(sum(pts)),
+                           "timing": "wall clock from first arrival to last completion, host set-up included"}})
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_precision(args):
+    """Precision form: the large workload's medium generator and source at
+    512 x 512 x 256 (dx = 0.5 km), run with FP32, FP16 and BF16 storage of
+    the memory variables for --nt steps; reports updates/s (CUDA events over
+    the whole run), the byte model per step and the receiver misfit of each
+    16-bit form against the FP32 path."""
+    from openswpc_gb300 import gpu
+    import torch
+    gpu.lib()
+    w = WORKLOADS["mid"]
+    seed = 20261203
+    med = make_medium(w, seed)
+    med["src"], med["mij"], med["sta"] = source_and_stations(w, med, seed)
+    n_int, n_pml = counts(w)
+    npt = w["nx"] * w["ny"] * w["nz"]
+    res = {}
+    for store in ("fp32", "fp16", "bf16"):
+        sim = build_sim(w, med, args.nt, store=store)
+        st = torch.cuda.ExternalStream(sim.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sim.run(1, args.nt)
+        e1.record(st)
+        e1.synchronize()
+        sim.sync()
+        ms = e0.elapsed_time(e1) / args.nt
+        wav = sim.waveforms()
+        sim.close()
+        b_int, b_pml, _ = byte_model(store)
+        res[store] = {"ms_per_step": ms, "updates_per_s": npt / (ms / 1e3),
+                      "bytes_per_step": b_int * n_int + b_pml * n_pml, "wav": wav}
+    ref = res["fp32"]["wav"]
+    den = float(np.linalg.norm(ref))
+    forms = {}
+    for store, r in res.items():
+        forms[store] = {k: v for k, v in r.items() if k != "wav"}
+        forms[store]["misfit_vs_fp32"] = float(np.linalg.norm(r["wav"] - ref)) / den if den > 0 else None
+        forms[store]["speedup_vs_fp32"] = res["fp32"]["ms_per_step"] / r["ms_per_step"]
+    out = {"metric": "grid-pt updates/s by storage precision", "value": forms["fp16"]["updates_per_s"],
+           "unit": "pt/s", "n_gpus": 1, "steps": args.nt, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "forms": forms,
+           "config": {"workload": "precision form 512x512x256, large-workload medium and source, nt=%d" % args.nt,
+                      "timing": "CUDA events over the whole run from it=1 (graph replay)"}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + ["batch"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS) + ["batch", "serve", "precision"])
     ap.add_argument("--nsim", type=int, default=64, help="members of the batched workload")
+    ap.add_argument("--rates", default="2,10,50", help="serving: Poisson arrival rates [1/s]")
+    ap.add_argument("--requests", type=int, default=48, help="serving: requests per rate")
+    ap.add_argument("--nt", type=int, default=300, help="serving / precision: time steps per simulation")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
+    ap.add_argument("--quantum", type=int, default=50, help="serving: steps between scheduling points")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])
@@ -485,6 +623,10 @@ def main():
         args.warmup = 3
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
+    if args.workload == "precision":
+        return run_precision(args)
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)

@@ -785,11 +785,21 @@ int Sim::upload_medium(const float* rho, const float* lam, const float* mu, cons
     coef.e4y0 = (float)(18.0 / 16.0 / dy); coef.e4y1 = (float)(2.0 / 48.0 / dy);
     coef.e4z0 = (float)(18.0 / 16.0 / dz); coef.e4z1 = (float)(2.0 / 48.0 / dz);
     coef.e2x = (float)(1.0 / dx); coef.e2y = (float)(1.0 / dy); coef.e2z = (float)(1.0 / dz);
+    // FP16 storage of the memory variables keeps them scaled by a power of two
+    // rscale, folded into c2 (R is built from c2 terms) and d1 (R enters the
+    // stress through d1); both products stay exact in FP32, so only where the
+    // 16-bit rounding happens changes.  The stress next to a unit source
+    // reaches about 1/(dx dy dz) and R about 0.05 of that, so
+    // rscale = 4096 dx dy dz puts the largest R near 200 (overflow at 65504)
+    // and keeps R down to ~1e-6 of its peak in the normal FP16 range.
+    double rscale = 1.0;
+    if (dims.store == SWPC_STORE_FP16)
+        rscale = std::ldexp(1.0, std::max(0, std::min(20, (int)std::lround(std::log2(4096.0 * dx * dy * dz)))));
     double d2 = 0;
     for (int m = 0; m < NM; ++m) {
         coef.c1[m] = (float)((2 * ts[m] - dt) / (2 * ts[m] + dt));
-        coef.c2[m] = (float)(2.0 / (2 * ts[m] + dt) / NM);
-        coef.d1[m] = (float)(2 * ts[m] / (2 * ts[m] - dt));
+        coef.c2[m] = (float)(2.0 / (2 * ts[m] + dt) / NM * rscale);
+        coef.d1[m] = (float)(2 * ts[m] / (2 * ts[m] - dt) / rscale);
         d2 += dt / (2 * ts[m] - dt);
     }
     coef.d2 = (float)(d2 / NM);
