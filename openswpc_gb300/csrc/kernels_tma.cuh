@@ -448,6 +448,15 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
     int sS[5] = {0, 1, 2, 3, 4}, sM0 = 0;
     bool ok = mbar_wait(&sm.barM[0], 0u);
     for (int q = 0; q < 4; ++q) ok &= mbar_wait(&sm.barS[q], 0u);
+    const int lx = tx + 4, ly = ty + 2;
+    // z stencil columns rolled in registers: Sxz and Syz of planes k-2..k+1,
+    // Szz of planes k-1..k+2 (slots 0..3 hold planes kz0-2..kz0+1)
+    float cxz[4], cyz[4], czz[4];
+    for (int q = 0; q < 4; ++q) {
+        cxz[q] = sm.S[q].d[ly][4][lx];
+        cyz[q] = sm.S[q].d[ly][3][lx];
+    }
+    for (int q = 0; q < 3; ++q) czz[q] = sm.S[q + 1].d[ly][2][lx];
 
     for (int k = kz0; k < kz1; ++k) {
         ok &= mbar_wait(&sm.barS[cS2.slot], cS2.par);
@@ -456,33 +465,34 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
         if (!ok) bad = 1;
         sS[4] = cS2.slot;
         const int sM1 = cM1.slot;
+        czz[3] = sm.S[sS[4]].d[ly][2][lx];
         if (act && ok) {
             const int kk = k + 1;
             const bool nb = in_band(kk, band);
             const float e40x = nb ? cf.e2x : cf.e4x0, e41x = nb ? 0.f : cf.e4x1;
             const float e40y = nb ? cf.e2y : cf.e4y0, e41y = nb ? 0.f : cf.e4y1;
             const float e40z = nb ? cf.e2z : cf.e4z0, e41z = nb ? 0.f : cf.e4z1;
-            const int lx = tx + 4, ly = ty + 2;
             float (*Sk)[6][40] = sm.S[sS[2]].d;
             // plane-k tile fields: 0 Sxx 1 Syy 2 Szz 3 Syz 4 Sxz 5 Sxy
             auto T = [&](int f, int dy, int dx) { return Sk[ly + dy][f][lx + dx]; };
-            auto zc = [&](int d, int f) { return sm.S[sS[d + 2]].d[ly][f][lx]; };
             const float d3Sx3 = (T(0, 0, 1) - T(0, 0, 0)) * e40x - (T(0, 0, 2) - T(0, 0, -1)) * e41x
                               + (T(5, 0, 0) - T(5, -1, 0)) * e40y - (T(5, 1, 0) - T(5, -2, 0)) * e41y
-                              + (zc(0, 4) - zc(-1, 4)) * e40z - (zc(1, 4) - zc(-2, 4)) * e41z;
+                              + (cxz[2] - cxz[1]) * e40z - (cxz[3] - cxz[0]) * e41z;
             const float d3Sy3 = (T(5, 0, 0) - T(5, 0, -1)) * e40x - (T(5, 0, 1) - T(5, 0, -2)) * e41x
                               + (T(1, 1, 0) - T(1, 0, 0)) * e40y - (T(1, 2, 0) - T(1, -1, 0)) * e41y
-                              + (zc(0, 3) - zc(-1, 3)) * e40z - (zc(1, 3) - zc(-2, 3)) * e41z;
+                              + (cyz[2] - cyz[1]) * e40z - (cyz[3] - cyz[0]) * e41z;
             const float d3Sz3 = (T(4, 0, 0) - T(4, 0, -1)) * e40x - (T(4, 0, 1) - T(4, 0, -2)) * e41x
                               + (T(3, 0, 0) - T(3, -1, 0)) * e40y - (T(3, 1, 0) - T(3, -2, 0)) * e41y
-                              + (zc(1, 2) - zc(0, 2)) * e40z - (zc(2, 2) - zc(-1, 2)) * e41z;
+                              + (czz[2] - czz[1]) * e40z - (czz[3] - czz[0]) * e41z;
             float (*R0)[36] = sm.M[sM0].d;
             float (*R1)[36] = sm.M[sM1].d;
             const float r0 = R0[ty][tx];
             float (*Vk)[3][32] = sm.V[cV.slot].d;
-            float vx = Vk[ty][0][tx] + 2.f / (r0 + R0[ty][tx + 1]) * d3Sx3 * dt;
-            float vy = Vk[ty][1][tx] + 2.f / (r0 + R0[ty + 1][tx]) * d3Sy3 * dt;
-            float vz = Vk[ty][2][tx] + 2.f / (r0 + R1[ty][tx]) * d3Sz3 * dt;
+            // 2/(rho_a + rho_b) as 2 * (correctly rounded reciprocal): the
+            // same value as the IEEE quotient, since doubling is exact
+            float vx = Vk[ty][0][tx] + 2.f * __frcp_rn(r0 + R0[ty][tx + 1]) * d3Sx3 * dt;
+            float vy = Vk[ty][1][tx] + 2.f * __frcp_rn(r0 + R0[ty + 1][tx]) * d3Sy3 * dt;
+            float vz = Vk[ty][2][tx] + 2.f * __frcp_rn(r0 + R1[ty][tx]) * d3Sz3 * dt;
             if (a.cer) {  // Cerjan sponge epilogue (m_absorb_c.f90:170-198)
                 const float gxc = a.cer[a.cer_off[0] + ix], gxb = a.cer[a.cer_off[1] + ix];
                 const float gyc = a.cer[a.cer_off[2] + jy], gyb = a.cer[a.cer_off[3] + jy];
@@ -503,6 +513,14 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
             if (nV <= kz1 - 1) issueV();
         }
         for (int q = 0; q < 4; ++q) sS[q] = sS[q + 1];
+        for (int q = 0; q < 3; ++q) {
+            cxz[q] = cxz[q + 1];
+            cyz[q] = cyz[q + 1];
+            czz[q] = czz[q + 1];
+        }
+        // plane k+2 (now at sS[3]) supplies the new Sxz, Syz column entries
+        cxz[3] = sm.S[sS[3]].d[ly][4][lx];
+        cyz[3] = sm.S[sS[3]].d[ly][3][lx];
         cS2.advance();
         sM0 = sM1;
         cM1.advance();

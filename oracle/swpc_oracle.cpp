@@ -11,8 +11,9 @@
 // example/example.out).  This restatement is therefore checked by its own
 // known-answer tests (operator exactness, coefficient closed forms, source
 // time function integrals, reciprocity, analytic far field, cross-precision
-// agreement) in tests/test_oracle_*.py -- parity against the reference's own
-// binary is UNPINNED.
+// agreement) in tests/test_oracle.py, and held to its own committed traces
+// (tests/golden/, regenerated by tests/golden/make_golden.py) -- parity
+// against the reference's own binary is UNPINNED.
 //
 // Three precision modes mirror the reference's build variants:
 //   mode 0  fp32   MP = SP = float            (reference rebuilt with MP = SP)

@@ -4,6 +4,8 @@ reference, MP = SP) on identical inputs.
 Tolerance: relative L2 misfit <= 1e-5 of receiver waveforms (the stated
 bar), and of the full wavefields after a few steps.  The GPU evaluates the
 same formulas in FP32 with fused multiply-adds; the oracle does not fuse."""
+import os
+
 import numpy as np
 import pytest
 
@@ -64,3 +66,22 @@ def test_step_by_step_equals_graph_replay(small_inf):
     for name in ("Vx", "Szz", "Sxy"):
         assert np.array_equal(a.field(name), b.field(name))
     a.close(); b.close()
+
+
+@pytest.mark.gpu
+def test_drop_in_path_matches_golden_traces(tmp_path):
+    """input.inf -> host set-up (swpc_host_prepare) -> GPU -> receiver traces,
+    against the committed oracle traces: relative L2 <= 1e-5 against the
+    fp32 build, and the error against the fp64 build is stated."""
+    from tests.golden import make_golden
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "plain_small_nt200.npz"))
+    inf = make_golden.write_inputs(str(tmp_path))
+    s = gpu.Simulation.from_inf(inf)
+    s.run(1, int(g["nt"]))
+    s.sync()
+    w = s.waveforms()
+    s.close()
+    m32, m64 = misfit(w, g["fp32"]), misfit(w, g["fp64"])
+    print("drop-in path: misfit vs fp32 oracle %.3e, vs fp64 oracle %.3e" % (m32, m64))
+    assert m32 <= 1e-5
+    assert m64 <= 1e-5

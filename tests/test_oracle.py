@@ -114,3 +114,20 @@ def test_p_wave_arrival_time(tmp_path):
     tpk = t[np.argmax(np.abs(vx))]
     # peak of a Kupper pulse of rise time 1 s radiated at t = 0.5 s (its centre)
     assert abs(tpk - (8.0 / 6.0 + 0.5)) < 0.25, tpk
+
+
+def test_oracle_reproduces_golden_traces(tmp_path):
+    """The oracle is pinned to its committed golden traces
+    (tests/golden/make_golden.py): any change of its arithmetic shows here."""
+    from tests.golden import make_golden
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "plain_small_nt200.npz"))
+    inf = make_golden.write_inputs(str(tmp_path))
+    o = pyoracle.Oracle(inf, "fp32")
+    assert np.array_equal(o.stations(), g["stations"])
+    o.run(int(g["nt"]))
+    w = o.waveforms()
+    assert np.abs(g["fp32"]).max() > 0
+    assert misfit(w, g["fp32"]) < 1e-6
+    # the three builds agree to the expected orders
+    assert misfit(g["fp32"], g["fp64"]) < 1e-5
+    assert misfit(g["mixed"], g["fp64"]) < 1e-6
