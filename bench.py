@@ -320,7 +320,7 @@ def run_gpu(args, w):
     achieved = kern[top]["GBps"]
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
+    if os.path.exists(tp) and args.store == "fp32" and w is WORKLOADS["large"]:
         try:
             with open(tp) as f:
                 traffic = json.load(f).get(top + "_bytes_per_launch")

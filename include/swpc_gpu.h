@@ -163,6 +163,14 @@ long long swpc_gpu_launch_count(swpc_sim* sim);
 
 int swpc_gpu_destroy(swpc_sim* sim);
 
+/* Self-test of the bounded device waits used by the TMA kernels: launches
+ * one block that waits on a barrier nothing completes.  Returns
+ * SWPC_E_TIMEOUT when the wait gave up and reported, as designed (0 would
+ * mean the barrier completed, which cannot happen); *seconds receives how
+ * long the wait took.  The device stays usable afterwards.  No counterpart
+ * in the reference. */
+int swpc_gpu_selftest_wait(double* seconds);
+
 /* The dims the simulation was created with. */
 int swpc_gpu_get_dims(swpc_sim* sim, swpc_dims* out);
 
@@ -247,6 +255,14 @@ int swpc_host_medium(int nx, int ny, int nz, int na, double fq_min, double fq_ma
  * odir/wav/<title>.3d.<station>.<cmp>.sac (m_wav.f90:782-792). */
 int swpc_host_write_sac(swpc_sim* sim, const char* odir);
 
+/* Write the xy-section snapshots as the reference's native .snp files
+ * odir/<title>.3d.xy.v.snp and .xy.u.snp: header version 6
+ * (m_snap.f90:846-892), the rho/lam/mu planes at k0_xy and the topography
+ * (newfile_xy, m_snap.f90:413-473), then one (nxs, nys) plane per component
+ * per frame (wbuf_xy_v / wbuf_xy_u, m_snap.f90:1587-1653, 1963-2025).
+ * Does nothing when the input asked for no xy snapshot. */
+int swpc_host_write_snp(swpc_sim* sim, const char* odir);
+
 /* ------------------------------------------------------------------------
  * Serving form: a request loop with continuous batching.  No counterpart in
  * the reference (one simulation per mpiexec).  Requests are input.inf paths;
@@ -279,9 +295,9 @@ int swpc_serve_state(swpc_server* srv, long long id);
 /* Block until the request is done or failed, or timeout_s passes (< 0: no
  * limit); returns its state. */
 int swpc_serve_wait(swpc_server* srv, long long id, double timeout_s);
-/* Receiver traces of a finished request, laid out as swpc_gpu_fetch_waveforms
- * lays them out ((nst, ncmp, ntw)); with buf null only *nst and *ntw are set.
- * n_floats is the room in buf. */
+/* Receiver traces of a finished request in the layout of
+ * swpc_gpu_fetch_waveforms (Fortran order (ntw, ncmp, nst)); with buf null
+ * only *nst and *ntw are set.  n_floats is the room in buf. */
 int swpc_serve_result(swpc_server* srv, long long id, int kind, float* buf, size_t n_floats, int* nst, int* ntw);
 /* Error message of a failed request; returns its length. */
 int swpc_serve_error(swpc_server* srv, long long id, char* buf, size_t n);

@@ -18,7 +18,7 @@ DRIVER = os.path.join(BUILD, "swpc_3d_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off"]
 
 CU_SOURCES = ["swpc_gpu.cu"]
 CXX_SOURCES = ["host.cpp", "serve.cpp"]

@@ -230,6 +230,11 @@ struct Meta {  // what the SAC writer needs after set-up
     double m6[6] = {0, 0, 0, 0, 0, 0}, f3[3] = {0, 0, 0};
     long long exedate = 0;
     int ntw = 0, flags = 0;
+    // xy-section snapshot files (m_snap.f90:413-473, 846-892): section size,
+    // the medium planes rho, lam, mu at k0_xy and the topography depth
+    int snp_kinds = 0, nxs = 0, nys = 0;
+    std::vector<float> snp_med;  // (nxs, nys, 3) Fortran order
+    double bd0 = 0;
 };
 std::mutex g_meta_mu;
 std::map<swpc_sim*, Meta> g_meta;
@@ -731,6 +736,23 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     P.kinds = (p.xy_v ? SWPC_SNAP_XY_V : 0) | (p.xy_u ? SWPC_SNAP_XY_U : 0);
     P.k0 = std::max(1, std::min(p.nz, x2i(p.z0_xy, p.zbeg, p.dz)));
     P.idec = p.idec; P.jdec = p.jdec; P.ntdec_s = p.ntdec_s;
+    if (P.kinds) {  // snap__setup / newfile_xy (m_snap.f90:131-133, 436-458)
+        const int idec = std::max(1, p.idec), jdec = std::max(1, p.jdec);
+        meta.snp_kinds = P.kinds;
+        meta.nxs = (p.nx + idec / 2) / idec;
+        meta.nys = (p.ny + jdec / 2) / jdec;
+        meta.bd0 = bd0;
+        meta.snp_med.assign((size_t)meta.nxs * meta.nys * 3, 0.f);
+        const size_t pl = (size_t)meta.nxs * meta.nys;
+        for (int j = 1; j <= meta.nys; ++j)
+            for (int i = 1; i <= meta.nxs; ++i) {
+                const int ii = i * idec - idec / 2, jj = j * jdec - jdec / 2;
+                const size_t q = (size_t)(j - 1) * meta.nxs + (i - 1), c = G.idx(P.k0, ii, jj);
+                meta.snp_med[q] = P.rho[c];
+                meta.snp_med[pl + q] = P.lam[c];
+                meta.snp_med[2 * pl + q] = P.mu[c];
+            }
+    }
     P.meta = std::move(meta);
     return 0;
 }
@@ -861,6 +883,71 @@ int swpc_host_nt(swpc_sim* sim) {
     std::lock_guard<std::mutex> lk(g_meta_mu);
     auto it = g_meta.find(sim);
     return it == g_meta.end() ? 0 : it->second.p.nt;
+}
+
+int swpc_host_write_snp(swpc_sim* sim, const char* odir) {
+    Meta m;
+    {
+        std::lock_guard<std::mutex> lk(g_meta_mu);
+        auto it = g_meta.find(sim);
+        if (it == g_meta.end()) return swpc::set_err(SWPC_E_STATE, "simulation was not prepared by swpc_host_prepare");
+        m = it->second;
+    }
+    if (!m.snp_kinds) return 0;
+    try {
+        const Params& p = m.p;
+        std::string dir = (odir && *odir) ? std::string(odir) : p.odir;
+        mkdirs(dir);
+        int nxs = 0, nys = 0, nframes = 0;
+        int rc = swpc_gpu_query(sim, nullptr, nullptr, &nxs, &nys, &nframes);
+        if (rc) return rc;
+        if (nxs != m.nxs || nys != m.nys) return swpc::set_err(SWPC_E_STATE, "snapshot geometry differs from the set-up");
+        const int idec = std::max(1, p.idec), jdec = std::max(1, p.jdec);
+        // coordinates in single precision as i2x/j2y compute them (m_fdtool.f90:639-680)
+        const float xb = (float)p.xbeg, yb = (float)p.ybeg, dxf = (float)p.dx, dyf = (float)p.dy;
+        auto i2x = [](int i, float b, float d) { const float t = ((float)i - 0.5f) * d; return b + t; };
+        const float xs1 = i2x(idec - idec / 2, xb, dxf), xs2 = i2x(2 * idec - idec / 2, xb, dxf);
+        const float ys1 = i2x(jdec - jdec / 2, yb, dyf), ys2 = i2x(2 * jdec - jdec / 2, yb, dyf);
+        const size_t pl = (size_t)nxs * nys;
+        std::vector<float> frame(pl * 3);
+        for (int kind : {SWPC_SNAP_XY_V, SWPC_SNAP_XY_U}) {
+            if (!(m.snp_kinds & kind)) continue;
+            const bool v = kind == SWPC_SNAP_XY_V;
+            const std::string fn = dir + "/" + p.title + ".3d.xy." + (v ? "v" : "u") + ".snp";
+            std::ofstream f(fn, std::ios::binary | std::ios::trunc);
+            if (!f) throw std::runtime_error("cannot write " + fn);
+            auto wi = [&](int32_t x) { f.write((const char*)&x, 4); };
+            auto wf = [&](float x) { f.write((const char*)&x, 4); };
+            auto ws = [&](const std::string& t, size_t n) {
+                std::string u = t.substr(0, n);
+                u.resize(n, ' ');
+                f.write(u.data(), (std::streamsize)n);
+            };
+            // write_snp_header (m_snap.f90:846-892), header version 6
+            ws("STREAMIO", 8); ws("SWPC_3D ", 8); wi(6); ws(p.title, 80); wi((int32_t)m.exedate);
+            ws("xy", 2); ws(v ? "v3" : "u3", 2); wi(nxs); wi(nys);
+            wf(xs1); wf(ys1); wf(xs2 - xs1); wf(ys2 - ys1);
+            wf((float)p.dt * (float)p.ntdec_s);
+            wi(p.na / idec); wi(p.na / jdec);
+            wi(6); wi(3);  // nmed, nsnp of the xy section (m_snap.f90:200-205)
+            wf((float)p.clon); wf((float)p.clat); wf((float)p.phi);
+            wf(1.f); wf(1.f); wf(1.f);
+            // medium planes rho, lam, mu at k0_xy, then the topography (newfile_xy)
+            f.write((const char*)m.snp_med.data(), (std::streamsize)(m.snp_med.size() * 4));
+            const float topo = -(float)m.bd0 * 1000.f;
+            std::vector<float> tp(pl, topo);
+            f.write((const char*)tp.data(), (std::streamsize)(pl * 4));
+            // one (nxs, nys) plane per component per frame (wbuf_xy_v / wbuf_xy_u)
+            for (int q = 0; q < nframes; ++q) {
+                if ((rc = swpc_gpu_fetch_snapshot(sim, kind, q, frame.data()))) return rc;
+                f.write((const char*)frame.data(), (std::streamsize)(frame.size() * 4));
+            }
+            if (!f) throw std::runtime_error("short write to " + fn);
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
 }
 
 int swpc_host_write_sac(swpc_sim* sim, const char* odir) {

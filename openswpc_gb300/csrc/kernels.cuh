@@ -451,10 +451,10 @@ __device__ __forceinline__ PmlPt pml_point(const PArgs& a, long long p) {
     return r;
 }
 
-// PML stress update (m_absorb_p.f90:429-531) at shell point p.
-__device__ __forceinline__ void stress_pml_pt(const PArgs& a, const long long p) {
-    if (p >= a.npts) return;
-    const PmlPt c = pml_point(a, p);
+// PML stress update (m_absorb_p.f90:429-531) at shell point c.  Every load
+// is issued before any arithmetic or store, so a thread has all of its ~40
+// independent loads in flight at once (the kernel is bound by load latency).
+__device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
     const float eps = 1.1920928955078125e-07f;
@@ -466,65 +466,71 @@ __device__ __forceinline__ void stress_pml_pt(const PArgs& a, const long long p)
     const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
     const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
     const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
-    const float* __restrict__ V = a.V;
-    const float* __restrict__ M = a.M;
-    float* __restrict__ S = a.S;
+    const float* __restrict__ V = a.V + oV;
+    const float* __restrict__ M = a.M + oM;
+    float* __restrict__ S = a.S + oS;
+    float* __restrict__ A = a.adeV + oA;
+    const int AP = B.pitch;
+    // loads
     const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
     const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
-    const int AP = B.pitch;
-    {
-        const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
-        const float vx = V[oV], vy = V[oV + P], vz = V[oV + 2 * P];
-        // normal part (m_absorb_p.f90:453-474)
-        const float dxVx = (vx - V[oV - 1]) * a.r20x;
-        const float dyVy = (vy - V[oV + P - rowV]) * a.r20y;
-        const float dzVz = (vz - V[oV + 2 * P - planeV]) * a.r20z;
-        const float lamv = M[oM + P], muv = M[oM + 2 * P];
-        const float lam2mu = lamv + 2.f * muv;
-        const float lamR = lam2mu - 2.f * muv;
-        float* A = a.adeV + oA;
-        const float aVx = A[0], aVy = A[AP], aVz = A[2 * AP];
-        const float dxa = gxc.x * dxVx + gxc.y * aVx;
-        const float dya = gyc.x * dyVy + gyc.y * aVy;
-        const float dza = gzc.x * dzVz + gzc.y * aVz;
-        S[oS] += (lam2mu * dxa + lamR * (dya + dza)) * a.dt;
-        S[oS + P] += (lam2mu * dya + lamR * (dxa + dza)) * a.dt;
-        S[oS + 2 * P] += (lam2mu * dza + lamR * (dxa + dya)) * a.dt;
-        A[0] = gxc.z * aVx + gxc.w * dxVx * a.dt;
-        A[AP] = gyc.z * aVy + gyc.w * dyVy * a.dt;
-        A[2 * AP] = gzc.z * aVz + gzc.w * dzVz * a.dt;
-        // shear part (m_absorb_p.f90:477-518)
-        const float dxVy = (V[oV + P + 1] - vy) * a.r20x;
-        const float dxVz = (V[oV + 2 * P + 1] - vz) * a.r20x;
-        const float dyVx = (V[oV + rowV] - vx) * a.r20y;
-        const float dyVz = (V[oV + 2 * P + rowV] - vz) * a.r20y;
-        const float dzVx = (V[oV + planeV] - vx) * a.r20z;
-        const float dzVy = (V[oV + P + planeV] - vy) * a.r20z;
-        const float m000 = muv, m100 = M[oM + 2 * P + planeM], m010 = M[oM + 2 * P + 1], m110 = M[oM + 2 * P + planeM + 1];
-        const float m001 = M[oM + 2 * P + rowM], m011 = M[oM + 2 * P + rowM + 1], m101 = M[oM + 2 * P + planeM + rowM];
-        const float muxz = 4.f * m000 * m100 * m010 * m110 /
-                           (m000 * m100 * m010 + m000 * m100 * m110 + m000 * m010 * m110 + m100 * m010 * m110 + eps);
-        const float muxy = 4.f * m000 * m010 * m001 * m011 /
-                           (m000 * m010 * m001 + m000 * m010 * m011 + m000 * m001 * m011 + m010 * m001 * m011 + eps);
-        const float muyz = 4.f * m000 * m100 * m001 * m101 /
-                           (m000 * m100 * m001 + m000 * m100 * m101 + m000 * m001 * m101 + m100 * m001 * m101 + eps);
-        const float ayVx = A[3 * AP], azVx = A[4 * AP], axVy = A[5 * AP], azVy = A[6 * AP], axVz = A[7 * AP], ayVz = A[8 * AP];
-        S[oS + 3 * P] += muyz * (gye.x * dyVz + gze.x * dzVy + gye.y * ayVz + gze.y * azVy) * a.dt;
-        S[oS + 4 * P] += muxz * (gxe.x * dxVz + gze.x * dzVx + gxe.y * axVz + gze.y * azVx) * a.dt;
-        S[oS + 5 * P] += muxy * (gxe.x * dxVy + gye.x * dyVx + gxe.y * axVy + gye.y * ayVx) * a.dt;
-        A[3 * AP] = gye.z * ayVx + gye.w * dyVx * a.dt;
-        A[4 * AP] = gze.z * azVx + gze.w * dzVx * a.dt;
-        A[5 * AP] = gxe.z * axVy + gxe.w * dxVy * a.dt;
-        A[6 * AP] = gze.z * azVy + gze.w * dzVy * a.dt;
-        A[7 * AP] = gxe.z * axVz + gxe.w * dxVz * a.dt;
-        A[8 * AP] = gye.z * ayVz + gye.w * dyVz * a.dt;
-    }
+    const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
+    const float vx = V[0], vy = V[P], vz = V[2 * P];
+    const float vxw = V[-1], vys = V[P - rowV], vzu = V[2 * P - planeV];
+    const float vye = V[P + 1], vze = V[2 * P + 1], vxn = V[rowV], vzn = V[2 * P + rowV];
+    const float vxd = V[planeV], vyd = V[P + planeV];
+    const float lamv = M[P], m000 = M[2 * P], m100 = M[2 * P + planeM], m010 = M[2 * P + 1];
+    const float m110 = M[2 * P + planeM + 1], m001 = M[2 * P + rowM], m011 = M[2 * P + rowM + 1];
+    const float m101 = M[2 * P + planeM + rowM];
+    float ad[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) ad[q] = A[q * AP];
+    float sv[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) sv[q] = S[q * P];
+    // normal part (m_absorb_p.f90:453-474)
+    const float dxVx = (vx - vxw) * a.r20x;
+    const float dyVy = (vy - vys) * a.r20y;
+    const float dzVz = (vz - vzu) * a.r20z;
+    const float muv = m000;
+    const float lam2mu = lamv + 2.f * muv;
+    const float lamR = lam2mu - 2.f * muv;
+    const float dxa = gxc.x * dxVx + gxc.y * ad[0];
+    const float dya = gyc.x * dyVy + gyc.y * ad[1];
+    const float dza = gzc.x * dzVz + gzc.y * ad[2];
+    S[0] = sv[0] + (lam2mu * dxa + lamR * (dya + dza)) * a.dt;
+    S[P] = sv[1] + (lam2mu * dya + lamR * (dxa + dza)) * a.dt;
+    S[2 * P] = sv[2] + (lam2mu * dza + lamR * (dxa + dya)) * a.dt;
+    A[0] = gxc.z * ad[0] + gxc.w * dxVx * a.dt;
+    A[AP] = gyc.z * ad[1] + gyc.w * dyVy * a.dt;
+    A[2 * AP] = gzc.z * ad[2] + gzc.w * dzVz * a.dt;
+    // shear part (m_absorb_p.f90:477-518)
+    const float dxVy = (vye - vy) * a.r20x;
+    const float dxVz = (vze - vz) * a.r20x;
+    const float dyVx = (vxn - vx) * a.r20y;
+    const float dyVz = (vzn - vz) * a.r20y;
+    const float dzVx = (vxd - vx) * a.r20z;
+    const float dzVy = (vyd - vy) * a.r20z;
+    const float muxz = 4.f * m000 * m100 * m010 * m110 /
+                       (m000 * m100 * m010 + m000 * m100 * m110 + m000 * m010 * m110 + m100 * m010 * m110 + eps);
+    const float muxy = 4.f * m000 * m010 * m001 * m011 /
+                       (m000 * m010 * m001 + m000 * m010 * m011 + m000 * m001 * m011 + m010 * m001 * m011 + eps);
+    const float muyz = 4.f * m000 * m100 * m001 * m101 /
+                       (m000 * m100 * m001 + m000 * m100 * m101 + m000 * m001 * m101 + m100 * m001 * m101 + eps);
+    const float ayVx = ad[3], azVx = ad[4], axVy = ad[5], azVy = ad[6], axVz = ad[7], ayVz = ad[8];
+    S[3 * P] = sv[3] + muyz * (gye.x * dyVz + gze.x * dzVy + gye.y * ayVz + gze.y * azVy) * a.dt;
+    S[4 * P] = sv[4] + muxz * (gxe.x * dxVz + gze.x * dzVx + gxe.y * axVz + gze.y * azVx) * a.dt;
+    S[5 * P] = sv[5] + muxy * (gxe.x * dxVy + gye.x * dyVx + gxe.y * axVy + gye.y * ayVx) * a.dt;
+    A[3 * AP] = gye.z * ayVx + gye.w * dyVx * a.dt;
+    A[4 * AP] = gze.z * azVx + gze.w * dzVx * a.dt;
+    A[5 * AP] = gxe.z * axVy + gxe.w * dxVy * a.dt;
+    A[6 * AP] = gze.z * azVy + gze.w * dzVy * a.dt;
+    A[7 * AP] = gxe.z * axVz + gxe.w * dxVz * a.dt;
+    A[8 * AP] = gye.z * ayVz + gye.w * dyVz * a.dt;
 }
 
-// PML velocity update (m_absorb_p.f90:246-317) at shell point p.
-__device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
-    if (p >= a.npts) return;
-    const PmlPt c = pml_point(a, p);
+// PML velocity update (m_absorb_p.f90:246-317) at shell point c, loads first.
+__device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
     const int P = g.pitch;
@@ -535,46 +541,59 @@ __device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
     const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
     const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
     const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
-    const float* __restrict__ S = a.S;
-    const float* __restrict__ M = a.M;
-    float* __restrict__ V = a.V;
+    const float* __restrict__ S = a.S + oS;
+    const float* __restrict__ M = a.M + oM;
+    float* __restrict__ V = a.V + oV;
+    float* __restrict__ A = a.adeS + oA;
+    const int AP = B.pitch;
+    // loads
     const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
     const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
-    const int AP = B.pitch;
-    {
-        const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
-        // m_absorb_p.f90:265-305
-        const float sxx = S[oS], syy = S[oS + P], szz = S[oS + 2 * P];
-        const float syz = S[oS + 3 * P], sxz = S[oS + 4 * P], sxy = S[oS + 5 * P];
-        const float dxSxx = (S[oS + 1] - sxx) * a.r20x;
-        const float dySyy = (S[oS + P + rowS] - syy) * a.r20y;
-        const float dzSzz = (S[oS + 2 * P + planeS] - szz) * a.r20z;
-        const float dySyz = (syz - S[oS + 3 * P - rowS]) * a.r20y;
-        const float dzSyz = (syz - S[oS + 3 * P - planeS]) * a.r20z;
-        const float dxSxz = (sxz - S[oS + 4 * P - 1]) * a.r20x;
-        const float dzSxz = (sxz - S[oS + 4 * P - planeS]) * a.r20z;
-        const float dxSxy = (sxy - S[oS + 5 * P - 1]) * a.r20x;
-        const float dySxy = (sxy - S[oS + 5 * P - rowS]) * a.r20y;
-        const float r0 = M[oM];
-        const float bx = 2.f / (r0 + M[oM + 1]);
-        const float by = 2.f / (r0 + M[oM + rowM]);
-        const float bz = 2.f / (r0 + M[oM + planeM]);
-        float* A = a.adeS + oA;
-        const float axSxx = A[0], aySxy = A[AP], azSxz = A[2 * AP], axSxy = A[3 * AP], aySyy = A[4 * AP];
-        const float azSyz = A[5 * AP], axSxz = A[6 * AP], aySyz = A[7 * AP], azSzz = A[8 * AP];
-        V[oV] += bx * (gxe.x * dxSxx + gyc.x * dySxy + gzc.x * dzSxz + gxe.y * axSxx + gyc.y * aySxy + gzc.y * azSxz) * a.dt;
-        V[oV + P] += by * (gxc.x * dxSxy + gye.x * dySyy + gzc.x * dzSyz + gxc.y * axSxy + gye.y * aySyy + gzc.y * azSyz) * a.dt;
-        V[oV + 2 * P] += bz * (gxc.x * dxSxz + gyc.x * dySyz + gze.x * dzSzz + gxc.y * axSxz + gyc.y * aySyz + gze.y * azSzz) * a.dt;
-        A[0] = gxe.z * axSxx + gxe.w * dxSxx * a.dt;
-        A[AP] = gyc.z * aySxy + gyc.w * dySxy * a.dt;
-        A[2 * AP] = gzc.z * azSxz + gzc.w * dzSxz * a.dt;
-        A[3 * AP] = gxc.z * axSxy + gxc.w * dxSxy * a.dt;
-        A[4 * AP] = gye.z * aySyy + gye.w * dySyy * a.dt;
-        A[5 * AP] = gzc.z * azSyz + gzc.w * dzSyz * a.dt;
-        A[6 * AP] = gxc.z * axSxz + gxc.w * dxSxz * a.dt;
-        A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
-        A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
-    }
+    const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
+    const float sxx = S[0], syy = S[P], szz = S[2 * P], syz = S[3 * P], sxz = S[4 * P], sxy = S[5 * P];
+    const float sxxe = S[1], syyn = S[P + rowS], szzd = S[2 * P + planeS];
+    const float syzs = S[3 * P - rowS], syzu = S[3 * P - planeS];
+    const float sxzw = S[4 * P - 1], sxzu = S[4 * P - planeS];
+    const float sxyw = S[5 * P - 1], sxys = S[5 * P - rowS];
+    const float r0 = M[0], rx = M[1], ry = M[rowM], rz = M[planeM];
+    float ad[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) ad[q] = A[q * AP];
+    const float v0 = V[0], v1 = V[P], v2 = V[2 * P];
+    // m_absorb_p.f90:265-305
+    const float dxSxx = (sxxe - sxx) * a.r20x;
+    const float dySyy = (syyn - syy) * a.r20y;
+    const float dzSzz = (szzd - szz) * a.r20z;
+    const float dySyz = (syz - syzs) * a.r20y;
+    const float dzSyz = (syz - syzu) * a.r20z;
+    const float dxSxz = (sxz - sxzw) * a.r20x;
+    const float dzSxz = (sxz - sxzu) * a.r20z;
+    const float dxSxy = (sxy - sxyw) * a.r20x;
+    const float dySxy = (sxy - sxys) * a.r20y;
+    const float bx = 2.f / (r0 + rx);
+    const float by = 2.f / (r0 + ry);
+    const float bz = 2.f / (r0 + rz);
+    const float axSxx = ad[0], aySxy = ad[1], azSxz = ad[2], axSxy = ad[3], aySyy = ad[4];
+    const float azSyz = ad[5], axSxz = ad[6], aySyz = ad[7], azSzz = ad[8];
+    V[0] = v0 + bx * (gxe.x * dxSxx + gyc.x * dySxy + gzc.x * dzSxz + gxe.y * axSxx + gyc.y * aySxy + gzc.y * azSxz) * a.dt;
+    V[P] = v1 + by * (gxc.x * dxSxy + gye.x * dySyy + gzc.x * dzSyz + gxc.y * axSxy + gye.y * aySyy + gzc.y * azSyz) * a.dt;
+    V[2 * P] = v2 + bz * (gxc.x * dxSxz + gyc.x * dySyz + gze.x * dzSzz + gxc.y * axSxz + gyc.y * aySyz + gze.y * azSzz) * a.dt;
+    A[0] = gxe.z * axSxx + gxe.w * dxSxx * a.dt;
+    A[AP] = gyc.z * aySxy + gyc.w * dySxy * a.dt;
+    A[2 * AP] = gzc.z * azSxz + gzc.w * dzSxz * a.dt;
+    A[3 * AP] = gxc.z * axSxy + gxc.w * dxSxy * a.dt;
+    A[4 * AP] = gye.z * aySyy + gye.w * dySyy * a.dt;
+    A[5 * AP] = gzc.z * azSyz + gzc.w * dzSyz * a.dt;
+    A[6 * AP] = gxc.z * axSxz + gxc.w * dxSxz * a.dt;
+    A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
+    A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
+}
+
+__device__ __forceinline__ void stress_pml_pt(const PArgs& a, const long long p) {
+    if (p < a.npts) stress_pml_at(a, pml_point(a, p));
+}
+__device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
+    if (p < a.npts) vel_pml_at(a, pml_point(a, p));
 }
 
 // one thread per shell point; batched: block b covers points

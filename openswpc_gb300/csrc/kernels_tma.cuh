@@ -542,6 +542,20 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__
     vel_tma_tile(ta, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+// Self-test of the bounded wait: an mbarrier that expects one arrival which
+// never comes.  Every thread's wait gives up after WAIT_LIMIT polls and the
+// block records the time-out in the error word, as the TMA kernels do.
+__global__ void k_wait_selftest(int* err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait(&bar, 0u);
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+}
+
 // Batched launches: block b works on tile (e.y, e.z, e.w) of simulation e.x,
 // with e = blocks[b]; every simulation's tensor maps live in `all` (global
 // memory, 128-byte aligned).

@@ -616,6 +616,28 @@ extern "C" int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out
     return 0;
 }
 
+int swpc_gpu_selftest_wait(double* seconds) {
+    int* err = nullptr;
+    CK(cudaMalloc(&err, sizeof(int)));
+    int h = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemset(err, 0, sizeof(int));
+    cudaEventRecord(e0);
+    k_wait_selftest<<<1, 32>>>(err);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(err);
+    if (seconds) *seconds = ms / 1e3;
+    if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("wait self-test: ") + cudaGetErrorString(e));
+    return h == 1 ? set_err(SWPC_E_TIMEOUT, "bounded wait gave up as designed") : 0;
+}
+
 int swpc_gpu_get_dims(swpc_sim* sim, swpc_dims* out) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s || !out) return set_err(SWPC_E_ARG, "null argument");

@@ -46,10 +46,10 @@ EXPORTS = [
     "swpc_gpu_fetch_waveforms", "swpc_gpu_fetch_snapshot", "swpc_gpu_query", "swpc_gpu_vmax",
     "swpc_gpu_fetch_field", "swpc_gpu_profile", "swpc_gpu_profile_read", "swpc_gpu_stream",
     "swpc_gpu_launch_count", "swpc_gpu_destroy", "swpc_gpu_last_error", "swpc_host_prepare",
-    "swpc_host_write_sac", "swpc_host_nt", "swpc_host_medium",
+    "swpc_host_write_sac", "swpc_host_write_snp", "swpc_host_nt", "swpc_host_medium",
     "swpc_host_check", "swpc_gpu_fetch_field_static", "swpc_gpu_reset", "swpc_gpu_get_dims", "swpc_gpu_set_zchunk",
     "swpc_gpu_get_zchunk", "swpc_batch_create", "swpc_batch_run", "swpc_batch_sync", "swpc_batch_stream",
-    "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes",
+    "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes", "swpc_gpu_selftest_wait",
     "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
@@ -103,6 +103,7 @@ def lib(build=True):
     L.swpc_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.swpc_host_prepare.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_write_sac.argtypes = [vp, ctypes.c_char_p]
+    L.swpc_host_write_snp.argtypes = [vp, ctypes.c_char_p]
     L.swpc_host_nt.argtypes = [vp]
     L.swpc_host_check.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
     L.swpc_host_medium.argtypes = [i, i, i, i, d, d, d] + [fp] * 5 + [ip] * 6 + [dp]
@@ -118,6 +119,7 @@ def lib(build=True):
     L.swpc_batch_launch_count.argtypes = [vp]
     L.swpc_batch_launch_count.restype = ctypes.c_longlong
     L.swpc_batch_destroy.argtypes = [vp]
+    L.swpc_gpu_selftest_wait.argtypes = [dp]
     L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_request_bytes.argtypes = [vp]
     L.swpc_host_request_bytes.restype = ctypes.c_longlong
@@ -329,6 +331,9 @@ class Simulation:
 
     def write_sac(self, odir=None):
         _ck(lib().swpc_host_write_sac(self._h, os.fsencode(odir) if odir else None))
+
+    def write_snp(self, odir=None):
+        _ck(lib().swpc_host_write_snp(self._h, os.fsencode(odir) if odir else None))
 
     def close(self):
         if self._h:
