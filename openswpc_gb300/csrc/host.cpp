@@ -452,9 +452,10 @@ void mkdirs(const std::string& d) {
     }
 }
 
-// SAC header + data (src/shared/m_sac.f90:267-449, header defaults :452-562)
-void write_sac(const std::string& fn, const Meta& m, const Station& st, const char* cmp, int idep, double cmpinc,
-               double cmpaz, const float* dat, int npts) {
+// SAC header + data as bytes (src/shared/m_sac.f90:267-449, header defaults
+// :452-562): 70 floats, 35 ints, 5 logicals, 192 characters, then the data.
+std::string sac_image(const Meta& m, const Station& st, const char* cmp, int idep, double cmpinc, double cmpaz,
+                      const float* dat, int npts) {
     float fh[70];
     int ih[35], lh[5];
     char kh[192];
@@ -499,14 +500,57 @@ void write_sac(const std::string& fn, const Meta& m, const Station& st, const ch
     kset(111, 8, st.name);
     kset(113, 16, p.title.substr(0, 16));
     kset(151, 8, cmp);
+    std::string out;
+    out.reserve(632 + (size_t)npts * 4);
+    out.append((const char*)fh, sizeof fh);
+    out.append((const char*)ih, sizeof ih);
+    out.append((const char*)lh, sizeof lh);
+    out.append(kh, sizeof kh);
+    out.append((const char*)dat, (size_t)npts * 4);
+    return out;
+}
+
+void write_file(const std::string& fn, const std::string& bytes) {
     std::ofstream f(fn, std::ios::binary | std::ios::trunc);
     if (!f) throw std::runtime_error("cannot write " + fn);
-    f.write((const char*)fh, sizeof fh);
-    f.write((const char*)ih, sizeof ih);
-    f.write((const char*)lh, sizeof lh);
-    f.write(kh, sizeof kh);
-    f.write((const char*)dat, (std::streamsize)npts * 4);
+    f.write(bytes.data(), (std::streamsize)bytes.size());
+    if (!f) throw std::runtime_error("short write to " + fn);
 }
+
+// One ustar entry as the reference's tar writer lays it out
+// (src/shared/m_tar.f90 tar__whdr, tar__wpad; src/shared/m_sac.f90 tarwrite_s):
+// numeric fields as 8 or 12 octal digits without terminator, mode 0644,
+// uid/gid 0, owner root, magic "ustar" with an empty version field, and the
+// data padded with 512 - (size mod 512) zero bytes (a whole block when the
+// size is a multiple of 512).
+std::string tar_entry(const std::string& name, const std::string& data, long long mtime) {
+    char h[512];
+    std::memset(h, 0, sizeof h);
+    std::memcpy(h, name.data(), std::min<size_t>(name.size(), 99));
+    auto oct = [&](int off, int width, long long v) {
+        char buf[32];
+        std::snprintf(buf, sizeof buf, "%0*llo", width, v);
+        std::memcpy(h + off, buf + std::max(0, (int)std::strlen(buf) - width), width);
+    };
+    oct(100, 8, 420);
+    oct(108, 8, 0);
+    oct(116, 8, 0);
+    oct(124, 12, (long long)data.size());
+    oct(136, 12, mtime);
+    std::memset(h + 148, ' ', 8);
+    h[156] = '0';
+    std::memcpy(h + 257, "ustar", 5);
+    std::memcpy(h + 265, "root", 4);
+    std::memcpy(h + 297, "root", 4);
+    long long sum = 0;
+    for (unsigned char c : h) sum += c;
+    oct(148, 8, sum);
+    std::string out(h, sizeof h);
+    out += data;
+    out.append(512 - data.size() % 512, '\0');
+    return out;
+}
+
 
 // Everything the host set-up derives from one input.inf, held until the
 // simulation is put on a device: the medium, the source and receiver grid
@@ -966,18 +1010,63 @@ int swpc_host_write_sac(swpc_sim* sim, const char* odir) {
         const K kinds[4] = {{SWPC_WAV_V, 3, 7, {"Vx", "Vy", "Vz"}}, {SWPC_WAV_U, 3, 6, {"Ux", "Uy", "Uz"}},
                             {SWPC_WAV_STRESS, 6, 5, {"Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"}},
                             {SWPC_WAV_STRAIN, 6, 5, {"Exx", "Eyy", "Ezz", "Eyz", "Exz", "Exy"}}};
-        for (const K& k : kinds) {
+        // traces of every recorded kind, (ntw, ncmp, nst) Fortran order
+        std::vector<std::vector<float>> wav(4);
+        for (int q = 0; q < 4; ++q) {
+            const K& k = kinds[q];
             if (!(m.flags & k.kind)) continue;
-            std::vector<float> w((size_t)ntw * k.nc * nst);
-            int rc = swpc_gpu_fetch_waveforms(sim, k.kind, w.data());
+            wav[q].resize((size_t)ntw * k.nc * nst);
+            int rc = swpc_gpu_fetch_waveforms(sim, k.kind, wav[q].data());
             if (rc) return rc;
-            for (int s = 0; s < nst; ++s)
-                for (int c = 0; c < k.nc; ++c) {
-                    double inc = -12345, az = -12345;
-                    if (k.nc == 3) { inc = 90.0; az = c == 0 ? 0.0 + m.p.phi : c == 1 ? 90.0 + m.p.phi : 0.0; }
-                    std::string fn = dir + "/wav/" + m.p.title + ".3d." + m.st[s].name + "." + k.names[c] + ".sac";
-                    write_sac(fn, m, m.st[s], k.names[c], k.idep, inc, az, &w[((size_t)s * k.nc + c) * ntw], ntw);
+        }
+        // SAC image of station s, component c of kind q (m_wav.f90:276-330)
+        auto image = [&](int q, int s, int c) {
+            const K& k = kinds[q];
+            double inc = -12345, az = -12345;
+            if (k.nc == 3) { inc = 90.0; az = c == 0 ? 0.0 + m.p.phi : c == 1 ? 90.0 + m.p.phi : 0.0; }
+            return sac_image(m, m.st[s], k.names[c], k.idep, inc, az, &wav[q][((size_t)s * k.nc + c) * ntw], ntw);
+        };
+        const std::string& fmt = m.p.wav_format;
+        if (fmt == "csf") {
+            // one CSF file per kind, the last kind written wins as in the
+            // reference, whose file name does not name the kind
+            // (m_wav.f90:707-712, 795-808; m_sac.f90 wcsf_s)
+            for (int q = 0; q < 4; ++q) {
+                if (wav[q].empty()) continue;
+                std::string b = "CSFD";
+                const int32_t ntr = nst * kinds[q].nc, np = ntw;
+                b.append((const char*)&ntr, 4);
+                b.append((const char*)&np, 4);
+                for (int st = 0; st < nst; ++st)
+                    for (int c = 0; c < kinds[q].nc; ++c) b += image(q, st, c);
+                write_file(dir + "/wav/" + m.p.title + "__00000__.csf", b);
+            }
+        } else if (fmt == "tar_st" || fmt == "tar_node") {
+            // tar archives of SAC entries named <title>.<station>.3d.<cmp>.sac,
+            // one per station or one for the whole run (m_wav.f90:714-779)
+            std::string node;
+            for (int st = 0; st < nst; ++st) {
+                std::string arc;
+                for (int q = 0; q < 4; ++q) {
+                    if (wav[q].empty()) continue;
+                    for (int c = 0; c < kinds[q].nc; ++c)
+                        arc += tar_entry(m.p.title + "." + m.st[st].name + ".3d." + kinds[q].names[c] + ".sac",
+                                         image(q, st, c), m.exedate);
                 }
+                if (fmt == "tar_st")
+                    write_file(dir + "/wav/" + m.p.title + ".3d." + m.st[st].name + ".sac.tar", arc + std::string(1024, '\0'));
+                else
+                    node += arc;
+            }
+            if (fmt == "tar_node") write_file(dir + "/wav/" + m.p.title + ".3d.000000.sac.tar", node + std::string(1024, '\0'));
+        } else {
+            for (int q = 0; q < 4; ++q) {
+                if (wav[q].empty()) continue;
+                for (int st = 0; st < nst; ++st)
+                    for (int c = 0; c < kinds[q].nc; ++c)
+                        write_file(dir + "/wav/" + m.p.title + ".3d." + m.st[st].name + "." + kinds[q].names[c] + ".sac",
+                                   image(q, st, c));
+            }
         }
         return 0;
     } catch (const std::exception& e) {

@@ -112,3 +112,41 @@ def test_command_line_driver(tmp_path):
     _, _, _, d = read_sac(str(tmp_path / "cli" / "wav" / "outs.3d.ST07.Vy.sac"))
     assert np.array_equal(d, w[6, 1])
     assert os.path.getsize(str(tmp_path / "cli" / "outs.3d.xy.v.snp")) > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fmt", ["csf", "tar_st", "tar_node"])
+def test_csf_and_tar_trace_formats(tmp_path, fmt):
+    """wav_format = csf / tar_st / tar_node hold the same SAC images as the
+    per-trace files (m_wav.f90:707-779)."""
+    import tarfile
+    inf = configs.write_plain_small(str(tmp_path), nt=NT, title="outs", wav_format=fmt)
+    s = gpu.Simulation.from_inf(inf)
+    s.run(1, NT)
+    s.sync()
+    w = s.waveforms()
+    s.write_sac(str(tmp_path / "o"))
+    s.close()
+    one = 632 + 4 * NT
+    if fmt == "csf":
+        b = open(str(tmp_path / "o" / "wav" / "outs__00000__.csf"), "rb").read()
+        assert b[:4] == b"CSFD"
+        ntr, npts = struct.unpack_from("<2i", b, 4)
+        assert (ntr, npts) == (16 * 3, NT) and len(b) == 12 + ntr * one
+        for st, c in ((0, 0), (5, 2), (15, 1)):
+            o = 12 + (3 * st + c) * one
+            assert np.array_equal(np.frombuffer(b[o + 632:o + one], np.float32), w[st, c])
+            assert b[o + 440:o + 448].decode().strip() == "ST%02d" % (st + 1)
+        return
+    fn = "outs.3d.ST03.sac.tar" if fmt == "tar_st" else "outs.3d.000000.sac.tar"
+    path = str(tmp_path / "o" / "wav" / fn)
+    raw = open(path, "rb").read()
+    assert len(raw) % 512 == 0 and raw[-1024:] == b"\0" * 1024
+    with tarfile.open(path) as t:
+        names = t.getnames()
+        assert "outs.ST03.3d.Vz.sac" in names
+        assert len(names) == (3 if fmt == "tar_st" else 48)
+        img = t.extractfile("outs.ST03.3d.Vz.sac").read()
+        m = t.getmember("outs.ST03.3d.Vz.sac")
+        assert m.size == one and m.mode == 0o644 and m.uname == "root"
+    assert np.array_equal(np.frombuffer(img[632:], np.float32), w[2, 2])
