@@ -50,8 +50,14 @@ enum { SWPC_STORE_FP32 = 0, SWPC_STORE_FP16 = 1, SWPC_STORE_BF16 = 2 };
 /* Receiver outputs (m_wav.f90:31-34) */
 enum { SWPC_WAV_V = 1, SWPC_WAV_U = 2, SWPC_WAV_STRESS = 4, SWPC_WAV_STRAIN = 8 };
 
-/* Snapshot kinds (m_snap.f90:105-119); the xy section only in this version */
+/* xy-section snapshot kinds of swpc_gpu_set_snapshot (m_snap.f90:105-119) */
 enum { SWPC_SNAP_XY_V = 1, SWPC_SNAP_XY_U = 2 };
+
+/* Snapshot sections and kinds of swpc_gpu_add_snapshot (m_snap.f90:105-119):
+ * xy at k0_xy, yz at i0_yz, xz at j0_xz, fs at kfs+1 and ob at kob+1 of
+ * every column; velocity, displacement, divergence/rotation ("ps"). */
+enum { SWPC_SEC_XY = 0, SWPC_SEC_YZ = 1, SWPC_SEC_XZ = 2, SWPC_SEC_FS = 3, SWPC_SEC_OB = 4 };
+enum { SWPC_SNAPK_V = 0, SWPC_SNAPK_U = 1, SWPC_SNAPK_PS = 2 };
 
 /* Source time functions (m_fdtool.f90:472-497) */
 enum { SWPC_STF_BOXCAR = 0, SWPC_STF_TRIANGLE = 1, SWPC_STF_HERRMANN = 2,
@@ -108,6 +114,18 @@ int swpc_gpu_set_receivers(swpc_sim* sim, int n, const int* ijk, int ntdec_w, in
  * decimation idec/jdec, every ntdec_s steps; kinds is a mask of SWPC_SNAP_*. */
 int swpc_gpu_set_snapshot(swpc_sim* sim, int kinds, int k0, int idec, int jdec, int ntdec_s);
 
+/* Any of the fifteen snapshots of m_snap.f90 (wbuf_{xy,yz,xz,fs,ob}_{v,u,ps},
+ * :981-2205): section SWPC_SEC_*, kind SWPC_SNAPK_*, fix = the 1-based k0
+ * (xy), i0 (yz) or j0 (xz) (ignored for fs/ob), decimation along the
+ * section's first and second axis (xy/fs/ob: idec, jdec; yz: jdec, kdec;
+ * xz: idec, kdec), frames at it = 1, 1+ntdec_s, ... (every snapshot shares
+ * ntdec_s).  A frame holds nc planes of (n1, n2) floats: nc = 3 (Vx Vy Vz,
+ * Ux Uy Uz) or 4 (div, rot_x, rot_y, rot_z), scaled as the reference
+ * writes them.  Adding the same section and kind again replaces it. */
+int swpc_gpu_add_snapshot(swpc_sim* sim, int section, int kind, int fix, int dec1, int dec2, int ntdec_s);
+int swpc_gpu_query_snapshot(swpc_sim* sim, int section, int kind, int* n1, int* n2, int* nframes);
+int swpc_gpu_fetch_section(swpc_sim* sim, int section, int kind, int frame, float* out);
+
 /* One time step it (main.f90:120-138 minus host I/O). */
 int swpc_gpu_step(swpc_sim* sim, int it);
 
@@ -132,7 +150,8 @@ int swpc_gpu_query(swpc_sim* sim, int* ntw, int* nst, int* nxs, int* nys, int* n
 int swpc_gpu_vmax(swpc_sim* sim, float out[3]);
 
 /* One state field over the physical grid, Fortran (nz, nx, ny) order, as
- * double: which = 0..8 for Vx Vy Vz Sxx Syy Szz Syz Sxz Sxy. */
+ * double: which = 0..8 for Vx Vy Vz Sxx Syy Szz Syz Sxz Sxy, 9..13 for the
+ * uploaded medium rho lam mu taup taus. */
 int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out);
 
 /* The same read-back for callers that cannot allocate device memory (a host

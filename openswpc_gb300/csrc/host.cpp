@@ -216,9 +216,10 @@ void c2g(double x, double y, double lon0, double lat0, double phi, double& lon, 
 // ---------------------------------------------------------------------------
 struct Params {
     std::string title, odir, abc_type, vmodel_type, stftype, stf_format, fn_stf, sdep_fit, st_format, fn_stloc, wav_format;
-    int nx, ny, nz, nt, na, ntdec_w, ntdec_r, ntdec_s, idec, jdec;
-    double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut, z0_xy;
-    bool bf_mode, sw_v, sw_u, sw_stress, sw_strain, xy_v, xy_u, munk;
+    int nx, ny, nz, nt, na, ntdec_w, ntdec_r, ntdec_s, idec, jdec, kdec;
+    double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut, z0_xy, x0_yz, y0_xz;
+    bool bf_mode, sw_v, sw_u, sw_stress, sw_strain, munk;
+    int snap_sw[5];  // per section xy yz xz fs ob: bit SWPC_SNAPK_* set when <sec>_<kind>%sw is true
 };
 
 struct Station { std::string name; double x, y, z, lon, lat; int i, j, k; };
@@ -230,10 +231,16 @@ struct Meta {  // what the SAC writer needs after set-up
     double m6[6] = {0, 0, 0, 0, 0, 0}, f3[3] = {0, 0, 0};
     long long exedate = 0;
     int ntw = 0, flags = 0;
-    // xy-section snapshot files (m_snap.f90:413-473, 846-892): section size,
-    // the medium planes rho, lam, mu at k0_xy and the topography depth
-    int snp_kinds = 0, nxs = 0, nys = 0;
-    std::vector<float> snp_med;  // (nxs, nys, 3) Fortran order
+    // snapshot files (m_snap.f90:324-473, 846-892): per section the grid of
+    // pixels, the header's first coordinates and spacings, the absorber
+    // widths and the medium planes (rho, lam, mu over the section, Fortran
+    // order), plus the topography depth of the horizontal sections
+    struct SnapSec {
+        int sec = 0, kinds = 0, fix = 1, d1 = 1, d2 = 1, n1 = 0, n2 = 0, na1 = 0, na2 = 0;
+        float x1 = 0, x2 = 0, dx1 = 0, dx2 = 0;
+        std::vector<float> med;
+    };
+    std::vector<SnapSec> snaps;
     double bd0 = 0;
 };
 std::mutex g_meta_mu;
@@ -563,7 +570,7 @@ struct Prepared {
     double ts[3] = {0, 0, 0};
     std::vector<int> sijk, rijk;
     std::vector<double> smo, smij, sf3, sprm;
-    int stf = 0, bf_mode = 0, flags = 0, ntdec_w = 1, kinds = 0, k0 = 1, idec = 1, jdec = 1, ntdec_s = 10;
+    int stf = 0, bf_mode = 0, flags = 0, ntdec_w = 1, ntdec_s = 10;
 };
 
 // Host half of the set-up (src/swpc_3d/main.f90:48-117 without the device):
@@ -597,13 +604,25 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     p.sw_v = inf.b("sw_wav_v", false); p.sw_u = inf.b("sw_wav_u", false);
     p.sw_stress = inf.b("sw_wav_stress", false); p.sw_strain = inf.b("sw_wav_strain", false);
     p.ntdec_r = inf.i("ntdec_r", 100);
-    p.xy_v = inf.b("xy_v%sw", false); p.xy_u = inf.b("xy_u%sw", false);
-    double zend = p.zbeg + p.nz * p.dz;
+    // snapshot switches and planes (m_snap.f90:105-127)
+    {
+        const char* secs[5] = {"xy", "yz", "xz", "fs", "ob"};
+        const char* kinds[3] = {"v", "u", "ps"};
+        for (int q = 0; q < 5; ++q) {
+            p.snap_sw[q] = 0;
+            for (int c = 0; c < 3; ++c)
+                if (inf.b(std::string(secs[q]) + "_" + kinds[c] + "%sw", false)) p.snap_sw[q] |= 1 << c;
+        }
+    }
+    double zend = p.zbeg + p.nz * p.dz, xend = p.xbeg + p.nx * p.dx, yend = p.ybeg + p.ny * p.dy;
     p.z0_xy = inf.r("z0_xy", std::max(std::min(10.0, zend), p.zbeg));
-    p.idec = inf.i("idec", 1); p.jdec = inf.i("jdec", 1); p.ntdec_s = inf.i("ntdec_s", 10);
-    for (const char* k : {"xy_ps%sw", "yz_ps%sw", "xz_ps%sw", "fs_ps%sw", "ob_ps%sw", "yz_v%sw", "xz_v%sw", "fs_v%sw",
-                          "ob_v%sw", "yz_u%sw", "xz_u%sw", "fs_u%sw", "ob_u%sw"})
-        if (inf.b(k, false)) std::fprintf(stderr, "swpc: snapshot %s is not produced by this build\n", k);
+    p.x0_yz = inf.r("x0_yz", std::max(std::min(0.0, xend), p.xbeg));
+    p.y0_xz = inf.r("y0_xz", std::max(std::min(0.0, yend), p.ybeg));
+    p.idec = inf.i("idec", 1); p.jdec = inf.i("jdec", 1); p.kdec = inf.i("kdec", 1); p.ntdec_s = inf.i("ntdec_s", 10);
+    if (p.idec < 1 || p.jdec < 1 || p.kdec < 1 || p.ntdec_s < 1)
+        throw std::runtime_error("idec, jdec, kdec and ntdec_s must be positive");
+    if (inf.s("snp_format", "native") != "native")
+        std::fprintf(stderr, "swpc: snp_format other than native is written as native by this build\n");
     if (p.nt < 1) throw std::runtime_error("nt must be positive");
 
     Grid G{p.nx, p.ny, p.nz};
@@ -684,7 +703,6 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     } else {
         for (auto& s : srcs) M0 += s.mo;
     }
-    const double xend = p.xbeg + p.nx * p.dx, yend = p.ybeg + p.ny * p.dy;
     std::vector<int> sijk;
     std::vector<double> smo, smij, sf3, sprm;
     for (auto& s : srcs) {
@@ -777,25 +795,57 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     for (auto& st : meta.st) P.rijk.insert(P.rijk.end(), {st.i, st.j, st.k});
     P.flags = flags;
     P.ntdec_w = std::max(1, p.ntdec_w);
-    P.kinds = (p.xy_v ? SWPC_SNAP_XY_V : 0) | (p.xy_u ? SWPC_SNAP_XY_U : 0);
-    P.k0 = std::max(1, std::min(p.nz, x2i(p.z0_xy, p.zbeg, p.dz)));
-    P.idec = p.idec; P.jdec = p.jdec; P.ntdec_s = p.ntdec_s;
-    if (P.kinds) {  // snap__setup / newfile_xy (m_snap.f90:131-133, 436-458)
-        const int idec = std::max(1, p.idec), jdec = std::max(1, p.jdec);
-        meta.snp_kinds = P.kinds;
-        meta.nxs = (p.nx + idec / 2) / idec;
-        meta.nys = (p.ny + jdec / 2) / jdec;
-        meta.bd0 = bd0;
-        meta.snp_med.assign((size_t)meta.nxs * meta.nys * 3, 0.f);
-        const size_t pl = (size_t)meta.nxs * meta.nys;
-        for (int j = 1; j <= meta.nys; ++j)
-            for (int i = 1; i <= meta.nxs; ++i) {
-                const int ii = i * idec - idec / 2, jj = j * jdec - jdec / 2;
-                const size_t q = (size_t)(j - 1) * meta.nxs + (i - 1), c = G.idx(P.k0, ii, jj);
-                meta.snp_med[q] = P.rho[c];
-                meta.snp_med[pl + q] = P.lam[c];
-                meta.snp_med[2 * pl + q] = P.mu[c];
+    P.ntdec_s = p.ntdec_s;
+    meta.bd0 = bd0;
+    {  // snap__setup and newfile_* (m_snap.f90:131-160, 324-473)
+        const int idec = p.idec, jdec = p.jdec, kdec = p.kdec;
+        const int nxs = (p.nx + idec / 2) / idec, nys = (p.ny + jdec / 2) / jdec, nzs = (p.nz + kdec / 2) / kdec;
+        // section coordinates in single precision as i2x/j2y/k2z compute them
+        // (m_fdtool.f90:639-680)
+        auto c2f = [](int i, double b, double d) { const float t = ((float)i - 0.5f) * (float)d; return (float)b + t; };
+        const int k0 = x2i(p.z0_xy, p.zbeg, p.dz), i0 = x2i(p.x0_yz, p.xbeg, p.dx), j0 = x2i(p.y0_xz, p.ybeg, p.dy);
+        for (int sec = 0; sec < 5; ++sec) {
+            if (!p.snap_sw[sec]) continue;
+            Meta::SnapSec S;
+            S.sec = sec;
+            S.kinds = p.snap_sw[sec];
+            const bool horiz = sec == SWPC_SEC_XY || sec == SWPC_SEC_FS || sec == SWPC_SEC_OB;
+            int dd1 = idec, dd2 = jdec;
+            double b1 = p.xbeg, b2 = p.ybeg, h1 = p.dx, h2 = p.dy;
+            if (sec == SWPC_SEC_YZ) { dd1 = jdec; dd2 = kdec; b1 = p.ybeg; b2 = p.zbeg; h1 = p.dy; h2 = p.dz; }
+            if (sec == SWPC_SEC_XZ) { dd1 = idec; dd2 = kdec; b2 = p.zbeg; h2 = p.dz; }
+            S.d1 = dd1; S.d2 = dd2;
+            S.n1 = sec == SWPC_SEC_YZ ? nys : nxs;
+            S.n2 = horiz ? nys : nzs;
+            S.na1 = p.na / dd1; S.na2 = p.na / dd2;
+            S.fix = sec == SWPC_SEC_XY ? k0 : sec == SWPC_SEC_YZ ? i0 : sec == SWPC_SEC_XZ ? j0 : 1;
+            if (!horiz || sec == SWPC_SEC_XY) {
+                const int lim = sec == SWPC_SEC_XY ? p.nz : sec == SWPC_SEC_YZ ? p.nx : p.ny;
+                if (S.fix < 1 || S.fix > lim) throw std::runtime_error("snapshot section outside the model");
             }
+            S.x1 = c2f(dd1 - dd1 / 2, b1, h1);
+            S.x2 = c2f(dd2 - dd2 / 2, b2, h2);
+            S.dx1 = c2f(2 * dd1 - dd1 / 2, b1, h1) - S.x1;
+            S.dx2 = c2f(2 * dd2 - dd2 / 2, b2, h2) - S.x2;
+            const size_t pl = (size_t)S.n1 * S.n2;
+            S.med.assign(3 * pl, 0.f);
+            for (int b = 1; b <= S.n2; ++b)
+                for (int a = 1; a <= S.n1; ++a) {
+                    const int ca = a * dd1 - dd1 / 2, cb = b * dd2 - dd2 / 2;
+                    int i, j, k;
+                    if (sec == SWPC_SEC_YZ) { i = S.fix; j = ca; k = cb; }
+                    else if (sec == SWPC_SEC_XZ) { i = ca; j = S.fix; k = cb; }
+                    else {
+                        i = ca; j = cb;
+                        k = sec == SWPC_SEC_XY ? S.fix : (sec == SWPC_SEC_FS ? P.kfs : P.kob)[G.idx2(i, j)] + 1;
+                    }
+                    const size_t q = (size_t)(b - 1) * S.n1 + (a - 1), c = G.idx(k, i, j);
+                    S.med[q] = P.rho[c];
+                    S.med[pl + q] = P.lam[c];
+                    S.med[2 * pl + q] = P.mu[c];
+                }
+            meta.snaps.push_back(std::move(S));
+        }
     }
     P.meta = std::move(meta);
     return 0;
@@ -817,8 +867,10 @@ int materialize(const Prepared& P, swpc_sim** out) {
         return bail(rc);
     if ((rc = swpc_gpu_set_receivers(sim, (int)P.meta.st.size(), P.rijk.data(), P.ntdec_w, P.flags)))
         return bail(rc);
-    if (P.kinds && (rc = swpc_gpu_set_snapshot(sim, P.kinds, P.k0, P.idec, P.jdec, P.ntdec_s)))
-        return bail(rc);
+    for (const auto& S : P.meta.snaps)
+        for (int kind = 0; kind < 3; ++kind)
+            if ((S.kinds >> kind & 1) && (rc = swpc_gpu_add_snapshot(sim, S.sec, kind, S.fix, S.d1, S.d2, P.ntdec_s)))
+                return bail(rc);
     Meta meta = P.meta;
     swpc_gpu_query(sim, &meta.ntw, nullptr, nullptr, nullptr, nullptr);
     {
@@ -937,56 +989,58 @@ int swpc_host_write_snp(swpc_sim* sim, const char* odir) {
         if (it == g_meta.end()) return swpc::set_err(SWPC_E_STATE, "simulation was not prepared by swpc_host_prepare");
         m = it->second;
     }
-    if (!m.snp_kinds) return 0;
+    if (m.snaps.empty()) return 0;
     try {
         const Params& p = m.p;
         std::string dir = (odir && *odir) ? std::string(odir) : p.odir;
         mkdirs(dir);
-        int nxs = 0, nys = 0, nframes = 0;
-        int rc = swpc_gpu_query(sim, nullptr, nullptr, &nxs, &nys, &nframes);
-        if (rc) return rc;
-        if (nxs != m.nxs || nys != m.nys) return swpc::set_err(SWPC_E_STATE, "snapshot geometry differs from the set-up");
-        const int idec = std::max(1, p.idec), jdec = std::max(1, p.jdec);
-        // coordinates in single precision as i2x/j2y compute them (m_fdtool.f90:639-680)
-        const float xb = (float)p.xbeg, yb = (float)p.ybeg, dxf = (float)p.dx, dyf = (float)p.dy;
-        auto i2x = [](int i, float b, float d) { const float t = ((float)i - 0.5f) * d; return b + t; };
-        const float xs1 = i2x(idec - idec / 2, xb, dxf), xs2 = i2x(2 * idec - idec / 2, xb, dxf);
-        const float ys1 = i2x(jdec - jdec / 2, yb, dyf), ys2 = i2x(2 * jdec - jdec / 2, yb, dyf);
-        const size_t pl = (size_t)nxs * nys;
-        std::vector<float> frame(pl * 3);
-        for (int kind : {SWPC_SNAP_XY_V, SWPC_SNAP_XY_U}) {
-            if (!(m.snp_kinds & kind)) continue;
-            const bool v = kind == SWPC_SNAP_XY_V;
-            const std::string fn = dir + "/" + p.title + ".3d.xy." + (v ? "v" : "u") + ".snp";
-            std::ofstream f(fn, std::ios::binary | std::ios::trunc);
-            if (!f) throw std::runtime_error("cannot write " + fn);
-            auto wi = [&](int32_t x) { f.write((const char*)&x, 4); };
-            auto wf = [&](float x) { f.write((const char*)&x, 4); };
-            auto ws = [&](const std::string& t, size_t n) {
-                std::string u = t.substr(0, n);
-                u.resize(n, ' ');
-                f.write(u.data(), (std::streamsize)n);
-            };
-            // write_snp_header (m_snap.f90:846-892), header version 6
-            ws("STREAMIO", 8); ws("SWPC_3D ", 8); wi(6); ws(p.title, 80); wi((int32_t)m.exedate);
-            ws("xy", 2); ws(v ? "v3" : "u3", 2); wi(nxs); wi(nys);
-            wf(xs1); wf(ys1); wf(xs2 - xs1); wf(ys2 - ys1);
-            wf((float)p.dt * (float)p.ntdec_s);
-            wi(p.na / idec); wi(p.na / jdec);
-            wi(6); wi(3);  // nmed, nsnp of the xy section (m_snap.f90:200-205)
-            wf((float)p.clon); wf((float)p.clat); wf((float)p.phi);
-            wf(1.f); wf(1.f); wf(1.f);
-            // medium planes rho, lam, mu at k0_xy, then the topography (newfile_xy)
-            f.write((const char*)m.snp_med.data(), (std::streamsize)(m.snp_med.size() * 4));
-            const float topo = -(float)m.bd0 * 1000.f;
-            std::vector<float> tp(pl, topo);
-            f.write((const char*)tp.data(), (std::streamsize)(pl * 4));
-            // one (nxs, nys) plane per component per frame (wbuf_xy_v / wbuf_xy_u)
-            for (int q = 0; q < nframes; ++q) {
-                if ((rc = swpc_gpu_fetch_snapshot(sim, kind, q, frame.data()))) return rc;
-                f.write((const char*)frame.data(), (std::streamsize)(frame.size() * 4));
+        const char* secname[5] = {"xy", "yz", "xz", "fs", "ob"};
+        const char* kindname[3] = {"v", "u", "ps"};
+        const char* typname[3] = {"v3", "u3", "ps"};
+        for (const auto& S : m.snaps) {
+            const bool horiz = S.sec == SWPC_SEC_XY || S.sec == SWPC_SEC_FS || S.sec == SWPC_SEC_OB;
+            const size_t pl = (size_t)S.n1 * S.n2;
+            for (int kind = 0; kind < 3; ++kind) {
+                if (!(S.kinds >> kind & 1)) continue;
+                int n1 = 0, n2 = 0, nframes = 0;
+                int rc = swpc_gpu_query_snapshot(sim, S.sec, kind, &n1, &n2, &nframes);
+                if (rc) return rc;
+                if (n1 != S.n1 || n2 != S.n2) return swpc::set_err(SWPC_E_STATE, "snapshot geometry differs from the set-up");
+                const int nc = kind == SWPC_SNAPK_PS ? 4 : 3;
+                const std::string fn = dir + "/" + p.title + ".3d." + secname[S.sec] + "." + kindname[kind] + ".snp";
+                std::ofstream f(fn, std::ios::binary | std::ios::trunc);
+                if (!f) throw std::runtime_error("cannot write " + fn);
+                auto wi = [&](int32_t x) { f.write((const char*)&x, 4); };
+                auto wf = [&](float x) { f.write((const char*)&x, 4); };
+                auto ws = [&](const std::string& t, size_t n) {
+                    std::string u = t.substr(0, n);
+                    u.resize(n, ' ');
+                    f.write(u.data(), (std::streamsize)n);
+                };
+                // write_snp_header (m_snap.f90:846-892), header version 6
+                ws("STREAMIO", 8); ws("SWPC_3D ", 8); wi(6); ws(p.title, 80); wi((int32_t)m.exedate);
+                ws(secname[S.sec], 2); ws(typname[kind], 2); wi(S.n1); wi(S.n2);
+                wf(S.x1); wf(S.x2); wf(S.dx1); wf(S.dx2);
+                wf((float)p.dt * (float)p.ntdec_s);
+                wi(S.na1); wi(S.na2);
+                wi(horiz ? 6 : 3); wi(nc);  // nmed, nsnp (m_snap.f90:200-207)
+                wf((float)p.clon); wf((float)p.clat); wf((float)p.phi);
+                wf(1.f); wf(1.f); wf(1.f);
+                // medium planes rho, lam, mu, and the topography of the
+                // horizontal sections (newfile_yz/xz/xy)
+                f.write((const char*)S.med.data(), (std::streamsize)(S.med.size() * 4));
+                if (horiz) {
+                    std::vector<float> tp(pl, -(float)m.bd0 * 1000.f);
+                    f.write((const char*)tp.data(), (std::streamsize)(pl * 4));
+                }
+                // nc planes of (n1, n2) per frame (wbuf_*)
+                std::vector<float> frame(pl * nc);
+                for (int q = 0; q < nframes; ++q) {
+                    if ((rc = swpc_gpu_fetch_section(sim, S.sec, kind, q, frame.data()))) return rc;
+                    f.write((const char*)frame.data(), (std::streamsize)(frame.size() * 4));
+                }
+                if (!f) throw std::runtime_error("short write to " + fn);
             }
-            if (!f) throw std::runtime_error("short write to " + fn);
         }
         return 0;
     } catch (const std::exception& e) {

@@ -800,43 +800,99 @@ __device__ __forceinline__ void taps_one(const TapArgs& a, const int n) {
 __global__ void k_taps(const TapArgs a) { taps_one(a, blockIdx.x * blockDim.x + threadIdx.x); }
 __global__ void k_taps_batch(const TapArgs* __restrict__ all) { taps_one(all[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x); }
 
+// Snapshot sections (m_snap.f90:95-473): xy at k0, yz at i0, xz at j0, and
+// the free-surface / ocean-bottom maps at kfs+1 / kob+1 of every column;
+// kinds: velocity, displacement (integrated every step), and divergence /
+// rotation with the medium and shear-stress masks.
+enum { SEC_XY = 0, SEC_YZ = 1, SEC_XZ = 2, SEC_FS = 3, SEC_OB = 4 };
+enum { SNAP_V = 0, SNAP_U = 1, SNAP_PS = 2 };
+constexpr int MAX_SNAP = 15;
+
+struct SnapPlane {
+    int sec, kind;
+    int n1, n2;         // pixels along the first and second axis
+    int d1, d2;         // decimation along them
+    int fix;            // 0-based k (xy), i (yz) or j (xz)
+    int nc;             // 3 (v, u) or 4 (ps)
+    float* frames;      // (maxframes, nc, n2, n1)
+    double* uacc;       // (3, n2, n1) running displacement (u only)
+};
+
 struct SnapArgs {
     Geo g;
     const float* V;
-    int kinds, kz0, idec, jdec, ntdec_s, nxs, nys, maxframes;
-    float vscale;   // UC * M0
-    float dt;
-    float* xy_v;    // frames of (nxs, nys, 3)
-    float* xy_u;    // same
-    double* uacc;   // (nxs, nys, 3) running displacement
+    const float* S;
+    const float* M;
+    const int* kfs;     // (nx, ny) 1-based kfs of each column, 0-based map
+    const int* kob;     // same for kob
+    int n, ntdec_s, maxframes, maxpix;
+    float UC, M0, dt, r20x, r20y, r20z;
+    SnapPlane pl[MAX_SNAP];
     const int* it;
 };
 
-// m_snap.f90:1587-1653 (xy_v) and 1963-2025 (xy_u)
-__device__ __forceinline__ void snap_one(const SnapArgs& a, const int ii, const int jj) {
-    if (!a.kinds || ii >= a.nxs || jj >= a.nys) return;
+// wbuf_{xy,yz,xz,fs,ob}_{v,u,ps} (m_snap.f90:981-2205) for pixel q of plane P
+__device__ __forceinline__ void snap_pix(const SnapArgs& a, const SnapPlane& P, const int q) {
+    if (q >= P.n1 * P.n2) return;
     const int it = *a.it;
-    const int i = (ii + 1) * a.idec - a.idec / 2 - 1;
-    const int j = (jj + 1) * a.jdec - a.jdec / 2 - 1;
     const Geo& g = a.g;
-    const size_t pl = (size_t)a.nxs * a.nys;
-    const size_t q = (size_t)jj * a.nxs + ii;
-    float v3[3];
-    for (int c = 0; c < 3; ++c) v3[c] = a.V[goff(g, 3, c, i, j, a.kz0)];
-    if (a.kinds & 2)
-        for (int c = 0; c < 3; ++c) a.uacc[q + c * pl] += (double)v3[c] * (double)a.vscale * (double)a.dt;
-    if ((it - 1) % a.ntdec_s != 0) return;
-    const int fr = (it - 1) / a.ntdec_s;
-    if (fr >= a.maxframes) return;
-    if (a.kinds & 1)
-        for (int c = 0; c < 3; ++c) a.xy_v[(size_t)fr * 3 * pl + c * pl + q] = v3[c] * a.vscale;
-    if (a.kinds & 2)
-        for (int c = 0; c < 3; ++c) a.xy_u[(size_t)fr * 3 * pl + c * pl + q] = (float)a.uacc[q + c * pl];
+    const int p1 = q % P.n1, p2 = q / P.n1;
+    auto dec = [](int pp, int d) { return (pp + 1) * d - d / 2 - 1; };  // 0-based cell of pixel pp
+    int i, j, k;
+    switch (P.sec) {
+    case SEC_YZ: i = P.fix; j = dec(p1, P.d1); k = dec(p2, P.d2); break;
+    case SEC_XZ: i = dec(p1, P.d1); j = P.fix; k = dec(p2, P.d2); break;
+    default:
+        i = dec(p1, P.d1); j = dec(p2, P.d2);
+        k = P.sec == SEC_XY ? P.fix : (P.sec == SEC_FS ? a.kfs : a.kob)[(size_t)j * g.nx + i];  // (kfs|kob)+1, 1-based
+        break;
+    }
+    const size_t pl = (size_t)P.n1 * P.n2;
+    const bool frame = (it - 1) % a.ntdec_s == 0 && (it - 1) / a.ntdec_s < a.maxframes;
+    float* out = P.frames + (frame ? (size_t)((it - 1) / a.ntdec_s) * P.nc * pl : 0) + q;
+    const float* V = a.V;
+    auto v = [&](int c, int di, int dj, int dk) { return V[goff(g, 3, c, i + di, j + dj, k + dk)]; };
+    if (P.kind == SNAP_V) {
+        if (!frame) return;
+        for (int c = 0; c < 3; ++c) out[c * pl] = v(c, 0, 0, 0) * a.UC * a.M0;
+    } else if (P.kind == SNAP_U) {
+        // integrated every step; FP64 accumulation (the reference sums in FP32)
+        for (int c = 0; c < 3; ++c) {
+            double u = P.uacc[c * pl + q] + (double)(v(c, 0, 0, 0) * a.UC * a.M0) * (double)a.dt;
+            P.uacc[c * pl + q] = u;
+            if (frame) out[c * pl] = (float)u;
+        }
+    } else {
+        if (!frame) return;
+        const float eps = 1.1920928955078125e-07f;
+        const float vx = v(0, 0, 0, 0), vy = v(1, 0, 0, 0), vz = v(2, 0, 0, 0);
+        float div = (vx - v(0, -1, 0, 0)) * a.r20x + (vy - v(1, 0, -1, 0)) * a.r20y + (vz - v(2, 0, 0, -1)) * a.r20z;
+        float rx = (v(2, 0, 1, 0) - vz) * a.r20y - (v(1, 0, 0, 1) - vy) * a.r20z;
+        float ry = (v(0, 0, 0, 1) - vx) * a.r20z - (v(2, 1, 0, 0) - vz) * a.r20x;
+        float rz = (v(1, 1, 0, 0) - vy) * a.r20x - (v(0, 0, 1, 0) - vx) * a.r20y;
+        const float lam = a.M[goff(g, 5, 1, i, j, k)];
+        const float syz = a.S[goff(g, 6, 3, i, j, k)], sxz = a.S[goff(g, 6, 4, i, j, k)], sxy = a.S[goff(g, 6, 5, i, j, k)];
+        div = div * lam / fabsf(lam + eps);
+        if (P.sec == SEC_YZ) {  // wbuf_yz_ps masks with |S| / |S + eps| (m_snap.f90:1027-1030)
+            rx = rx * fabsf(syz) / fabsf(syz + eps);
+            ry = ry * fabsf(sxz) / fabsf(sxz + eps);
+            rz = rz * fabsf(sxy) / fabsf(sxy + eps);
+        } else {
+            rx = rx * fabsf(syz) / (fabsf(syz) + eps);
+            ry = ry * fabsf(sxz) / (fabsf(sxz) + eps);
+            rz = rz * fabsf(sxy) / (fabsf(sxy) + eps);
+        }
+        out[0] = div * a.UC * a.M0 * 1e-3f;
+        out[pl] = rx * a.UC * a.M0 * 1e-3f;
+        out[2 * pl] = ry * a.UC * a.M0 * 1e-3f;
+        out[3 * pl] = rz * a.UC * a.M0 * 1e-3f;
+    }
 }
 
-__global__ void k_snap_xy(const SnapArgs a) { snap_one(a, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y); }
-__global__ void k_snap_xy_batch(const SnapArgs* __restrict__ all) {
-    snap_one(all[blockIdx.z], blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+__global__ void k_snap(const SnapArgs a) { snap_pix(a, a.pl[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_snap_batch(const SnapArgs* __restrict__ all) {
+    const SnapArgs& a = all[blockIdx.z];
+    if ((int)blockIdx.y < a.n) snap_pix(a, a.pl[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 struct VmaxArgs {

@@ -44,6 +44,7 @@ struct Sim {
     int cer_off[6] = {0, 0, 0, 0, 0, 0};
     int* d_it = nullptr;
     int* d_kob = nullptr;
+    int* d_kfs = nullptr;
     int* d_err = nullptr;   // set by a kernel whose bounded wait ran out
     Coef coef{};
     int kchunk = 1, kchunk_auto = 1;
@@ -70,12 +71,14 @@ struct Sim {
     int dalloc(void** ptr, size_t bytes);
     int allocate();
     int upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
-                      const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top, const int* kob_bot,
-                      const double* ts);
+                      const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
+                      const int* kob_bot, const double* ts);
     int set_sources(int n, const int* ijk, const double* mo, const double* mij, const double* fxyz, const double* prm,
                     int stftype, bool bf);
     int set_receivers(int n, const int* ijk, int ntdec_w, int flags);
-    int set_snapshot(int kinds, int k0, int idec, int jdec, int ntdec_s);
+    int add_snapshot(int sec, int kind, int fix, int d1, int d2, int ntdec_s);
+    const SnapPlane* find_plane(int sec, int kind) const;
+    int nframes_done() const;
     void fill_zargs(ZArgs& z) const;
     int launch_step(bool timed);
     int ensure_graph();

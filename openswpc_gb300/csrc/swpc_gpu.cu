@@ -171,9 +171,9 @@ int Sim::launch_step(bool timed) {
         k_taps<<<(tap_args.n + 127) / 128, 128, 0, stream>>>(tap_args); ++launches;
         ev1(4, stream);
     }
-    if (snap_args.kinds) {
-        dim3 sg((snap_args.nxs + 127) / 128, snap_args.nys);
-        k_snap_xy<<<sg, 128, 0, stream>>>(snap_args); ++launches;
+    if (snap_args.n) {
+        dim3 sg((snap_args.maxpix + 127) / 128, snap_args.n);
+        k_snap<<<sg, 128, 0, stream>>>(snap_args); ++launches;
     }
     ZArgs z;
     fill_zargs(z);
@@ -421,8 +421,8 @@ int swpc_gpu_upload_medium(swpc_sim* sim, const float* rho, const float* lam, co
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s || !rho || !lam || !mu || !taup || !taus || !kob || !kfs_top || !kfs_bot || !kob_top || !kob_bot || !ts)
         return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium");
-    (void)kfs;
-    return s->upload_medium(rho, lam, mu, taup, taus, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts);
+    if (!kfs) return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium");
+    return s->upload_medium(rho, lam, mu, taup, taus, kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts);
 }
 
 int swpc_gpu_set_sources(swpc_sim* sim, int n, const int* ijk, const double* mo, const double* mij, const double* fxyz,
@@ -445,7 +445,45 @@ int swpc_gpu_set_snapshot(swpc_sim* sim, int kinds, int k0, int idec, int jdec, 
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s || (kinds & ~3) || idec <= 0 || jdec <= 0 || ntdec_s <= 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_snapshot");
     if (kinds && (k0 < 1 || k0 > s->dims.nz)) return set_err(SWPC_E_ARG, "snapshot plane k0 outside 1..nz");
-    return s->set_snapshot(kinds, k0, idec, jdec, ntdec_s);
+    int rc = 0;
+    if (kinds & SWPC_SNAP_XY_V) rc = s->add_snapshot(SWPC_SEC_XY, SWPC_SNAPK_V, k0, idec, jdec, ntdec_s);
+    if (!rc && (kinds & SWPC_SNAP_XY_U)) rc = s->add_snapshot(SWPC_SEC_XY, SWPC_SNAPK_U, k0, idec, jdec, ntdec_s);
+    return rc;
+}
+
+int swpc_gpu_add_snapshot(swpc_sim* sim, int section, int kind, int fix, int dec1, int dec2, int ntdec_s) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || section < SWPC_SEC_XY || section > SWPC_SEC_OB || kind < SWPC_SNAPK_V || kind > SWPC_SNAPK_PS ||
+        dec1 <= 0 || dec2 <= 0 || ntdec_s <= 0)
+        return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_add_snapshot");
+    const int lim = section == SWPC_SEC_XY ? s->dims.nz : section == SWPC_SEC_YZ ? s->dims.nx
+                  : section == SWPC_SEC_XZ ? s->dims.ny : 1;
+    if (section >= SWPC_SEC_FS) fix = 1;  // the surface maps choose k per column
+    if (fix < 1 || fix > lim) return set_err(SWPC_E_ARG, "snapshot section index outside the grid");
+    return s->add_snapshot(section, kind, fix, dec1, dec2, ntdec_s);
+}
+
+int swpc_gpu_query_snapshot(swpc_sim* sim, int section, int kind, int* n1, int* n2, int* nframes) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    const SnapPlane* P = s->find_plane(section, kind);
+    if (!P) return set_err(SWPC_E_STATE, "that snapshot was not requested");
+    if (n1) *n1 = P->n1;
+    if (n2) *n2 = P->n2;
+    if (nframes) *nframes = s->nframes_done();
+    return 0;
+}
+
+int swpc_gpu_fetch_section(swpc_sim* sim, int section, int kind, int frame, float* out) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !out) return set_err(SWPC_E_ARG, "null argument");
+    const SnapPlane* P = s->find_plane(section, kind);
+    if (!P) return set_err(SWPC_E_STATE, "that snapshot was not requested");
+    if (frame < 0 || frame >= s->snap_args.maxframes) return set_err(SWPC_E_ARG, "frame out of range");
+    const size_t n = (size_t)P->n1 * P->n2 * P->nc;
+    CK(cudaMemcpyAsync(out, P->frames + frame * n, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
 }
 
 int swpc_gpu_step(swpc_sim* sim, int it) { return swpc_gpu_run(sim, it, it); }
@@ -489,9 +527,11 @@ int swpc_gpu_query(swpc_sim* sim, int* ntw, int* nst, int* nxs, int* nys, int* n
     if (!s) return set_err(SWPC_E_ARG, "null simulation");
     if (ntw) *ntw = s->tap_args.ntw;
     if (nst) *nst = s->tap_args.n;
-    if (nxs) *nxs = s->snap_args.nxs;
-    if (nys) *nys = s->snap_args.nys;
-    if (nframes) *nframes = s->snap_args.kinds ? std::min(s->snap_args.maxframes, (s->it_done - 1) / std::max(1, s->snap_args.ntdec_s) + 1) : 0;
+    const SnapPlane* P = s->find_plane(SWPC_SEC_XY, SWPC_SNAPK_V);
+    if (!P) P = s->find_plane(SWPC_SEC_XY, SWPC_SNAPK_U);
+    if (nxs) *nxs = P ? P->n1 : 0;
+    if (nys) *nys = P ? P->n2 : 0;
+    if (nframes) *nframes = P ? s->nframes_done() : 0;
     return 0;
 }
 
@@ -517,13 +557,8 @@ int swpc_gpu_fetch_waveforms(swpc_sim* sim, int kind, float* out) {
 int swpc_gpu_fetch_snapshot(swpc_sim* sim, int kind, int frame, float* out) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s || !out) return set_err(SWPC_E_ARG, "null argument");
-    const SnapArgs& a = s->snap_args;
-    if (!(a.kinds & kind) || (kind != 1 && kind != 2)) return set_err(SWPC_E_STATE, "that snapshot kind was not requested");
-    if (frame < 0 || frame >= a.maxframes) return set_err(SWPC_E_ARG, "frame out of range");
-    const size_t pl = (size_t)a.nxs * a.nys * 3;
-    CK(cudaMemcpyAsync(out, (kind == 1 ? a.xy_v : a.xy_u) + frame * pl, pl * 4, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return 0;
+    if (kind != SWPC_SNAP_XY_V && kind != SWPC_SNAP_XY_U) return set_err(SWPC_E_ARG, "kind must be SWPC_SNAP_XY_V or _U");
+    return swpc_gpu_fetch_section(sim, SWPC_SEC_XY, kind == SWPC_SNAP_XY_V ? SWPC_SNAPK_V : SWPC_SNAPK_U, frame, out);
 }
 
 int swpc_gpu_vmax(swpc_sim* sim, float out[3]) {
@@ -545,13 +580,14 @@ int swpc_gpu_vmax(swpc_sim* sim, float out[3]) {
 
 int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out) {
     Sim* s = reinterpret_cast<Sim*>(sim);
-    if (!s || !out || which < 0 || which > 8) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_fetch_field");
+    if (!s || !out || which < 0 || which > 13) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_fetch_field");
     const Geo& g = s->p.g;
     size_t n = (size_t)g.nx * g.ny * g.nz;
     double* d = nullptr;
     CK(cudaMallocAsync(&d, n * 8, s->stream));
     if (which < 3) k_gather_d<<<1024, 256, 0, s->stream>>>(s->V, d, g, 3, which);
-    else k_gather_d<<<1024, 256, 0, s->stream>>>(s->S, d, g, 6, which - 3);
+    else if (which < 9) k_gather_d<<<1024, 256, 0, s->stream>>>(s->S, d, g, 6, which - 3);
+    else k_gather_d<<<1024, 256, 0, s->stream>>>(s->M, d, g, 5, which - 9);
     ++s->launches;
     CK(cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaFreeAsync(d, s->stream));
@@ -664,11 +700,11 @@ int swpc_gpu_reset(swpc_sim* sim) {
         if (t.acc) CK(cudaMemsetAsync(t.acc, 0, (size_t)9 * t.n * 8, s->stream));
     }
     const SnapArgs& a = s->snap_args;
-    if (a.kinds) {
-        const size_t fr = (size_t)a.maxframes * 3 * a.nxs * a.nys * 4;
-        if (a.xy_v) CK(cudaMemsetAsync(a.xy_v, 0, fr, s->stream));
-        if (a.xy_u) CK(cudaMemsetAsync(a.xy_u, 0, fr, s->stream));
-        if (a.uacc) CK(cudaMemsetAsync(a.uacc, 0, (size_t)3 * a.nxs * a.nys * 8, s->stream));
+    for (int q = 0; q < a.n; ++q) {
+        const SnapPlane& P = a.pl[q];
+        const size_t pix = (size_t)P.n1 * P.n2;
+        CK(cudaMemsetAsync(P.frames, 0, (size_t)a.maxframes * P.nc * pix * 4, s->stream));
+        if (P.uacc) CK(cudaMemsetAsync(P.uacc, 0, 3 * pix * 8, s->stream));
     }
     if (s->vmax_args.rep) CK(cudaMemsetAsync(s->vmax_args.rep, 0, (size_t)s->vmax_args.nrep * 12, s->stream));
     CK(cudaMemsetAsync(s->d_err, 0, 4, s->stream));
@@ -747,6 +783,7 @@ int Sim::allocate() {
     }
     if ((rc = dalloc((void**)&d_it, 16))) return rc;
     if ((rc = dalloc((void**)&d_kob, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
+    if ((rc = dalloc((void**)&d_kfs, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     // z chunking: enough blocks to fill the GPU at least ~4 times
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
@@ -771,8 +808,8 @@ int Sim::allocate() {
 }
 
 int Sim::upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
-                       const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top, const int* kob_bot,
-                       const double* ts) {
+                       const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
+                       const int* kob_bot, const double* ts) {
     const Geo& g = p.g;
     const size_t n3 = (size_t)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
     float* stage = nullptr;
@@ -795,11 +832,17 @@ int Sim::upload_medium(const float* rho, const float* lam, const float* mu, cons
             bnd[q] = at(kfs_top, i, j); bnd[q + 1] = at(kfs_bot, i, j);
             bnd[q + 2] = at(kob_top, i, j); bnd[q + 3] = at(kob_bot, i, j);
         }
-    std::vector<int> kb((size_t)g.nx * g.ny);
+    // per-column kob and kfs (1-based, clamped to 0..nz-1 so that k+1 is a
+    // valid 0-based plane index plus one)
+    std::vector<int> kb((size_t)g.nx * g.ny), kf((size_t)g.nx * g.ny);
     for (int j = 0; j < g.ny; ++j)
-        for (int i = 0; i < g.nx; ++i) kb[(size_t)j * g.nx + i] = std::max(0, std::min(g.nz - 1, at(kob, i + 1, j + 1)));
+        for (int i = 0; i < g.nx; ++i) {
+            kb[(size_t)j * g.nx + i] = std::max(0, std::min(g.nz - 1, at(kob, i + 1, j + 1)));
+            kf[(size_t)j * g.nx + i] = std::max(0, std::min(g.nz - 1, at(kfs, i + 1, j + 1)));
+        }
     CK(cudaMemcpyAsync(band, bnd.data(), bnd.size() * 4, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_kob, kb.data(), kb.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d_kfs, kf.data(), kf.size() * 4, cudaMemcpyHostToDevice, stream));
 
     // FD and Zener coefficients in FP64 (m_kernel.f90:43-67)
     const double dt = dims.dt, dx = dims.dx, dy = dims.dy, dz = dims.dz;
@@ -962,28 +1005,63 @@ int Sim::set_receivers(int n, const int* ijk, int ntdec_w, int flags) {
     return 0;
 }
 
-int Sim::set_snapshot(int kinds, int k0, int idec, int jdec, int ntdec_s) {
+// Snapshot planes (snap__setup, m_snap.f90:95-207): every plane shares the
+// frame interval ntdec_s; adding a plane of the same section and kind again
+// replaces its geometry.
+int Sim::add_snapshot(int sec, int kind, int fix, int d1, int d2, int ntdec_s) {
     SnapArgs& a = snap_args;
-    a.g = p.g; a.V = V; a.it = d_it;
-    a.kinds = kinds;
-    if (!kinds) return 0;
-    a.kz0 = k0 - 1; a.idec = idec; a.jdec = jdec; a.ntdec_s = ntdec_s;
-    a.nxs = (p.g.nx + idec / 2) / idec;
-    a.nys = (p.g.ny + jdec / 2) / jdec;
+    if (a.n > 0 && ntdec_s != a.ntdec_s) return set_err(SWPC_E_ARG, "all snapshots share one ntdec_s");
+    const Geo& g = p.g;
+    a.g = g; a.V = V; a.S = S; a.M = M; a.kfs = d_kfs; a.kob = d_kob; a.it = d_it;
+    a.ntdec_s = ntdec_s;
     a.maxframes = (dims.nt - 1) / ntdec_s + 1;
-    a.vscale = (float)(dims.UC * dims.M0);
-    a.dt = (float)dims.dt;
-    const size_t fr = (size_t)a.maxframes * 3 * a.nxs * a.nys;
-    int rc;
-    a.xy_v = a.xy_u = nullptr; a.uacc = nullptr;
-    if ((kinds & 1) && (rc = dalloc((void**)&a.xy_v, fr * 4))) return rc;
-    if (kinds & 2) {
-        if ((rc = dalloc((void**)&a.xy_u, fr * 4))) return rc;
-        if ((rc = dalloc((void**)&a.uacc, (size_t)3 * a.nxs * a.nys * 8))) return rc;
+    a.UC = (float)dims.UC; a.M0 = (float)dims.M0; a.dt = (float)dims.dt;
+    a.r20x = (float)(1.0 / dims.dx); a.r20y = (float)(1.0 / dims.dy); a.r20z = (float)(1.0 / dims.dz);
+    int q = 0;
+    while (q < a.n && !(a.pl[q].sec == sec && a.pl[q].kind == kind)) ++q;
+    if (q == MAX_SNAP) return set_err(SWPC_E_ARG, "too many snapshot planes");
+    SnapPlane P{};
+    P.sec = sec; P.kind = kind; P.d1 = d1; P.d2 = d2; P.nc = kind == SNAP_PS ? 4 : 3;
+    const int nxs = (g.nx + d1 / 2) / d1;
+    switch (sec) {  // nxs, nys, nzs of m_snap.f90:131-133
+    case SEC_YZ: P.n1 = (g.ny + d1 / 2) / d1; P.n2 = (g.nz + d2 / 2) / d2; P.fix = fix - 1; break;
+    case SEC_XZ: P.n1 = nxs; P.n2 = (g.nz + d2 / 2) / d2; P.fix = fix - 1; break;
+    default: P.n1 = nxs; P.n2 = (g.ny + d2 / 2) / d2; P.fix = fix - 1; break;
     }
+    const size_t pix = (size_t)P.n1 * P.n2;
+    const bool same = q < a.n && a.pl[q].n1 == P.n1 && a.pl[q].n2 == P.n2;
+    if (same) {
+        P.frames = a.pl[q].frames;
+        P.uacc = a.pl[q].uacc;
+    } else {
+        int rc;
+        if ((rc = dalloc((void**)&P.frames, (size_t)a.maxframes * P.nc * pix * 4))) return rc;
+        if (kind == SNAP_U && (rc = dalloc((void**)&P.uacc, 3 * pix * 8))) return rc;
+    }
+    if (kind == SNAP_U && !P.uacc) {
+        int rc = dalloc((void**)&P.uacc, 3 * pix * 8);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(P.frames, 0, (size_t)a.maxframes * P.nc * pix * 4, stream));
+    if (P.uacc) CK(cudaMemsetAsync(P.uacc, 0, 3 * pix * 8, stream));
+    a.pl[q] = P;
+    if (q == a.n) ++a.n;
+    a.maxpix = 0;
+    for (int r = 0; r < a.n; ++r) a.maxpix = std::max(a.maxpix, a.pl[r].n1 * a.pl[r].n2);
     CK(cudaStreamSynchronize(stream));
     if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
     return 0;
+}
+
+const SnapPlane* Sim::find_plane(int sec, int kind) const {
+    for (int q = 0; q < snap_args.n; ++q)
+        if (snap_args.pl[q].sec == sec && snap_args.pl[q].kind == kind) return &snap_args.pl[q];
+    return nullptr;
+}
+
+int Sim::nframes_done() const {
+    if (!snap_args.n || it_done < 1) return 0;
+    return std::min(snap_args.maxframes, (it_done - 1) / std::max(1, snap_args.ntdec_s) + 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1010,7 +1088,7 @@ struct Batch {
     int** d_its = nullptr;
     int4* d_tblocks = nullptr;
     int2* d_pblocks = nullptr;
-    int n_tblocks = 0, n_pblocks = 0, max_nst = 0, max_src = 0, max_nxs = 0, max_nys = 0;
+    int n_tblocks = 0, n_pblocks = 0, max_nst = 0, max_src = 0, max_pix = 0, max_planes = 0;
     bool any_vmax = false, any_snap = false, any_bf = false, any_mt = false;
     size_t smem_stress = 0, smem_vel = 0;
     long long launches = 0, launches_per_graph = 0;
@@ -1036,7 +1114,7 @@ struct Batch {
         const int n = (int)sims.size();
         if (any_vmax) { k_vmax_batch<<<dim3(64, n), 256, 0, stream>>>(d_vmax); ++launches; }
         if (max_nst) { k_taps_batch<<<dim3((max_nst + 127) / 128, n), 128, 0, stream>>>(d_tap); ++launches; }
-        if (any_snap) { k_snap_xy_batch<<<dim3((max_nxs + 127) / 128, max_nys, n), 128, 0, stream>>>(d_snap); ++launches; }
+        if (any_snap) { k_snap_batch<<<dim3((max_pix + 127) / 128, max_planes, n), 128, 0, stream>>>(d_snap); ++launches; }
         const dim3 tblk(32, TTY);
         if (n_pblocks) {
             cudaEventRecord(ev[0], stream);
@@ -1136,10 +1214,10 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         b->max_src = std::max(b->max_src, s->src_args.n);
         if (s->src_args.n > 0) { if (s->bf_mode) b->any_bf = true; else b->any_mt = true; }
         if (s->vmax_args.ntdec_r > 0) b->any_vmax = true;
-        if (s->snap_args.kinds) {
+        if (s->snap_args.n) {
             b->any_snap = true;
-            b->max_nxs = std::max(b->max_nxs, s->snap_args.nxs);
-            b->max_nys = std::max(b->max_nys, s->snap_args.nys);
+            b->max_pix = std::max(b->max_pix, s->snap_args.maxpix);
+            b->max_planes = std::max(b->max_planes, s->snap_args.n);
         }
     }
     int rc;

@@ -16,9 +16,12 @@ from . import build as _build
 
 SWPC_WAV_V, SWPC_WAV_U, SWPC_WAV_STRESS, SWPC_WAV_STRAIN = 1, 2, 4, 8
 SWPC_SNAP_XY_V, SWPC_SNAP_XY_U = 1, 2
+SEC_XY, SEC_YZ, SEC_XZ, SEC_FS, SEC_OB = range(5)
+SNAPK_V, SNAPK_U, SNAPK_PS = range(3)
 STORE = {"fp32": 0, "fp16": 1, "bf16": 2}
 STF = {"boxcar": 0, "triangle": 1, "herrmann": 2, "kupper": 3, "cosine": 4, "scosine": 4, "texp": 5}
 FIELDS = ["Vx", "Vy", "Vz", "Sxx", "Syy", "Szz", "Syz", "Sxz", "Sxy"]
+MEDIUM_FIELDS = ["rho", "lam", "mu", "taup", "taus"]  # fetch_field codes 9..13
 STATIC_FIELD_MAX = 4 * 1024 * 1024  # SWPC_STATIC_FIELD_MAX of include/swpc_gpu.h
 
 
@@ -50,6 +53,7 @@ EXPORTS = [
     "swpc_host_check", "swpc_gpu_fetch_field_static", "swpc_gpu_reset", "swpc_gpu_get_dims", "swpc_gpu_set_zchunk",
     "swpc_gpu_get_zchunk", "swpc_batch_create", "swpc_batch_run", "swpc_batch_sync", "swpc_batch_stream",
     "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes", "swpc_gpu_selftest_wait",
+    "swpc_gpu_add_snapshot", "swpc_gpu_query_snapshot", "swpc_gpu_fetch_section",
     "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
@@ -120,6 +124,9 @@ def lib(build=True):
     L.swpc_batch_launch_count.restype = ctypes.c_longlong
     L.swpc_batch_destroy.argtypes = [vp]
     L.swpc_gpu_selftest_wait.argtypes = [dp]
+    L.swpc_gpu_add_snapshot.argtypes = [vp, i, i, i, i, i, i]
+    L.swpc_gpu_query_snapshot.argtypes = [vp, i, i, ip, ip, ip]
+    L.swpc_gpu_fetch_section.argtypes = [vp, i, i, i, fp]
     L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_request_bytes.argtypes = [vp]
     L.swpc_host_request_bytes.restype = ctypes.c_longlong
@@ -273,6 +280,22 @@ class Simulation:
         _ck(lib().swpc_gpu_fetch_waveforms(self._h, int(kind), out.ctypes.data))
         return out
 
+    def add_snapshot(self, section, kind, fix=1, dec1=1, dec2=1, ntdec_s=10):
+        _ck(lib().swpc_gpu_add_snapshot(self._h, int(section), int(kind), int(fix), int(dec1), int(dec2), int(ntdec_s)))
+
+    def query_section(self, section, kind):
+        v = np.zeros(3, np.int32)
+        _ck(lib().swpc_gpu_query_snapshot(self._h, int(section), int(kind), *[v[q:].ctypes.data for q in range(3)]))
+        return dict(n1=int(v[0]), n2=int(v[1]), nframes=int(v[2]))
+
+    def section(self, section, kind, frame):
+        """Frame `frame` of a snapshot: (nc, n2, n1) float32."""
+        q = self.query_section(section, kind)
+        nc = 4 if kind == SNAPK_PS else 3
+        out = np.zeros((nc, q["n2"], q["n1"]), np.float32)
+        _ck(lib().swpc_gpu_fetch_section(self._h, int(section), int(kind), int(frame), out.ctypes.data))
+        return out
+
     def snapshot(self, kind, frame):
         q = self.query()
         out = np.zeros((3, q["nys"], q["nxs"]), np.float32)
@@ -284,7 +307,8 @@ class Simulation:
         if d is None:
             raise SwpcError(-1, "field() needs the dims the simulation was created with")
         out = np.zeros((d.ny, d.nx, d.nz), np.float64)
-        _ck(lib().swpc_gpu_fetch_field(self._h, FIELDS.index(name), out.ctypes.data))
+        code = FIELDS.index(name) if name in FIELDS else 9 + MEDIUM_FIELDS.index(name)
+        _ck(lib().swpc_gpu_fetch_field(self._h, code, out.ctypes.data))
         return out
 
     def field_static(self, name):

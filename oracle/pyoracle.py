@@ -66,6 +66,8 @@ def lib():
         L.oracle_medium.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
         L.oracle_vmax.argtypes = [vp, ctypes.c_void_p]
         L.oracle_snap_xy_v.argtypes = [vp, ctypes.c_void_p]
+        L.oracle_snap.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_snap.restype = ctypes.c_longlong
         L.oracle_destroy.argtypes = [vp]
         L.oracle_sources.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_stf.argtypes = [vp]
@@ -141,6 +143,17 @@ class Oracle:
         out = np.zeros((self.nvmax, 4), np.float32)
         self._L.oracle_vmax(self.h, out.ctypes.data)
         return out
+
+    def snap(self, section, kind, n1, n2):
+        """Stacked frames of one snapshot: (nframes, nc, n2, n1) float32
+        (section 0 xy, 1 yz, 2 xz, 3 fs, 4 ob; kind 0 v, 1 u, 2 ps)."""
+        n = self._L.oracle_snap(self.h, int(section), int(kind), None)
+        if n < 0:
+            raise RuntimeError("snapshot not requested")
+        out = np.zeros(n, np.float32)
+        self._L.oracle_snap(self.h, int(section), int(kind), out.ctypes.data)
+        nc = 4 if kind == 2 else 3
+        return out.reshape(-1, nc, n2, n1)
 
     def snap_xy_v(self):
         out = np.zeros(self.nsnap, np.float32)

@@ -218,9 +218,10 @@ static std::vector<std::string> tokens(const std::string& s) {
 // ---------------------------------------------------------------------------
 struct Params {
     std::string title, odir, abc_type, vmodel_type, fn_lhm, stftype, stf_format, fn_stf, sdep_fit, st_format, fn_stloc;
-    int nx, ny, nz, nt, na, ntdec_w, ntdec_r, ntdec_s, idec, jdec;
+    int nx, ny, nz, nt, na, ntdec_w, ntdec_r, ntdec_s, idec, jdec, kdec;
     double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut;
-    double vp0, vs0, rho0, qp0, qs0, topo0, z0_xy;
+    double vp0, vs0, rho0, qp0, qs0, topo0, z0_xy, x0_yz, y0_xz;
+    int snap_sw[5];  // sections xy yz xz fs ob; bits: 1 v, 2 u, 4 ps
     bool bf_mode, pw_mode, green_mode, sw_wav_v, sw_wav_u, sw_wav_stress, sw_wav_strain, munk, xy_v, xy_u;
 };
 
@@ -265,10 +266,23 @@ static Params read_params(const Ini& ini) {
     p.st_format = ini.str("st_format", "xy");
     p.fn_stloc = ini.str("fn_stloc", "");
     p.ntdec_r = ini.integer("ntdec_r", 100);
-    p.xy_v = ini.logical("xy_v%sw", false); p.xy_u = ini.logical("xy_u%sw", false);
+    // src/swpc_3d/m_snap.f90:105-127
+    {
+        const char* secs[5] = {"xy", "yz", "xz", "fs", "ob"};
+        const char* kinds[3] = {"v", "u", "ps"};
+        for (int q = 0; q < 5; ++q) {
+            p.snap_sw[q] = 0;
+            for (int c = 0; c < 3; ++c)
+                if (ini.logical(std::string(secs[q]) + "_" + kinds[c] + "%sw", false)) p.snap_sw[q] |= 1 << c;
+        }
+    }
+    p.xy_v = p.snap_sw[0] & 1; p.xy_u = (p.snap_sw[0] & 2) != 0;
     float zend = (float)p.zbeg + p.nz * (float)p.dz;
+    float xend = (float)p.xbeg + p.nx * (float)p.dx, yend = (float)p.ybeg + p.ny * (float)p.dy;
     p.z0_xy = ini.real("z0_xy", std::max(std::min(10.0f, zend), (float)p.zbeg));
-    p.idec = ini.integer("idec", 1); p.jdec = ini.integer("jdec", 1);
+    p.x0_yz = ini.real("x0_yz", std::max(std::min(0.0f, xend), (float)p.xbeg));
+    p.y0_xz = ini.real("y0_xz", std::max(std::min(0.0f, yend), (float)p.ybeg));
+    p.idec = ini.integer("idec", 1); p.jdec = ini.integer("jdec", 1); p.kdec = ini.integer("kdec", 1);
     p.ntdec_s = ini.integer("ntdec_s", 10);
     return p;
 }
@@ -291,7 +305,15 @@ struct SimBase {
     int nst = 0, ntw = 0;
     std::vector<float> wav_vel, wav_disp, wav_stress, wav_strain;  // (ntw, ncmp, nst) Fortran order
     std::vector<float> vmax_log;  // (it, vx, vy, vz) every ntdec_r
-    std::vector<float> snap_xy_v;  // stacked frames of (nxs, nys, 3)
+    // snapshot planes: section (0 xy, 1 yz, 2 xz, 3 fs, 4 ob), kind (0 v,
+    // 1 u, 2 ps), pixel grid and decimation, fixed index; frames stacked as
+    // (nc, n2, n1) each
+    struct OSnap {
+        int sec, kind, n1, n2, d1, d2, fix;
+        std::vector<double> ubuf;   // running displacement (u), FP32 values as the reference sums them
+        std::vector<float> frames;
+    };
+    std::vector<OSnap> snaps;
     float M0 = 0, UC = 1e-15f, fcut = 0;
     int nxs = 0, nys = 0, k0_xy = 0;
     std::vector<Sta> sta;
@@ -327,7 +349,6 @@ struct Sim : SimBase {
     // receivers
     std::vector<SP> ux, uy, uz, exx, eyy, ezz, eyz, exz, exy;
     MP r40x, r40y, r40z, r41x, r41y, r41z;
-    std::vector<SP> buf_xy_u;
 
     SP& gx(std::vector<SP>& g, int l, int i, int b) { return g[4 * (i - b) + (l - 1)]; }
 
@@ -779,12 +800,24 @@ struct Sim : SimBase {
         r41x = MP(1.0) / MP(24.0) / dx; r41y = MP(1.0) / MP(24.0) / dy; r41z = MP(1.0) / MP(24.0) / dz;
     }
 
-    // src/swpc_3d/m_snap.f90:95-160 (xy section only)
+    // src/swpc_3d/m_snap.f90:95-207
     void snap_setup() {
         nxs = (nx + p.idec / 2) / p.idec;
         nys = (ny + p.jdec / 2) / p.jdec;
+        const int nzs = (nz + p.kdec / 2) / p.kdec;
         k0_xy = x2i((SP)p.z0_xy, zbeg, (SP)dz);
-        if (p.xy_u) buf_xy_u.assign((size_t)nxs * nys * 3, 0);
+        const int i0 = x2i((SP)p.x0_yz, xbeg, (SP)dx), j0 = x2i((SP)p.y0_xz, ybeg, (SP)dy);
+        for (int sec = 0; sec < 5; ++sec)
+            for (int kind = 0; kind < 3; ++kind) {
+                if (!(p.snap_sw[sec] >> kind & 1)) continue;
+                OSnap o;
+                o.sec = sec; o.kind = kind;
+                if (sec == 1) { o.n1 = nys; o.n2 = nzs; o.d1 = p.jdec; o.d2 = p.kdec; o.fix = i0; }
+                else if (sec == 2) { o.n1 = nxs; o.n2 = nzs; o.d1 = p.idec; o.d2 = p.kdec; o.fix = j0; }
+                else { o.n1 = nxs; o.n2 = nys; o.d1 = p.idec; o.d2 = p.jdec; o.fix = k0_xy; }
+                if (kind == 1) o.ubuf.assign((size_t)3 * o.n1 * o.n2, 0.0);
+                snaps.push_back(std::move(o));
+            }
     }
 
     // ------------------------------------------------------------------
@@ -1162,31 +1195,71 @@ struct Sim : SimBase {
         exy[n] = exy[n] + (SP)(dxVy + dyVx) / (SP)2.0 * dt;
     }
 
-    // src/swpc_3d/m_snap.f90:1587-1653 (xy_v), 1963-2025 (xy_u), native buffer only
+    // wbuf_{xy,yz,xz,fs,ob}_{v,u,ps} (src/swpc_3d/m_snap.f90:981-2205),
+    // native buffers only.  v: V * UC * M0 at frame steps; u: V * UC * M0 * dt
+    // summed every step; ps: the
+    // divergence and rotation of V with the lam and |S| masks, * UC * M0 * 1e-3.
+    // The u sums are rounded to single precision after every step, as the
+    // reference's real buffers are.
     void snap_write(int it) {
-        if (!p.xy_v && !p.xy_u) return;
-        SP UCs = (SP)UC, M0s = (SP)M0;
-        if (p.xy_u)
-            for (int jj = 1; jj <= nys; ++jj)
-                for (int ii = 1; ii <= nxs; ++ii) {
-                    int i = ii * p.idec - p.idec / 2, j = jj * p.jdec - p.jdec / 2, k = k0_xy;
-                    SP* b = &buf_xy_u[(size_t)(jj - 1) * nxs + (ii - 1)];
-                    size_t pl = (size_t)nxs * nys;
-                    b[0] = b[0] + (SP)(Vx(k, i, j) * (MP)UCs * (MP)M0s * (MP)dt);
-                    b[pl] = b[pl] + (SP)(Vy(k, i, j) * (MP)UCs * (MP)M0s * (MP)dt);
-                    b[2 * pl] = b[2 * pl] + (SP)(Vz(k, i, j) * (MP)UCs * (MP)M0s * (MP)dt);
-                }
-        if ((it - 1) % p.ntdec_s != 0) return;
-        if (p.xy_v) {
-            size_t base = snap_xy_v.size(), pl = (size_t)nxs * nys;
-            snap_xy_v.resize(base + 3 * pl);
-            for (int jj = 1; jj <= nys; ++jj)
-                for (int ii = 1; ii <= nxs; ++ii) {
-                    int i = ii * p.idec - p.idec / 2, j = jj * p.jdec - p.jdec / 2, k = k0_xy;
-                    size_t q = base + (size_t)(jj - 1) * nxs + (ii - 1);
-                    snap_xy_v[q] = (float)(Vx(k, i, j) * (MP)UCs * (MP)M0s);
-                    snap_xy_v[q + pl] = (float)(Vy(k, i, j) * (MP)UCs * (MP)M0s);
-                    snap_xy_v[q + 2 * pl] = (float)(Vz(k, i, j) * (MP)UCs * (MP)M0s);
+        if (snaps.empty()) return;
+        const SP UCs = (SP)UC, M0s = (SP)M0;
+        const bool frame = (it - 1) % p.ntdec_s == 0;
+        const SP eps = std::numeric_limits<float>::epsilon();
+        for (auto& o : snaps) {
+            if (o.kind != 1 && !frame) continue;
+            const size_t pl = (size_t)o.n1 * o.n2, nc = o.kind == 2 ? 4 : 3;
+            size_t base = 0;
+            if (frame) {
+                base = o.frames.size();
+                o.frames.resize(base + nc * pl);
+            }
+            for (int b = 1; b <= o.n2; ++b)
+                for (int a = 1; a <= o.n1; ++a) {
+                    const int ca = a * o.d1 - o.d1 / 2, cb = b * o.d2 - o.d2 / 2;
+                    int i, j, k;
+                    if (o.sec == 1) { i = o.fix; j = ca; k = cb; }
+                    else if (o.sec == 2) { i = ca; j = o.fix; k = cb; }
+                    else {
+                        i = ca; j = cb;
+                        k = o.sec == 0 ? o.fix : (o.sec == 3 ? kfs(i, j) : kob(i, j)) + 1;
+                    }
+                    const size_t q = (size_t)(b - 1) * o.n1 + (a - 1);
+                    if (o.kind == 0) {
+                        o.frames[base + q] = (float)(Vx(k, i, j) * (MP)UCs * (MP)M0s);
+                        o.frames[base + pl + q] = (float)(Vy(k, i, j) * (MP)UCs * (MP)M0s);
+                        o.frames[base + 2 * pl + q] = (float)(Vz(k, i, j) * (MP)UCs * (MP)M0s);
+                    } else if (o.kind == 1) {
+                        const MP v3[3] = {Vx(k, i, j), Vy(k, i, j), Vz(k, i, j)};
+                        for (int c = 0; c < 3; ++c) {
+                            const float u = (float)o.ubuf[c * pl + q] + (float)(v3[c] * (MP)UCs * (MP)M0s * (MP)dt);
+                            o.ubuf[c * pl + q] = u;
+                            if (frame) o.frames[base + c * pl + q] = u;
+                        }
+                    } else {
+                        SP div = (SP)((Vx(k, i, j) - Vx(k, i - 1, j)) * r20x + (Vy(k, i, j) - Vy(k, i, j - 1)) * r20y +
+                                      (Vz(k, i, j) - Vz(k - 1, i, j)) * r20z);
+                        SP rx = (SP)((Vz(k, i, j + 1) - Vz(k, i, j)) * r20y - (Vy(k + 1, i, j) - Vy(k, i, j)) * r20z);
+                        SP ry = (SP)((Vx(k + 1, i, j) - Vx(k, i, j)) * r20z - (Vz(k, i + 1, j) - Vz(k, i, j)) * r20x);
+                        SP rz = (SP)((Vy(k, i + 1, j) - Vy(k, i, j)) * r20x - (Vx(k, i, j + 1) - Vx(k, i, j)) * r20y);
+                        const SP l = lam(k, i, j);
+                        const SP syz = (SP)Syz(k, i, j), sxz = (SP)Sxz(k, i, j), sxy = (SP)Sxy(k, i, j);
+                        div = div * l / std::abs(l + eps);
+                        if (o.sec == 1) {  // m_snap.f90:1027-1030
+                            rx = rx * std::abs(syz) / std::abs(syz + eps);
+                            ry = ry * std::abs(sxz) / std::abs(sxz + eps);
+                            rz = rz * std::abs(sxy) / std::abs(sxy + eps);
+                        } else {
+                            rx = rx * std::abs(syz) / (std::abs(syz) + eps);
+                            ry = ry * std::abs(sxz) / (std::abs(sxz) + eps);
+                            rz = rz * std::abs(sxy) / (std::abs(sxy) + eps);
+                        }
+                        const SP f = (SP)1e-3;
+                        o.frames[base + q] = (float)(div * UCs * M0s * f);
+                        o.frames[base + pl + q] = (float)(rx * UCs * M0s * f);
+                        o.frames[base + 2 * pl + q] = (float)(ry * UCs * M0s * f);
+                        o.frames[base + 3 * pl + q] = (float)(rz * UCs * M0s * f);
+                    }
                 }
         }
     }
@@ -1300,7 +1373,9 @@ void oracle_info(void* h, int* ints, double* reals) {
     ints[0] = s->p.nx; ints[1] = s->p.ny; ints[2] = s->p.nz; ints[3] = s->p.nt; ints[4] = s->p.na;
     ints[5] = s->nst; ints[6] = s->ntw; ints[7] = s->nt_done; ints[8] = s->nxs; ints[9] = s->nys; ints[10] = s->k0_xy;
     ints[11] = (int)(s->vmax_log.size() / 4);
-    ints[12] = (int)(s->snap_xy_v.size());
+    ints[12] = 0;
+    for (auto& o : s->snaps)
+        if (o.sec == 0 && o.kind == 0) ints[12] = (int)o.frames.size();
     reals[0] = s->M0; reals[1] = s->UC; reals[2] = s->fcut;
     reals[3] = s->p.dx; reals[4] = s->p.dy; reals[5] = s->p.dz; reals[6] = s->p.dt;
     reals[7] = s->p.xbeg; reals[8] = s->p.ybeg; reals[9] = s->p.zbeg; reals[10] = s->p.tbeg;
@@ -1328,7 +1403,22 @@ int oracle_medium(void* h, int which, float* out) {
     try { ((SimBase*)h)->get_medium(which, out); return 0; } catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
 void oracle_vmax(void* h, float* out) { SimBase* s = (SimBase*)h; std::copy(s->vmax_log.begin(), s->vmax_log.end(), out); }
-void oracle_snap_xy_v(void* h, float* out) { SimBase* s = (SimBase*)h; std::copy(s->snap_xy_v.begin(), s->snap_xy_v.end(), out); }
+void oracle_snap_xy_v(void* h, float* out) {
+    SimBase* s = (SimBase*)h;
+    for (auto& o : s->snaps)
+        if (o.sec == 0 && o.kind == 0) std::copy(o.frames.begin(), o.frames.end(), out);
+}
+// stacked frames of one snapshot (section, kind); returns the float count,
+// -1 when that snapshot was not requested; out may be null to query
+long long oracle_snap(void* h, int sec, int kind, float* out) {
+    SimBase* s = (SimBase*)h;
+    for (auto& o : s->snaps)
+        if (o.sec == sec && o.kind == kind) {
+            if (out) std::copy(o.frames.begin(), o.frames.end(), out);
+            return (long long)o.frames.size();
+        }
+    return -1;
+}
 
 void oracle_destroy(void* h) { delete (SimBase*)h; }
 
