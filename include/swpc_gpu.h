@@ -126,6 +126,17 @@ int swpc_gpu_add_snapshot(swpc_sim* sim, int section, int kind, int fix, int dec
 int swpc_gpu_query_snapshot(swpc_sim* sim, int section, int kind, int* n1, int* n2, int* nframes);
 int swpc_gpu_fetch_section(swpc_sim* sim, int section, int kind, int frame, float* out);
 
+/* Reciprocal Green's-function taps (green__store, m_green.f90:406-551): n
+ * grid points at 1-based ijk (3n); every ntdec_w steps the combinations
+ * dxUx, dyUy, dzUz, dyUz+dzUy, dxUz+dzUx, dxUy+dyUx of the time-integrated
+ * displacement gradients (scaled by 1e-15 * 1e9) and, with bforce, the
+ * displacement Ux, Uy, Uz (scaled by 1e-12 * 1e9).  The pseudo source is an
+ * ordinary body-force source (swpc_gpu_set_sources, bf_mode = 1). */
+int swpc_gpu_set_green(swpc_sim* sim, int n, const int* ijk, int ntdec_w, int bforce);
+/* Green's-function traces (ntw, ncmp, n) in Fortran order; with out null
+ * only *n, *ncmp and *ntw are set. */
+int swpc_gpu_fetch_green(swpc_sim* sim, float* out, int* n, int* ncmp, int* ntw);
+
 /* One time step it (main.f90:120-138 minus host I/O). */
 int swpc_gpu_step(swpc_sim* sim, int it);
 
@@ -273,6 +284,14 @@ int swpc_host_medium(int nx, int ny, int nz, int na, double fq_min, double fq_ma
 /* Write the receiver traces as SAC files named
  * odir/wav/<title>.3d.<station>.<cmp>.sac (m_wav.f90:782-792). */
 int swpc_host_write_sac(swpc_sim* sim, const char* odir);
+
+/* Green's-function mode (green_mode = .true.): write the traces of every
+ * point of fn_glst as SAC files odir/green/<stnm>/<title>__<id8>__<stnm>__
+ * <cmp>__<mxx..fz_>__.sac or as one CSF file (wav_format = 'csf'), with the
+ * headers of green__setup and the sign flip of a vertical force
+ * (green__export, m_green.f90:318-398, 553-612).  Does nothing outside that
+ * mode. */
+int swpc_host_write_green(swpc_sim* sim, const char* odir);
 
 /* Write the xy-section snapshots as the reference's native .snp files
  * odir/<title>.3d.xy.v.snp and .xy.u.snp: header version 6

@@ -140,6 +140,29 @@ def write_layered(d, nx, ny, nz, seed, nt=1500, dx=0.5, dt=0.02, n_station=8, bo
     return os.path.join(d, "input.inf")
 
 
+def write_green(d, nx=96, ny=96, nz=64, nt=200, cmp="z", bforce=True, n_points=24, seed=7, **over):
+    """Reciprocal Green's-function run (green_mode): a unit body force in
+    direction `cmp` at the free-surface station G01, strain (and, with
+    bforce, displacement) recorded at `n_points` seeded grid points of the
+    list file green.lst (x y z id)."""
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    keys = base_keys(nx=nx, ny=ny, nz=nz, nt=nt, xbeg=-nx * 0.25, ybeg=-ny * 0.25, green_mode=True,
+                     green_stnm="G01", green_cmp=cmp, green_trise=1.0, green_bforce=bforce, fn_glst="green.lst",
+                     green_fmt="xyz", sw_wav_v=False, ntdec_w=2, **over)
+    write_inf(os.path.join(d, "input.inf"), keys)
+    write_lhm(os.path.join(d, "lhm.dat"), [(0, 2.7, 5.5, 3.2, 200, 100), (4, 2.9, 6.5, 3.7, 600, 300)])
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        f.write("  1.000 -2.000 0.0 G01 fsb\n  5.000 5.000 0.0 G02 fsb\n")
+    with open(os.path.join(d, "green.lst"), "w") as f:
+        f.write("# x y z id\n")
+        for q in range(n_points):
+            x, y = rng.uniform(-8, 8, 2)
+            z = rng.uniform(1.0, 9.0)
+            f.write("  %.3f %.3f %.3f %d\n" % (x, y, z, 1000 + q))
+    return os.path.join(d, "input.inf")
+
+
 def write_uniform(d, nx=64, ny=64, nz=64, nt=100, dx=0.5, dt=0.02, vp=6.0, vs=3.5, rho=2.8, q=1e6,
                   source="0.0 0.0 0.0", stations=(("0.0", "0.0", "0.0", "C"),), bf=None, **over):
     """Uniform whole-space medium (no air layer), used by the analytic and

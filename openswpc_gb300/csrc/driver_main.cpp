@@ -42,6 +42,7 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "  time loop: %d steps in %.3f s (%.3f ms/step)\n", nt, s, 1e3 * s / nt);
     if (nst > 0 && swpc_host_write_sac(sim, odir.empty() ? nullptr : odir.c_str())) return fail("waveform output");
     if (swpc_host_write_snp(sim, odir.empty() ? nullptr : odir.c_str())) return fail("snapshot output");
+    if (swpc_host_write_green(sim, odir.empty() ? nullptr : odir.c_str())) return fail("Green's-function output");
     swpc_gpu_destroy(sim);
     return 0;
 }

@@ -220,6 +220,10 @@ struct Params {
     double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut, z0_xy, x0_yz, y0_xz;
     bool bf_mode, sw_v, sw_u, sw_stress, sw_strain, munk;
     int snap_sw[5];  // per section xy yz xz fs ob: bit SWPC_SNAPK_* set when <sec>_<kind>%sw is true
+    // Green's-function mode (m_green.f90:100-160)
+    bool green_mode = false, green_bforce = false;
+    std::string green_stnm, green_cmp, fn_glst, green_fmt;
+    double green_trise = 1.0, green_maxdist = 1e30;
 };
 
 struct Station { std::string name; double x, y, z, lon, lat; int i, j, k; };
@@ -242,6 +246,9 @@ struct Meta {  // what the SAC writer needs after set-up
     };
     std::vector<SnapSec> snaps;
     double bd0 = 0;
+    // Green's-function mode: the pseudo-source station and the output points
+    struct GPoint { double x = 0, y = 0, z = 0, lon = 0, lat = 0; long long gid = 0; int i = 0, j = 0, k = 0; };
+    struct Green { bool on = false; Station station; std::vector<GPoint> pts; } green;
 };
 std::mutex g_meta_mu;
 std::map<swpc_sim*, Meta> g_meta;
@@ -426,6 +433,64 @@ void medium_post(int nx, int ny, int nz, int na, double fq_min, double fq_max, d
         }
 }
 
+// stabilize_absorber (src/swpc_3d/m_medium.f90:273-337), single precision as
+// the reference: inside the absorber (k >= the smallest kbeg_a of the 5x5
+// neighbourhood) a thin low-velocity layer (at most 20 cells) gets the medium
+// of the cell above it at its top cell, and shear velocities below 0.4 of the
+// model's largest P velocity are raised to it with Vp = sqrt(3) Vs.
+void stabilize_absorber(int nx, int ny, int nz, int na, float* rho, float* lam, float* mu, float* taup, float* taus,
+                        const int* kfs) {
+    Grid G{nx, ny, nz};
+    const float eps = 1.1920928955078125e-07f;
+    float vmax = -1;  // velocity_minmax (m_medium.f90:396-427)
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+            for (int k = kfs[G.idx2(i, j)] + 1; k <= nz; ++k) {
+                const size_t c = G.idx(k, i, j);
+                vmax = std::max(vmax, std::sqrt((lam[c] + 2 * mu[c]) / rho[c]));
+            }
+    const float vmin_pml = vmax * 0.4f;
+    const int LV_THICK = 20;
+    auto kbeg_a = [&](int i, int j) { return (i <= na || nx - na + 1 <= i || j <= na || ny - na + 1 <= j) ? 1 : nz - na + 1; };
+    auto kmin = [&](int i, int j) {
+        int m = 1 << 30;
+        for (int jj = j - 2; jj <= j + 2; ++jj)
+            for (int ii = i - 2; ii <= i + 2; ++ii) m = std::min(m, kbeg_a(ii, jj));
+        return m;
+    };
+    for (int j = 0; j <= ny + 1; ++j)
+        for (int i = 0; i <= nx + 1; ++i) {
+            int k = kmin(i, j);
+            while (k <= nz) {
+                const size_t c = G.idx(k, i, j), u = G.idx(k - 1, i, j);
+                if (lam[c] < lam[u] || mu[c] < mu[u]) {
+                    int k2 = k + 1;
+                    for (; k2 <= nz; ++k2)
+                        if (lam[G.idx(k2, i, j)] > lam[G.idx(k2 - 1, i, j)] || mu[G.idx(k2, i, j)] > mu[G.idx(k2 - 1, i, j)]) break;
+                    if (k2 - k <= LV_THICK) {
+                        rho[c] = rho[u]; lam[c] = lam[u]; mu[c] = mu[u]; taup[c] = taup[u]; taus[c] = taus[u];
+                        k = k2 - 1;
+                    }
+                }
+                ++k;
+            }
+        }
+    const float gamma = std::sqrt(3.0f);
+    for (int j = 0; j <= ny + 1; ++j)
+        for (int i = 0; i <= nx + 1; ++i)
+            for (int k = kmin(i, j); k <= nz; ++k) {
+                const size_t c = G.idx(k, i, j);
+                float vs = std::sqrt(mu[c] / rho[c]);
+                if (vs < eps) continue;
+                if (vs < vmin_pml) {
+                    vs = vmin_pml;
+                    const float vp = vs * gamma;
+                    lam[c] = rho[c] * (vp * vp - 2 * vs * vs);
+                    mu[c] = rho[c] * (vs * vs);
+                }
+            }
+}
+
 // src/shared/m_fdtool.f90:307-336
 void sdr2moment(double strike, double dip, double rake, double* m6) {
     const double r = PI / 180;
@@ -459,62 +524,75 @@ void mkdirs(const std::string& d) {
     }
 }
 
-// SAC header + data as bytes (src/shared/m_sac.f90:267-449, header defaults
-// :452-562): 70 floats, 35 ints, 5 logicals, 192 characters, then the data.
+// SAC header (src/shared/m_sac.f90:267-449, defaults of sac__init :452-562):
+// 70 floats, 35 ints, 5 logicals and 192 characters, written before the data.
+struct SacHeader {
+    float f[70];
+    int i[35], l[5];
+    char k[192];
+    SacHeader() {
+        for (auto& v : f) v = -12345.0f;
+        for (auto& v : i) v = -12345;
+        for (auto& v : l) v = 0;
+        for (int q = 0; q < 24; ++q) std::memcpy(k + 8 * q, "-12345  ", 8);
+        kset(113, 16, "-12345");  // kevnm is 16 characters
+        i[6] = 6;   // nvhdr
+        i[15] = 1;  // iftype: time series
+        l[0] = 1;   // leven
+        l[2] = 1;   // lovrok
+    }
+    void kset(int word, int len, const std::string& v) {
+        std::string t = v.substr(0, len);
+        t.resize(len, ' ');
+        std::memcpy(k + 4 * (word - 111), t.data(), len);
+    }
+    void set_time(long long exedate) {  // nzyear .. nzmsec from the run's start time
+        time_t tt = (time_t)exedate;
+        struct tm lt;
+        localtime_r(&tt, &lt);
+        i[0] = lt.tm_year + 1900; i[1] = lt.tm_yday + 1; i[2] = lt.tm_hour; i[3] = lt.tm_min; i[4] = lt.tm_sec; i[5] = 0;
+    }
+    void set_delta(double delta) { f[0] = (float)((long long)(delta * 1e7)) / 1e7f; }
+    std::string bytes(const float* dat, int npts) {
+        i[9] = npts;
+        std::string out;
+        out.reserve(632 + (size_t)npts * 4);
+        out.append((const char*)f, sizeof f);
+        out.append((const char*)i, sizeof i);
+        out.append((const char*)l, sizeof l);
+        out.append(k, sizeof k);
+        out.append((const char*)dat, (size_t)npts * 4);
+        return out;
+    }
+};
+
+// Receiver trace as SAC bytes (headers of m_wav.f90:276-330)
 std::string sac_image(const Meta& m, const Station& st, const char* cmp, int idep, double cmpinc, double cmpaz,
                       const float* dat, int npts) {
-    float fh[70];
-    int ih[35], lh[5];
-    char kh[192];
-    for (auto& v : fh) v = -12345.0f;
-    for (auto& v : ih) v = -12345;
-    for (auto& v : lh) v = 0;
-    for (int q = 0; q < 24; ++q) std::memcpy(kh + 8 * q, "-12345  ", 8);
-    auto kset = [&](int word, int len, const std::string& s) {
-        std::string t = s.substr(0, len);
-        t.resize(len, ' ');
-        std::memcpy(kh + 4 * (word - 111), t.data(), len);
-    };
-    kset(113, 16, "-12345");  // kevnm is 16 characters
+    SacHeader h;
     const Params& p = m.p;
-    double delta = p.ntdec_w * p.dt;
-    fh[0] = (float)((long long)(delta * 1e7)) / 1e7f;
-    fh[5] = (float)p.tbeg;
-    fh[7] = (float)m.otim;
-    fh[31] = (float)st.lat; fh[32] = (float)st.lon; fh[34] = (float)(st.z * 1000);
-    fh[35] = (float)m.evla; fh[36] = (float)m.evlo; fh[38] = (float)m.evdp;
-    fh[39] = m.M0 < 1.1920928955078125e-07 ? -12345.0f : (float)((std::log10(m.M0) - 9.1) * 2.0 / 3.0);
-    if (p.bf_mode) { fh[40] = (float)m.f3[0]; fh[41] = (float)m.f3[1]; fh[42] = (float)m.f3[2]; }
+    h.set_delta(p.ntdec_w * p.dt);
+    h.f[5] = (float)p.tbeg;
+    h.f[7] = (float)m.otim;
+    h.f[31] = (float)st.lat; h.f[32] = (float)st.lon; h.f[34] = (float)(st.z * 1000);
+    h.f[35] = (float)m.evla; h.f[36] = (float)m.evlo; h.f[38] = (float)m.evdp;
+    h.f[39] = m.M0 < 1.1920928955078125e-07 ? -12345.0f : (float)((std::log10(m.M0) - 9.1) * 2.0 / 3.0);
+    if (p.bf_mode) { h.f[40] = (float)m.f3[0]; h.f[41] = (float)m.f3[1]; h.f[42] = (float)m.f3[2]; }
     else {
-        fh[40] = (float)m.m6[0]; fh[41] = (float)m.m6[1]; fh[42] = (float)m.m6[2];
-        fh[43] = (float)m.m6[3]; fh[44] = (float)m.m6[4]; fh[45] = (float)m.m6[5];
+        h.f[40] = (float)m.m6[0]; h.f[41] = (float)m.m6[1]; h.f[42] = (float)m.m6[2];
+        h.f[43] = (float)m.m6[3]; h.f[44] = (float)m.m6[4]; h.f[45] = (float)m.m6[5];
     }
-    fh[46] = (float)p.clon; fh[47] = (float)p.clat; fh[48] = (float)p.phi;
-    fh[50] = (float)std::sqrt((m.sx0 - st.x) * (m.sx0 - st.x) + (m.sy0 - st.y) * (m.sy0 - st.y));
-    fh[51] = (float)(std::atan2(st.y - m.sy0, st.x - m.sx0) * 180 / PI);
-    fh[52] = (float)(std::atan2(m.sy0 - st.y, m.sx0 - st.x) * 180 / PI);
-    fh[57] = (float)cmpaz; fh[58] = (float)cmpinc;
-    time_t tt = (time_t)m.exedate;
-    struct tm lt;
-    localtime_r(&tt, &lt);
-    ih[0] = lt.tm_year + 1900; ih[1] = lt.tm_yday + 1; ih[2] = lt.tm_hour; ih[3] = lt.tm_min; ih[4] = lt.tm_sec; ih[5] = 0;
-    ih[6] = 6;          // nvhdr
-    ih[9] = npts;       // npts
-    ih[15] = 1;         // iftype
-    ih[16] = idep;      // idep
-    lh[0] = 1;          // leven
-    lh[2] = 1;          // lovrok
-    kset(111, 8, st.name);
-    kset(113, 16, p.title.substr(0, 16));
-    kset(151, 8, cmp);
-    std::string out;
-    out.reserve(632 + (size_t)npts * 4);
-    out.append((const char*)fh, sizeof fh);
-    out.append((const char*)ih, sizeof ih);
-    out.append((const char*)lh, sizeof lh);
-    out.append(kh, sizeof kh);
-    out.append((const char*)dat, (size_t)npts * 4);
-    return out;
+    h.f[46] = (float)p.clon; h.f[47] = (float)p.clat; h.f[48] = (float)p.phi;
+    h.f[50] = (float)std::sqrt((m.sx0 - st.x) * (m.sx0 - st.x) + (m.sy0 - st.y) * (m.sy0 - st.y));
+    h.f[51] = (float)(std::atan2(st.y - m.sy0, st.x - m.sx0) * 180 / PI);
+    h.f[52] = (float)(std::atan2(m.sy0 - st.y, m.sx0 - st.x) * 180 / PI);
+    h.f[57] = (float)cmpaz; h.f[58] = (float)cmpinc;
+    h.set_time(m.exedate);
+    h.i[16] = idep;
+    h.kset(111, 8, st.name);
+    h.kset(113, 16, p.title.substr(0, 16));
+    h.kset(151, 8, cmp);
+    return h.bytes(dat, npts);
 }
 
 void write_file(const std::string& fn, const std::string& bytes) {
@@ -571,6 +649,8 @@ struct Prepared {
     std::vector<int> sijk, rijk;
     std::vector<double> smo, smij, sf3, sprm;
     int stf = 0, bf_mode = 0, flags = 0, ntdec_w = 1, ntdec_s = 10;
+    std::vector<int> gijk;  // Green's-function points, 1-based
+    bool green_bforce = false;
 };
 
 // Host half of the set-up (src/swpc_3d/main.f90:48-117 without the device):
@@ -595,8 +675,19 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     p.munk = inf.b("munk_profile", false);
     p.bf_mode = inf.b("bf_mode", false);
     if (inf.b("pw_mode", false)) throw std::runtime_error("pw_mode is not supported by this build");
-    if (inf.b("green_mode", false)) throw std::runtime_error("green_mode is not supported by this build");
-    if (inf.b("stabilize_pml", false)) throw std::runtime_error("stabilize_pml is not supported by this build");
+    p.green_mode = inf.b("green_mode", false);
+    if (p.green_mode) {
+        p.green_stnm = inf.s("green_stnm", ""); p.green_cmp = inf.s("green_cmp", "");
+        p.green_trise = inf.r("green_trise", 1.0); p.green_bforce = inf.b("green_bforce", false);
+        p.green_maxdist = inf.r("green_maxdist", 1e30); p.fn_glst = inf.s("fn_glst", "");
+        p.green_fmt = inf.s("green_fmt", "xyz");
+        if (!(p.green_maxdist > 0)) throw std::runtime_error("green_maxdist must be positive");
+        if (p.green_fmt != "xyz" && p.green_fmt != "llz") throw std::runtime_error("green_fmt must be xyz or llz");
+        if (p.green_cmp != "x" && p.green_cmp != "y" && p.green_cmp != "z") throw std::runtime_error("no matching green_cmp");
+        // m_wav.f90:76-82: no station recording in this mode
+        p.sw_v = p.sw_u = p.sw_stress = p.sw_strain = false;
+    }
+
     p.stftype = inf.s("stftype", "kupper"); p.stf_format = inf.s("stf_format", "xym0ij");
     p.fn_stf = inf.s("fn_stf", ""); p.sdep_fit = inf.s("sdep_fit", "asis");
     p.ntdec_w = inf.i("ntdec_w", 10); p.st_format = inf.s("st_format", "xy"); p.fn_stloc = inf.s("fn_stloc", "");
@@ -633,12 +724,15 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     double ts[3];
     medium_post(p.nx, p.ny, p.nz, p.na, p.fq_min, p.fq_max, p.fq_ref, rho.data(), lam.data(),
                 mu.data(), tp.data(), tsv.data(), kfs.data(), kob.data(), kft.data(), kfb.data(), kot.data(), kobb.data(), ts);
+    if (inf.b("stabilize_pml", false))  // m_medium.f90:218-222, after surface detection
+        stabilize_absorber(p.nx, p.ny, p.nz, p.na, rho.data(), lam.data(), mu.data(), tp.data(), tsv.data(), kfs.data());
 
     // sources (src/swpc_3d/m_source.f90:41-314, 468-774)
     Meta meta;
     meta.p = p;
     meta.exedate = (long long)std::time(nullptr);
-    auto rows = table_rows(inf.path(p.fn_stf));
+    // m_source.f90:84-91: no regular source grid in Green's-function mode
+    auto rows = p.green_mode ? std::vector<std::string>() : table_rows(inf.path(p.fn_stf));
     const std::string& f = p.stf_format;
     struct S0 { double x, y, z, t0, tr, mo, m6[6], f3[3]; };
     std::vector<S0> srcs;
@@ -692,11 +786,13 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
         }
         srcs.push_back(s);
     }
-    if (srcs.empty()) throw std::runtime_error("no source grid in " + p.fn_stf);
+    if (srcs.empty() && !p.green_mode) throw std::runtime_error("no source grid in " + p.fn_stf);
     double fcut = 0, M0 = 0;
     for (auto& s : srcs) fcut = std::max(fcut, 1.0 / s.tr);
     double UC = 1e-15;
-    if (p.bf_mode) {
+    if (p.green_mode) {
+        M0 = 1;  // m_green.f90:127; fcut stays 0, source__setup never sets it
+    } else if (p.bf_mode) {
         for (auto& s : srcs) M0 += s.f3[0] * s.f3[0] + s.f3[1] * s.f3[1] + s.f3[2] * s.f3[2];
         M0 = std::sqrt(M0);
         UC *= 1e3;
@@ -721,7 +817,8 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     // stations (src/swpc_3d/m_wav.f90:141-271)
     int flags = (p.sw_v ? SWPC_WAV_V : 0) | (p.sw_u ? SWPC_WAV_U : 0) | (p.sw_stress ? SWPC_WAV_STRESS : 0) |
                 (p.sw_strain ? SWPC_WAV_STRAIN : 0);
-    if (flags) {
+    std::vector<Station> all_st;
+    if (flags || p.green_mode) {
         std::vector<std::string> srows;
         try { srows = table_rows(inf.path(p.fn_stloc)); }
         catch (...) { std::fprintf(stderr, "swpc: no station location file found\n"); }
@@ -752,7 +849,50 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
             else if (zsw == "bd0") st.k = x2i(bd0, p.zbeg, p.dz);
             if (st.k > p.nz) st.k = p.nz - 1;
             if (st.k < 1) st.k = 2;
-            meta.st.push_back(st);
+            all_st.push_back(st);
+        }
+    }
+    if (flags) meta.st = all_st;
+
+    // Green's-function mode: the pseudo source at station green_stnm and
+    // the grid points of fn_glst (m_green.f90:145-404)
+    std::vector<int> gijk;
+    if (p.green_mode) {
+        const Station* gs = nullptr;
+        for (const auto& st : all_st)
+            if (st.name == p.green_stnm.substr(0, 8)) gs = &st;
+        if (!gs) throw std::runtime_error("green_stnm " + p.green_stnm + " is not a station inside the model");
+        Meta::Green& g = meta.green;
+        g.on = true;
+        g.station = *gs;
+        sijk.insert(sijk.end(), {gs->i, gs->j, gs->k});
+        smo.push_back(0.0);
+        smij.insert(smij.end(), 6, 0.0);
+        sf3.push_back(p.green_cmp == "x" ? 1.0 : 0.0);
+        sf3.push_back(p.green_cmp == "y" ? 1.0 : 0.0);
+        sf3.push_back(p.green_cmp == "z" ? 1.0 : 0.0);
+        sprm.insert(sprm.end(), {0.0, p.green_trise});
+        for (auto& r : table_rows(inf.path(p.fn_glst))) {
+            auto t = split(r);
+            if (t.size() < 4) throw std::runtime_error("bad Green's-function point: " + r);
+            Meta::GPoint q;
+            if (p.green_fmt == "xyz") {
+                q.x = Inf::num(t[0]); q.y = Inf::num(t[1]);
+                c2g(q.x, q.y, p.clon, p.clat, p.phi, q.lon, q.lat);
+            } else {
+                q.lon = Inf::num(t[0]); q.lat = Inf::num(t[1]);
+                g2c(q.lon, q.lat, p.clon, p.clat, p.phi, q.x, q.y);
+            }
+            q.z = Inf::num(t[2]);
+            q.gid = (long long)Inf::num(t[3]);
+            if (q.gid < 0 || q.gid > 99999999) throw std::runtime_error("Green's-function id outside 0..99999999");
+            const double dd = std::sqrt((q.x - gs->x) * (q.x - gs->x) + (q.y - gs->y) * (q.y - gs->y));
+            if (dd > p.green_maxdist) continue;
+            q.i = x2i(q.x, p.xbeg, p.dx); q.j = x2i(q.y, p.ybeg, p.dy); q.k = x2i(q.z, p.zbeg, p.dz);
+            if (!(1 <= q.i && q.i <= p.nx && 1 <= q.j && q.j <= p.ny)) continue;
+            if (!(kob[G.idx2(q.i, q.j)] <= q.k && q.k <= p.nz)) continue;  // the solid part only
+            g.pts.push_back(q);
+            gijk.insert(gijk.end(), {q.i, q.j, q.k});
         }
     }
 
@@ -790,7 +930,9 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     P.sijk = std::move(sijk); P.smo = std::move(smo); P.smij = std::move(smij); P.sf3 = std::move(sf3);
     P.sprm = std::move(sprm);
     P.stf = stf_code(p.stftype);
-    P.bf_mode = p.bf_mode;
+    P.bf_mode = p.bf_mode || p.green_mode;  // the Green's-function pseudo source is a body force
+    P.gijk = std::move(gijk);
+    P.green_bforce = p.green_bforce;
     P.rijk.clear();
     for (auto& st : meta.st) P.rijk.insert(P.rijk.end(), {st.i, st.j, st.k});
     P.flags = flags;
@@ -866,6 +1008,9 @@ int materialize(const Prepared& P, swpc_sim** out) {
                                    P.sprm.data(), P.stf, P.bf_mode)))
         return bail(rc);
     if ((rc = swpc_gpu_set_receivers(sim, (int)P.meta.st.size(), P.rijk.data(), P.ntdec_w, P.flags)))
+        return bail(rc);
+    if (!P.gijk.empty() &&
+        (rc = swpc_gpu_set_green(sim, (int)P.gijk.size() / 3, P.gijk.data(), P.ntdec_w, P.green_bforce ? 1 : 0)))
         return bail(rc);
     for (const auto& S : P.meta.snaps)
         for (int kind = 0; kind < 3; ++kind)
@@ -1041,6 +1186,80 @@ int swpc_host_write_snp(swpc_sim* sim, const char* odir) {
                 }
                 if (!f) throw std::runtime_error("short write to " + fn);
             }
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return swpc::set_err(SWPC_E_IO, e.what());
+    }
+}
+
+int swpc_host_write_green(swpc_sim* sim, const char* odir) {
+    Meta m;
+    {
+        std::lock_guard<std::mutex> lk(g_meta_mu);
+        auto it = g_meta.find(sim);
+        if (it == g_meta.end()) return swpc::set_err(SWPC_E_STATE, "simulation was not prepared by swpc_host_prepare");
+        m = it->second;
+    }
+    if (!m.green.on || m.green.pts.empty()) return 0;
+    try {
+        const Params& p = m.p;
+        const int ng = (int)m.green.pts.size();
+        int ncmp = 0, ntw = 0;
+        int rc = swpc_gpu_fetch_green(sim, nullptr, nullptr, &ncmp, &ntw);
+        if (rc) return rc;
+        std::vector<float> gf((size_t)ntw * ncmp * ng);
+        if ((rc = swpc_gpu_fetch_green(sim, gf.data(), nullptr, nullptr, nullptr))) return rc;
+        if (p.green_cmp == "z")  // m_green.f90:566-568: positive upward force
+            for (auto& v : gf) v = -v;
+        const Station& st = m.green.station;
+        const std::string dir = ((odir && *odir) ? std::string(odir) : p.odir) + "/green/" + st.name;
+        mkdirs(dir);
+        const char* cmp[9] = {"mxx", "myy", "mzz", "myz", "mxz", "mxy", "fx_", "fy_", "fz_"};
+        const std::string V = p.green_cmp == "x" ? "G_Vx_" : p.green_cmp == "y" ? "G_Vy_" : "G_Vz_";
+        const float inc = p.green_cmp == "z" ? 0.f : 90.f;
+        const float az = p.green_cmp == "x" ? (float)(0.0 + p.phi) : p.green_cmp == "y" ? (float)(90.0 + p.phi) : 0.f;
+        // SAC images of every point and component (m_green.f90:318-398)
+        auto image = [&](int n, int c) {
+            const Meta::GPoint& q = m.green.pts[n];
+            char cid8[16];
+            std::snprintf(cid8, sizeof cid8, "%08lld", q.gid);
+            SacHeader h;
+            h.f[31] = (float)st.lat; h.f[32] = (float)st.lon; h.f[34] = (float)(st.z * 1000);  // stla stlo stdp
+            h.kset(151, 8, V + cmp[c]);
+            h.f[58] = inc; h.f[57] = az;
+            h.kset(113, 16, cid8);
+            h.kset(111, 8, st.name);
+            h.f[36] = (float)q.lon; h.f[35] = (float)q.lat; h.f[38] = (float)q.z;  // evlo evla evdp
+            h.set_time(m.exedate);
+            h.i[16] = c < 6 ? 7 : 6;
+            h.f[5] = (float)p.tbeg;
+            h.set_delta(p.ntdec_w * p.dt);
+            h.f[40] = (float)q.x; h.f[41] = (float)q.y; h.f[42] = (float)q.z;  // user0-2: location asked for
+            const float xb = (float)p.xbeg, yb = (float)p.ybeg, zb = (float)p.zbeg;
+            auto c2f = [](int i, float b, float d) { const float t = ((float)i - 0.5f) * d; return b + t; };
+            h.f[43] = c2f(q.i, xb, (float)p.dx); h.f[44] = c2f(q.j, yb, (float)p.dy); h.f[45] = c2f(q.k, zb, (float)p.dz);
+            h.f[46] = (float)p.clon; h.f[47] = (float)p.clat; h.f[48] = (float)p.phi;  // user6-8
+            return h.bytes(&gf[((size_t)n * ncmp + c) * ntw], ntw);
+        };
+        if (p.wav_format == "csf") {  // m_green.f90:577-585
+            std::string b = "CSFD";
+            const int32_t ntr = ng * ncmp, np = ntw;
+            b.append((const char*)&ntr, 4);
+            b.append((const char*)&np, 4);
+            for (int n = 0; n < ng; ++n)
+                for (int c = 0; c < ncmp; ++c) b += image(n, c);
+            write_file(dir + "/" + p.title + "__" + st.name + "__" + p.green_cmp + "__000000__.csf", b);
+        } else if (p.wav_format == "sac") {  // m_green.f90:571-576, file names :326-331
+            for (int n = 0; n < ng; ++n) {
+                char cid8[16];
+                std::snprintf(cid8, sizeof cid8, "%08lld", m.green.pts[n].gid);
+                for (int c = 0; c < ncmp; ++c)
+                    write_file(dir + "/" + p.title + "__" + cid8 + "__" + st.name + "__" + p.green_cmp + "__" + cmp[c] + "__.sac",
+                               image(n, c));
+            }
+        } else {
+            return swpc::set_err(SWPC_E_ARG, "Green's-function output is written as sac or csf by this build");
         }
         return 0;
     } catch (const std::exception& e) {

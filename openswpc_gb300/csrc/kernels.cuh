@@ -895,6 +895,78 @@ __global__ void k_snap_batch(const SnapArgs* __restrict__ all) {
     if ((int)blockIdx.y < a.n) snap_pix(a, a.pl[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// Green's-function taps (src/swpc_3d/m_green.f90:406-551): at every grid
+// point of the list, the nine displacement gradients (four-point averages of
+// the 4th-order staggered derivatives for the off-diagonal ones) and, with
+// body-force output, the displacement, integrated every step; every ntdec_w
+// steps the six strain-like combinations (and the displacement) are stored.
+struct GreenArgs {
+    Geo g;
+    const float* V;
+    int n, ncmp, ntdec_w, ntw;
+    const int* ijk;     // 3n, 0-based i, j, k
+    double* acc;        // (12, n): dxUx dxUy dxUz dyUx dyUy dyUz dzUx dzUy dzUz Ux Uy Uz
+    float* gf;          // (ntw, ncmp, n) Fortran order
+    float dt, r40x, r41x, r40y, r41y, r40z, r41z;
+    const int* it;
+};
+
+__device__ __forceinline__ void green_pt(const GreenArgs& a, const int n) {
+    if (n >= a.n) return;
+    const int it = *a.it;
+    const Geo& g = a.g;
+    const int i = a.ijk[3 * n], j = a.ijk[3 * n + 1], k = a.ijk[3 * n + 2];
+    auto V = [&](int c, int kk, int ii, int jj) { return a.V[goff(g, 3, c, ii, jj, kk)]; };
+    // (V(k1,i1,j1) - V(k0,i0,j0)) r0 - (V(k2,i2,j2) - V(k3,i3,j3)) r1 along x, y or z
+    auto dx = [&](int c, int kk, int jj, int i0) {  // derivative between i0 and i0 + 1
+        return (V(c, kk, i0 + 1, jj) - V(c, kk, i0, jj)) * a.r40x - (V(c, kk, i0 + 2, jj) - V(c, kk, i0 - 1, jj)) * a.r41x;
+    };
+    auto dy = [&](int c, int kk, int ii, int j0) {
+        return (V(c, kk, ii, j0 + 1) - V(c, kk, ii, j0)) * a.r40y - (V(c, kk, ii, j0 + 2) - V(c, kk, ii, j0 - 1)) * a.r41y;
+    };
+    auto dz = [&](int c, int ii, int jj, int k0) {
+        return (V(c, k0 + 1, ii, jj) - V(c, k0, ii, jj)) * a.r40z - (V(c, k0 + 2, ii, jj) - V(c, k0 - 1, ii, jj)) * a.r41z;
+    };
+    const float dxVx = dx(0, k, j, i - 1), dyVy = dy(1, k, i, j - 1), dzVz = dz(2, i, j, k - 1);
+    const float dxVy = (dx(1, k, j, i) + dx(1, k, j - 1, i) + dx(1, k, j, i - 1) + dx(1, k, j - 1, i - 1)) * 0.25f;
+    const float dxVz = (dx(2, k, j, i) + dx(2, k - 1, j, i) + dx(2, k, j, i - 1) + dx(2, k - 1, j, i - 1)) * 0.25f;
+    const float dyVx = (dy(0, k, i, j) + dy(0, k, i - 1, j) + dy(0, k, i, j - 1) + dy(0, k, i - 1, j - 1)) * 0.25f;
+    const float dyVz = (dy(2, k, i, j) + dy(2, k - 1, i, j) + dy(2, k, i, j - 1) + dy(2, k - 1, i, j - 1)) * 0.25f;
+    const float dzVx = (dz(0, i, j, k) + dz(0, i - 1, j, k) + dz(0, i, j, k - 1) + dz(0, i - 1, j, k - 1)) * 0.25f;
+    const float dzVy = (dz(1, i, j, k) + dz(1, i, j - 1, k) + dz(1, i, j, k - 1) + dz(1, i, j - 1, k - 1)) * 0.25f;
+    const float g9[9] = {dxVx, dxVy, dxVz, dyVx, dyVy, dyVz, dzVx, dzVy, dzVz};
+    double* acc = a.acc;
+    const size_t N = a.n;
+    // time integration in FP64 (the reference sums in FP32)
+    for (int c = 0; c < 9; ++c) acc[c * N + n] += (double)(g9[c] * a.dt);
+    if (a.ncmp == 9) {
+        acc[9 * N + n] += (double)(0.5f * (V(0, k, i, j) + V(0, k, i - 1, j)) * a.dt);
+        acc[10 * N + n] += (double)(0.5f * (V(1, k, i, j) + V(1, k, i, j - 1)) * a.dt);
+        acc[11 * N + n] += (double)(0.5f * (V(2, k, i, j) + V(2, k - 1, i, j)) * a.dt);
+    }
+    if ((it - 1) % a.ntdec_w != 0) return;
+    const int itw = (it - 1) / a.ntdec_w;
+    if (itw >= a.ntw) return;
+    auto A = [&](int c) { return (float)acc[c * N + n]; };
+    float* gf = a.gf + (size_t)n * a.ncmp * a.ntw + itw;
+    const float ud = 1e-15f, ub = 1e-12f, nm = 1e9f;  // UC_DERIV, UC_BF (m_green.f90:31-32), m -> nm
+    gf[0] = A(0) * ud * nm;
+    gf[(size_t)a.ntw] = A(4) * ud * nm;
+    gf[(size_t)2 * a.ntw] = A(8) * ud * nm;
+    gf[(size_t)3 * a.ntw] = (A(5) + A(7)) * ud * nm;
+    gf[(size_t)4 * a.ntw] = (A(2) + A(6)) * ud * nm;
+    gf[(size_t)5 * a.ntw] = (A(1) + A(3)) * ud * nm;
+    if (a.ncmp == 9) {
+        gf[(size_t)6 * a.ntw] = A(9) * ub * nm;
+        gf[(size_t)7 * a.ntw] = A(10) * ub * nm;
+        gf[(size_t)8 * a.ntw] = A(11) * ub * nm;
+    }
+}
+__global__ void k_green(const GreenArgs a) { green_pt(a, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_green_batch(const GreenArgs* __restrict__ all) {
+    green_pt(all[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 struct VmaxArgs {
     Geo g;
     const float* V;

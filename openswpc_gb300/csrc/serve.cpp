@@ -184,7 +184,11 @@ struct swpc_server {
             }
             r->nst = nst;
             r->ntw = ntw;
-            if (cfg.write_sac) status = swpc_host_write_sac(r->sim, nullptr);
+            if (cfg.write_sac) {
+                status = swpc_host_write_sac(r->sim, nullptr);
+                if (!status) status = swpc_host_write_snp(r->sim, nullptr);
+                if (!status) status = swpc_host_write_green(r->sim, nullptr);
+            }
         }
         swpc_gpu_destroy(r->sim);
         r->sim = nullptr;

@@ -56,6 +56,7 @@ struct Sim {
     SrcArgs src_args{};
     TapArgs tap_args{};
     SnapArgs snap_args{};
+    GreenArgs green_args{};
     VmaxArgs vmax_args{};
     std::vector<unsigned int> rep_host;
     bool bf_mode = false, medium_ready = false, diverged = false, profiling = false;
@@ -77,6 +78,7 @@ struct Sim {
                     int stftype, bool bf);
     int set_receivers(int n, const int* ijk, int ntdec_w, int flags);
     int add_snapshot(int sec, int kind, int fix, int d1, int d2, int ntdec_s);
+    int set_green(int n, const int* ijk, int ntdec_w, int bforce);
     const SnapPlane* find_plane(int sec, int kind) const;
     int nframes_done() const;
     void fill_zargs(ZArgs& z) const;

@@ -171,6 +171,9 @@ int Sim::launch_step(bool timed) {
         k_taps<<<(tap_args.n + 127) / 128, 128, 0, stream>>>(tap_args); ++launches;
         ev1(4, stream);
     }
+    if (green_args.n) {
+        k_green<<<(green_args.n + 127) / 128, 128, 0, stream>>>(green_args); ++launches;
+    }
     if (snap_args.n) {
         dim3 sg((snap_args.maxpix + 127) / 128, snap_args.n);
         k_snap<<<sg, 128, 0, stream>>>(snap_args); ++launches;
@@ -463,6 +466,26 @@ int swpc_gpu_add_snapshot(swpc_sim* sim, int section, int kind, int fix, int dec
     return s->add_snapshot(section, kind, fix, dec1, dec2, ntdec_s);
 }
 
+int swpc_gpu_set_green(swpc_sim* sim, int n, const int* ijk, int ntdec_w, int bforce) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || n < 0 || (n > 0 && !ijk) || ntdec_w <= 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_green");
+    return s->set_green(n, ijk, ntdec_w, bforce);
+}
+
+int swpc_gpu_fetch_green(swpc_sim* sim, float* out, int* n, int* ncmp, int* ntw) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    const GreenArgs& a = s->green_args;
+    if (!a.n) return set_err(SWPC_E_STATE, "no Green's-function points were set");
+    if (n) *n = a.n;
+    if (ncmp) *ncmp = a.ncmp;
+    if (ntw) *ntw = a.ntw;
+    if (!out) return 0;
+    CK(cudaMemcpyAsync(out, a.gf, (size_t)a.ntw * a.ncmp * a.n * 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return s->check_divergence();
+}
+
 int swpc_gpu_query_snapshot(swpc_sim* sim, int section, int kind, int* n1, int* n2, int* nframes) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s) return set_err(SWPC_E_ARG, "null simulation");
@@ -700,6 +723,11 @@ int swpc_gpu_reset(swpc_sim* sim) {
         if (t.acc) CK(cudaMemsetAsync(t.acc, 0, (size_t)9 * t.n * 8, s->stream));
     }
     const SnapArgs& a = s->snap_args;
+    const GreenArgs& gr = s->green_args;
+    if (gr.n) {
+        CK(cudaMemsetAsync(gr.acc, 0, (size_t)12 * gr.n * 8, s->stream));
+        CK(cudaMemsetAsync(gr.gf, 0, (size_t)gr.ntw * gr.ncmp * gr.n * 4, s->stream));
+    }
     for (int q = 0; q < a.n; ++q) {
         const SnapPlane& P = a.pl[q];
         const size_t pix = (size_t)P.n1 * P.n2;
@@ -1059,6 +1087,41 @@ const SnapPlane* Sim::find_plane(int sec, int kind) const {
     return nullptr;
 }
 
+// Green's-function points (m_green.f90:67-404): n points at 1-based ijk,
+// samples every ntdec_w steps, with (bforce) or without displacement output
+int Sim::set_green(int n, const int* ijk, int ntdec_w, int bforce) {
+    GreenArgs& a = green_args;
+    a = GreenArgs{};
+    if (n <= 0) return 0;
+    a.g = p.g; a.V = V; a.it = d_it;
+    a.n = n; a.ncmp = bforce ? 9 : 6; a.ntdec_w = ntdec_w;
+    a.ntw = (dims.nt - 1) / ntdec_w + 1;
+    a.dt = (float)dims.dt;
+    a.r40x = (float)(9.0 / 8.0 / dims.dx); a.r41x = (float)(1.0 / 24.0 / dims.dx);
+    a.r40y = (float)(9.0 / 8.0 / dims.dy); a.r41y = (float)(1.0 / 24.0 / dims.dy);
+    a.r40z = (float)(9.0 / 8.0 / dims.dz); a.r41z = (float)(1.0 / 24.0 / dims.dz);
+    std::vector<int> q(3 * (size_t)n);
+    for (int m = 0; m < n; ++m) {
+        const int i = ijk[3 * m], j = ijk[3 * m + 1], k = ijk[3 * m + 2];
+        // the 4th-order stencils reach two cells on either side
+        if (i < 1 || i > dims.nx || j < 1 || j > dims.ny || k < 1 || k > dims.nz)
+            return set_err(SWPC_E_ARG, "Green's-function point outside the grid");
+        q[3 * m] = i - 1; q[3 * m + 1] = j - 1; q[3 * m + 2] = k - 1;
+    }
+    int rc;
+    int* dq = nullptr;
+    if ((rc = dalloc((void**)&dq, q.size() * 4))) return rc;
+    if ((rc = dalloc((void**)&a.acc, (size_t)12 * n * 8))) return rc;
+    if ((rc = dalloc((void**)&a.gf, (size_t)a.ntw * a.ncmp * n * 4))) return rc;
+    a.ijk = dq;
+    CK(cudaMemcpyAsync(dq, q.data(), q.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(a.acc, 0, (size_t)12 * n * 8, stream));
+    CK(cudaMemsetAsync(a.gf, 0, (size_t)a.ntw * a.ncmp * n * 4, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    return 0;
+}
+
 int Sim::nframes_done() const {
     if (!snap_args.n || it_done < 1) return 0;
     return std::min(snap_args.maxframes, (it_done - 1) / std::max(1, snap_args.ntdec_s) + 1);
@@ -1084,6 +1147,8 @@ struct Batch {
     SrcArgs* d_src = nullptr;
     TapArgs* d_tap = nullptr;
     SnapArgs* d_snap = nullptr;
+    GreenArgs* d_green = nullptr;
+    int max_green = 0;
     VmaxArgs* d_vmax = nullptr;
     int** d_its = nullptr;
     int4* d_tblocks = nullptr;
@@ -1114,6 +1179,7 @@ struct Batch {
         const int n = (int)sims.size();
         if (any_vmax) { k_vmax_batch<<<dim3(64, n), 256, 0, stream>>>(d_vmax); ++launches; }
         if (max_nst) { k_taps_batch<<<dim3((max_nst + 127) / 128, n), 128, 0, stream>>>(d_tap); ++launches; }
+        if (max_green) { k_green_batch<<<dim3((max_green + 127) / 128, n), 128, 0, stream>>>(d_green); ++launches; }
         if (any_snap) { k_snap_batch<<<dim3((max_pix + 127) / 128, max_planes, n), 128, 0, stream>>>(d_snap); ++launches; }
         const dim3 tblk(32, TTY);
         if (n_pblocks) {
@@ -1186,6 +1252,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     std::vector<SrcArgs> sa(n);
     std::vector<TapArgs> tp(n);
     std::vector<SnapArgs> sn(n);
+    std::vector<GreenArgs> gr(n);
     std::vector<VmaxArgs> vm(n);
     std::vector<int*> its(n);
     std::vector<int4> tb;
@@ -1202,6 +1269,8 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         sa[q] = s->src_args;
         tp[q] = s->tap_args;
         sn[q] = s->snap_args;
+        gr[q] = s->green_args;
+        b->max_green = std::max(b->max_green, s->green_args.n);
         vm[q] = s->vmax_args;
         its[q] = s->d_it;
         const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + TTY - 1) / TTY, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
@@ -1222,7 +1291,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     }
     int rc;
     if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_pargs, pa)) || (rc = b->upload(&b->d_src, sa)) ||
-        (rc = b->upload(&b->d_tap, tp)) || (rc = b->upload(&b->d_snap, sn)) || (rc = b->upload(&b->d_vmax, vm)) ||
+        (rc = b->upload(&b->d_tap, tp)) || (rc = b->upload(&b->d_snap, sn)) || (rc = b->upload(&b->d_green, gr)) || (rc = b->upload(&b->d_vmax, vm)) ||
         (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_pblocks, pb)))
         return fail(rc);
     if (((uintptr_t)b->d_targs & 127) != 0) return fail(set_err(SWPC_E_CUDA, "tensor-map table is not 128-byte aligned"));

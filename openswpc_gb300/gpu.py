@@ -53,7 +53,8 @@ EXPORTS = [
     "swpc_host_check", "swpc_gpu_fetch_field_static", "swpc_gpu_reset", "swpc_gpu_get_dims", "swpc_gpu_set_zchunk",
     "swpc_gpu_get_zchunk", "swpc_batch_create", "swpc_batch_run", "swpc_batch_sync", "swpc_batch_stream",
     "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes", "swpc_gpu_selftest_wait",
-    "swpc_gpu_add_snapshot", "swpc_gpu_query_snapshot", "swpc_gpu_fetch_section",
+    "swpc_gpu_add_snapshot", "swpc_gpu_query_snapshot", "swpc_gpu_fetch_section", "swpc_gpu_set_green",
+    "swpc_gpu_fetch_green", "swpc_host_write_green",
     "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
@@ -127,6 +128,9 @@ def lib(build=True):
     L.swpc_gpu_add_snapshot.argtypes = [vp, i, i, i, i, i, i]
     L.swpc_gpu_query_snapshot.argtypes = [vp, i, i, ip, ip, ip]
     L.swpc_gpu_fetch_section.argtypes = [vp, i, i, i, fp]
+    L.swpc_gpu_set_green.argtypes = [vp, i, ip, i, i]
+    L.swpc_gpu_fetch_green.argtypes = [vp, fp, ip, ip, ip]
+    L.swpc_host_write_green.argtypes = [vp, ctypes.c_char_p]
     L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_request_bytes.argtypes = [vp]
     L.swpc_host_request_bytes.restype = ctypes.c_longlong
@@ -355,6 +359,21 @@ class Simulation:
 
     def write_sac(self, odir=None):
         _ck(lib().swpc_host_write_sac(self._h, os.fsencode(odir) if odir else None))
+
+    def green(self):
+        """Green's-function traces (n, ncmp, ntw) float32 (green mode)."""
+        n, nc, nw = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _ck(lib().swpc_gpu_fetch_green(self._h, None, ctypes.byref(n), ctypes.byref(nc), ctypes.byref(nw)))
+        out = np.zeros(n.value * nc.value * nw.value, np.float32)
+        _ck(lib().swpc_gpu_fetch_green(self._h, out.ctypes.data, None, None, None))
+        return out.reshape(n.value, nc.value, nw.value)
+
+    def set_green(self, ijk, ntdec_w=1, bforce=False):
+        ijk = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
+        _ck(lib().swpc_gpu_set_green(self._h, ijk.shape[0], ijk.ctypes.data, int(ntdec_w), int(bool(bforce))))
+
+    def write_green(self, odir=None):
+        _ck(lib().swpc_host_write_green(self._h, os.fsencode(odir) if odir else None))
 
     def write_snp(self, odir=None):
         _ck(lib().swpc_host_write_snp(self._h, os.fsencode(odir) if odir else None))

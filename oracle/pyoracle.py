@@ -68,6 +68,7 @@ def lib():
         L.oracle_snap_xy_v.argtypes = [vp, ctypes.c_void_p]
         L.oracle_snap.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.oracle_snap.restype = ctypes.c_longlong
+        L.oracle_green.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_destroy.argtypes = [vp]
         L.oracle_sources.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_stf.argtypes = [vp]
@@ -154,6 +155,15 @@ class Oracle:
         self._L.oracle_snap(self.h, int(section), int(kind), out.ctypes.data)
         nc = 4 if kind == 2 else 3
         return out.reshape(-1, nc, n2, n1)
+
+    def green(self):
+        """Green's-function traces as (ng, ncmp, ntw) float32 (green_mode)."""
+        v = np.zeros(3, np.int32)
+        if self._L.oracle_green(self.h, v.ctypes.data, None) != 0:
+            raise RuntimeError("not in green_mode")
+        out = np.zeros(int(v[0]) * int(v[1]) * int(v[2]), np.float32)
+        self._L.oracle_green(self.h, v.ctypes.data, out.ctypes.data)
+        return out.reshape(int(v[0]), int(v[1]), int(v[2]))
 
     def snap_xy_v(self):
         out = np.zeros(self.nsnap, np.float32)

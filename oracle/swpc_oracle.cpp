@@ -222,6 +222,10 @@ struct Params {
     double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut;
     double vp0, vs0, rho0, qp0, qs0, topo0, z0_xy, x0_yz, y0_xz;
     int snap_sw[5];  // sections xy yz xz fs ob; bits: 1 v, 2 u, 4 ps
+    // Green's-function mode (src/swpc_3d/m_green.f90:67-160)
+    std::string green_stnm, green_cmp, fn_glst, green_fmt;
+    double green_trise, green_maxdist;
+    bool green_bforce, stabilize_pml;
     bool bf_mode, pw_mode, green_mode, sw_wav_v, sw_wav_u, sw_wav_stress, sw_wav_strain, munk, xy_v, xy_u;
 };
 
@@ -253,9 +257,16 @@ static Params read_params(const Ini& ini) {
     p.green_mode = ini.logical("green_mode", false);
     p.bf_mode = ini.logical("bf_mode", false);
     if (p.pw_mode) throw std::runtime_error("pw_mode is not supported by the oracle");
-    if (p.green_mode) throw std::runtime_error("green_mode is not supported by the oracle");
+    if (p.green_mode) {
+        p.green_stnm = ini.str("green_stnm", ""); p.green_cmp = ini.str("green_cmp", "");
+        p.green_trise = ini.real("green_trise", 1.0); p.green_bforce = ini.logical("green_bforce", false);
+        p.green_maxdist = ini.real("green_maxdist", 1e30); p.fn_glst = ini.str("fn_glst", "");
+        p.green_fmt = ini.str("green_fmt", "xyz");
+        if (p.green_fmt != "xyz") throw std::runtime_error("only green_fmt = xyz is supported by the oracle");
+        if (p.green_cmp != "x" && p.green_cmp != "y" && p.green_cmp != "z") throw std::runtime_error("no matching green_cmp");
+    }
     if (ini.logical("earth_flattening", false)) throw std::runtime_error("earth_flattening is not supported by the oracle");
-    if (ini.logical("stabilize_pml", false)) throw std::runtime_error("stabilize_pml is not supported by the oracle");
+    p.stabilize_pml = ini.logical("stabilize_pml", false);
     p.fn_stf = ini.str("fn_stf", "");
     p.stftype = ini.str("stftype", "kupper");
     p.stf_format = ini.str("stf_format", "xym0ij");
@@ -300,6 +311,7 @@ struct SimBase {
     virtual void step(int it) = 0;
     virtual void get_field(int which, double* out) = 0;
     virtual void get_medium(int which, float* out) = 0;
+    virtual int green_out(int* ng_ncmp_ntw, float* out) = 0;
     Params p;
     int nt_done = 0;
     int nst = 0, ntw = 0;
@@ -366,10 +378,139 @@ struct Sim : SimBase {
         setup_regions();
         setup_medium(inf_dir, vm5);
         kernel_setup();
-        source_setup(inf_dir);
+        if (!p.green_mode) source_setup(inf_dir);  // m_source.f90:84-91: no regular source grid
+        else dt_dxyz = (MP)dt / (dx * dy * dz);
         absorb_setup();
         wav_setup(inf_dir);
+        if (p.green_mode) green_setup(inf_dir);
         snap_setup();
+    }
+
+    // ------------------------------------------------------------------
+    // Green's-function mode (src/swpc_3d/m_green.f90): a unit body force at
+    // the station green_stnm, strain (and displacement) recorded at the grid
+    // points of fn_glst
+    // ------------------------------------------------------------------
+    struct GPt { int i, j, k, gid; SP x, y, z; };
+    std::vector<GPt> gpts;
+    std::vector<SP> gacc;         // (12, ng): dxUx dxUy dxUz dyUx dyUy dyUz dzUx dzUy dzUz Ux Uy Uz
+    std::vector<float> gf;        // (ntw, ncmp * ng), Fortran order
+    int gncmp = 6, gsrc_i = 0, gsrc_j = 0, gsrc_k = 0;
+    SP gfx = 0, gfy = 0, gfz = 0;
+
+    // m_green.f90:67-404
+    void green_setup(const std::string& inf_dir) {
+        int q = 0;
+        while (q < (int)sta_all.size() && sta_all[q].name != p.green_stnm.substr(0, 8)) ++q;
+        if (q == (int)sta_all.size()) throw std::runtime_error("green_stnm not in the station list");
+        gsrc_i = sta_all[q].i; gsrc_j = sta_all[q].j; gsrc_k = sta_all[q].k;
+        const SP xsrc = sta_all[q].x, ysrc = sta_all[q].y;
+        gfx = p.green_cmp == "x" ? 1 : 0; gfy = p.green_cmp == "y" ? 1 : 0; gfz = p.green_cmp == "z" ? 1 : 0;
+        M0 = 1;
+        fcut = 0;  // never set by source__setup in this mode
+        stf = stf_code(p.stftype);
+        ntw = (int)std::floor((float)(p.nt - 1) / (float)p.ntdec_w + 1.0f);
+        std::string fn = p.fn_glst;
+        if (!fn.empty() && fn[0] != '/') fn = inf_dir + "/" + fn;
+        for (auto& r : data_lines(fn)) {
+            auto t = tokens(r);
+            if (t.size() < 4) throw std::runtime_error("bad Green's function point: " + r);
+            const SP xg = (SP)Ini::to_real(t[0]), yg = (SP)Ini::to_real(t[1]), zg = (SP)Ini::to_real(t[2]);
+            const int gid = (int)Ini::to_real(t[3]);
+            const SP dd = std::sqrt((xg - xsrc) * (xg - xsrc) + (yg - ysrc) * (yg - ysrc));
+            if (dd > (SP)p.green_maxdist) continue;
+            const int ii = x2i(xg, xbeg, (SP)dx), jj = x2i(yg, ybeg, (SP)dy), kk = x2i(zg, zbeg, (SP)dz);
+            if (ibeg <= ii && ii <= iend && jbeg <= jj && jj <= jend && kob(ii, jj) <= kk && kk <= kend)
+                gpts.push_back(GPt{ii, jj, kk, gid, xg, yg, zg});
+        }
+        gncmp = p.green_bforce ? 9 : 6;
+        gacc.assign(12 * gpts.size(), 0);
+        gf.assign((size_t)ntw * gncmp * gpts.size(), 0.f);
+        r40x = MP(9.0) / MP(8.0) / dx; r40y = MP(9.0) / MP(8.0) / dy; r40z = MP(9.0) / MP(8.0) / dz;
+        r41x = MP(1.0) / MP(24.0) / dx; r41y = MP(1.0) / MP(24.0) / dy; r41z = MP(1.0) / MP(24.0) / dz;
+        r20x = (MP)1.0 / dx; r20y = (MP)1.0 / dy; r20z = (MP)1.0 / dz;
+    }
+
+    int green_out(int* v, float* out) override {
+        if (!p.green_mode) return -1;
+        v[0] = (int)gpts.size(); v[1] = gncmp; v[2] = ntw;
+        if (out) std::copy(gf.begin(), gf.end(), out);
+        return 0;
+    }
+
+    // m_green.f90:406-551
+    void green_store(int it) {
+        if (!p.green_mode) return;
+        const SP UC_BF = (SP)1e-12, UC_DERIV = (SP)1e-15;
+        const int ng = (int)gpts.size();
+        for (int n = 0; n < ng; ++n) {
+            const int ii = gpts[n].i, jj = gpts[n].j, kk = gpts[n].k;
+            auto D = [&](F3<MP>& V, int k1, int i1, int j1, int k0, int i0, int j0, int k2, int i2, int j2, int k3, int i3,
+                         int j3, MP r0, MP r1) { return (V(k1, i1, j1) - V(k0, i0, j0)) * r0 - (V(k2, i2, j2) - V(k3, i3, j3)) * r1; };
+            const MP dxVx = D(Vx, kk, ii, jj, kk, ii - 1, jj, kk, ii + 1, jj, kk, ii - 2, jj, r40x, r41x);
+            const MP dyVy = D(Vy, kk, ii, jj, kk, ii, jj - 1, kk, ii, jj + 1, kk, ii, jj - 2, r40y, r41y);
+            const MP dzVz = D(Vz, kk, ii, jj, kk - 1, ii, jj, kk + 1, ii, jj, kk - 2, ii, jj, r40z, r41z);
+            // four-point averages of the staggered off-diagonal derivatives
+            auto dxq = [&](F3<MP>& V, int k, int j) {
+                return D(V, k, ii + 1, j, k, ii, j, k, ii + 2, j, k, ii - 1, j, r40x, r41x);
+            };
+            auto dxp = [&](F3<MP>& V, int k, int j) {
+                return D(V, k, ii, j, k, ii - 1, j, k, ii + 1, j, k, ii - 2, j, r40x, r41x);
+            };
+            auto dyq = [&](F3<MP>& V, int k, int i) {
+                return D(V, k, i, jj + 1, k, i, jj, k, i, jj + 2, k, i, jj - 1, r40y, r41y);
+            };
+            auto dyp = [&](F3<MP>& V, int k, int i) {
+                return D(V, k, i, jj, k, i, jj - 1, k, i, jj + 1, k, i, jj - 2, r40y, r41y);
+            };
+            auto dzq = [&](F3<MP>& V, int i, int j) {
+                return D(V, kk + 1, i, j, kk, i, j, kk + 2, i, j, kk - 1, i, j, r40z, r41z);
+            };
+            auto dzp = [&](F3<MP>& V, int i, int j) {
+                return D(V, kk, i, j, kk - 1, i, j, kk + 1, i, j, kk - 2, i, j, r40z, r41z);
+            };
+            const MP dxVy = (dxq(Vy, kk, jj) + dxq(Vy, kk, jj - 1) + dxp(Vy, kk, jj) + dxp(Vy, kk, jj - 1)) * (MP)0.25;
+            const MP dxVz = (dxq(Vz, kk, jj) + dxq(Vz, kk - 1, jj) + dxp(Vz, kk, jj) + dxp(Vz, kk - 1, jj)) * (MP)0.25;
+            const MP dyVx = (dyq(Vx, kk, ii) + dyq(Vx, kk, ii - 1) + dyp(Vx, kk, ii) + dyp(Vx, kk, ii - 1)) * (MP)0.25;
+            const MP dyVz = (dyq(Vz, kk, ii) + dyq(Vz, kk - 1, ii) + dyp(Vz, kk, ii) + dyp(Vz, kk - 1, ii)) * (MP)0.25;
+            const MP dzVx = (dzq(Vx, ii, jj) + dzq(Vx, ii - 1, jj) + dzp(Vx, ii, jj) + dzp(Vx, ii - 1, jj)) * (MP)0.25;
+            const MP dzVy = (dzq(Vy, ii, jj) + dzq(Vy, ii, jj - 1) + dzp(Vy, ii, jj) + dzp(Vy, ii, jj - 1)) * (MP)0.25;
+            SP* a = &gacc[12 * n];
+            const MP g9[9] = {dxVx, dxVy, dxVz, dyVx, dyVy, dyVz, dzVx, dzVy, dzVz};
+            for (int c = 0; c < 9; ++c) a[c] = a[c] + (SP)(g9[c] * (MP)dt);
+            if (p.green_bforce) {
+                a[9] = a[9] + (SP)0.5 * (SP)(Vx(kk, ii, jj) + Vx(kk, ii - 1, jj)) * dt;
+                a[10] = a[10] + (SP)0.5 * (SP)(Vy(kk, ii, jj) + Vy(kk, ii, jj - 1)) * dt;
+                a[11] = a[11] + (SP)0.5 * (SP)(Vz(kk, ii, jj) + Vz(kk - 1, ii, jj)) * dt;
+            }
+        }
+        if ((it - 1) % p.ntdec_w != 0) return;
+        const int itw = (it - 1) / p.ntdec_w;
+        const SP sd = UC_DERIV * (SP)1e9, sb = UC_BF * (SP)1e9;
+        for (int n = 0; n < ng; ++n) {
+            const SP* a = &gacc[12 * n];
+            float* g = &gf[(size_t)gncmp * n * ntw + itw];
+            auto put = [&](int c, SP v) { g[(size_t)c * ntw] = (float)v; };
+            put(0, a[0] * sd); put(1, a[4] * sd); put(2, a[8] * sd);
+            put(3, (a[5] + a[7]) * sd); put(4, (a[2] + a[6]) * sd); put(5, (a[1] + a[3]) * sd);
+            if (p.green_bforce) { put(6, a[9] * sb); put(7, a[10] * sb); put(8, a[11] * sb); }
+        }
+    }
+
+    // m_green.f90:614-649
+    void green_source(int it) {
+        if (!p.green_mode) return;
+        const SP st = momentrate<SP>(tbeg + it * dt, stf, (SP)0, (SP)p.green_trise);
+        const SP dtd = (SP)dt_dxyz;
+        const SP fx = gfx * dtd * st, fy = gfy * dtd * st, fz = gfz * dtd * st;
+        const int ii = gsrc_i, jj = gsrc_j, kk = gsrc_k;
+        const SP two = 2.0;
+        Vx(kk, ii, jj) = Vx(kk, ii, jj) + (MP)((two / (rho(kk, ii, jj) + rho(kk, ii + 1, jj))) * fx / 2);
+        Vx(kk, ii - 1, jj) = Vx(kk, ii - 1, jj) + (MP)((two / (rho(kk, ii, jj) + rho(kk, ii - 1, jj))) * fx / 2);
+        Vy(kk, ii, jj) = Vy(kk, ii, jj) + (MP)((two / (rho(kk, ii, jj) + rho(kk, ii, jj + 1))) * fy / 2);
+        Vy(kk, ii, jj - 1) = Vy(kk, ii, jj - 1) + (MP)((two / (rho(kk, ii, jj) + rho(kk, ii, jj - 1))) * fy / 2);
+        Vz(kk, ii, jj) = Vz(kk, ii, jj) + (MP)((two / (rho(kk, ii, jj) + rho(kk + 1, ii, jj))) * fz / 2);
+        Vz(kk - 1, ii, jj) = Vz(kk - 1, ii, jj) + (MP)((two / (rho(kk, ii, jj) + rho(kk - 1, ii, jj))) * fz / 2);
     }
 
     // m_global.f90:219-376 for a single rank
@@ -573,6 +714,55 @@ struct Sim : SimBase {
                 kfs_top(i, j) = std::max(fmn - 2, kbeg); kfs_bot(i, j) = std::min(fmx + 2, kend);
                 kob_top(i, j) = std::max(omn - 2, kbeg); kob_bot(i, j) = std::min(omx + 2, kend);
             }
+        if (p.stabilize_pml) stabilize_absorber();
+    }
+
+    // src/swpc_3d/m_medium.f90:273-337 (with velocity_minmax :396-427)
+    void stabilize_absorber() {
+        float vmax = -1;
+        for (int j = jbeg; j <= jend; ++j)
+            for (int i = ibeg; i <= iend; ++i)
+                for (int k = kfs(i, j) + 1; k <= kend; ++k)
+                    vmax = std::max(vmax, (float)std::sqrt((lam(k, i, j) + 2 * mu(k, i, j)) / rho(k, i, j)));
+        const float V_DYNAMIC_RANGE = 0.4f, vmin_pml = vmax * V_DYNAMIC_RANGE;
+        const int LV_THICK = 20;
+        auto ka = [&](int i, int j) { return (i <= na || nx - na + 1 <= i || j <= na || ny - na + 1 <= j) ? kbeg : kend - na + 1; };
+        auto kmin = [&](int i, int j) {
+            int m = 1 << 30;
+            for (int jj = j - 2; jj <= j + 2; ++jj)
+                for (int ii = i - 2; ii <= i + 2; ++ii) m = std::min(m, ka(ii, jj));
+            return m;
+        };
+        for (int j = jbeg - 1; j <= jend + 1; ++j)
+            for (int i = ibeg - 1; i <= iend + 1; ++i) {
+                int k = kmin(i, j);
+                while (k <= kend) {
+                    if (lam(k, i, j) < lam(k - 1, i, j) || mu(k, i, j) < mu(k - 1, i, j)) {
+                        int k2;
+                        for (k2 = k + 1; k2 <= kend; ++k2)
+                            if (lam(k2, i, j) > lam(k2 - 1, i, j) || mu(k2, i, j) > mu(k2 - 1, i, j)) break;
+                        if (k2 - k <= LV_THICK) {
+                            rho(k, i, j) = rho(k - 1, i, j); lam(k, i, j) = lam(k - 1, i, j); mu(k, i, j) = mu(k - 1, i, j);
+                            taup(k, i, j) = taup(k - 1, i, j); taus(k, i, j) = taus(k - 1, i, j);
+                            k = k2 - 1;
+                        }
+                    }
+                    k = k + 1;
+                }
+            }
+        const SP eps = std::numeric_limits<float>::epsilon(), gamma = std::sqrt((SP)3.0);
+        for (int j = jbeg - 1; j <= jend + 1; ++j)
+            for (int i = ibeg - 1; i <= iend + 1; ++i)
+                for (int k = kmin(i, j); k <= kend; ++k) {
+                    SP vs = std::sqrt(mu(k, i, j) / rho(k, i, j));
+                    if (vs < eps) continue;
+                    if (vs < (SP)vmin_pml) {
+                        vs = (SP)vmin_pml;
+                        const SP vp = vs * gamma;
+                        lam(k, i, j) = rho(k, i, j) * (vp * vp - 2 * vs * vs);
+                        mu(k, i, j) = rho(k, i, j) * (vs * vs);
+                    }
+                }
     }
 
     // src/swpc_3d/m_kernel.f90:30-73
@@ -763,8 +953,12 @@ struct Sim : SimBase {
     }
 
     // src/swpc_3d/m_wav.f90:54-271 (xy station format)
+    struct StaPos { int i, j, k; std::string name; SP x, y; };
+    std::vector<StaPos> sta_all;  // every station inside the model (the green_stnm look-up)
+
     void wav_setup(const std::string& inf_dir) {
-        if (!(p.sw_wav_v || p.sw_wav_u || p.sw_wav_stress || p.sw_wav_strain)) { nst = 0; return; }
+        const bool rec = p.sw_wav_v || p.sw_wav_u || p.sw_wav_stress || p.sw_wav_strain;
+        if (!rec && !p.green_mode) { nst = 0; return; }
         ntw = (int)std::floor((float)(p.nt - 1) / (float)p.ntdec_w + 1.0f);
         std::string fn = p.fn_stloc;
         if (!fn.empty() && fn[0] != '/') fn = inf_dir + "/" + fn;
@@ -786,10 +980,12 @@ struct Sim : SimBase {
                 else ks = x2i(zs, zbeg, (SP)dz);
                 if (ks > kend) ks = kend - 1;
                 if (ks < kbeg) ks = kbeg + 1;
-                sta.push_back(Sta{is, js, ks, nm8});
+                sta_all.push_back(StaPos{is, js, ks, nm8, xs, ys});
+                if (rec) sta.push_back(Sta{is, js, ks, nm8});
             }
         }
         nst = (int)sta.size();
+        if (!rec) return;
         if (p.sw_wav_v) wav_vel.assign((size_t)ntw * 3 * nst, 0);
         if (p.sw_wav_u) wav_disp.assign((size_t)ntw * 3 * nst, 0);
         if (p.sw_wav_stress) wav_stress.assign((size_t)ntw * 6 * nst, 0);
@@ -825,6 +1021,7 @@ struct Sim : SimBase {
     // ------------------------------------------------------------------
     void step(int it) override {
         if (p.ntdec_r > 0 && it % p.ntdec_r == 0) vmax(it);
+        green_store(it);
         wav_store(it);
         snap_write(it);
         update_stress();
@@ -834,6 +1031,7 @@ struct Sim : SimBase {
         update_vel();
         if (pml) pml_vel(); else cerjan_vel();
         bodyforce(it);
+        green_source(it);
         comm_vel();
         nt_done = it;
     }
@@ -1407,6 +1605,12 @@ void oracle_snap_xy_v(void* h, float* out) {
     SimBase* s = (SimBase*)h;
     for (auto& o : s->snaps)
         if (o.sec == 0 && o.kind == 0) std::copy(o.frames.begin(), o.frames.end(), out);
+}
+// Green's-function traces (ntw, ncmp * ng) in Fortran order and the layout
+// ints: ng, ncmp, ntw; returns 0, or -1 outside green mode
+int oracle_green(void* h, int* ng_ncmp_ntw, float* out) {
+    SimBase* s = (SimBase*)h;
+    return s->green_out(ng_ncmp_ntw, out);
 }
 // stacked frames of one snapshot (section, kind); returns the float count,
 // -1 when that snapshot was not requested; out may be null to query

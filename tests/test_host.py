@@ -140,3 +140,12 @@ def test_create_rejects_bad_dims():
     d = gpu.make_dims(64, 64, 64, 10, 0.5, 0.5, 0.5, 0.02, na=10)
     d.nm = 2
     assert gpu.required_bytes(d) < 0  # nm must be 3
+
+
+def test_green_mode_host_setup(tmp_path):
+    """green_mode: no regular source grid, one body-force pseudo source at
+    the station, no station recording (m_source.f90:84-91, m_wav.f90:76-82)."""
+    inf = configs.write_green(str(tmp_path), nt=20)
+    h = gpu.host_check(inf)
+    assert h["nsrc"] == 1 and h["nst"] == 0
+    assert h["M0"] == 1.0 and h["fcut"] == 0.0
