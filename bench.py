@@ -244,6 +244,17 @@ def cpu_sample(steps=8, warmup=2, n=(512, 512, 256), dx=0.5, dt=0.02, mode="mixe
                 seconds=el)
 
 
+def arm_config(w, args, world):
+    """The workload description both arms print."""
+    n_int, n_pml = counts(w)
+    gb = (B_INT * n_int + B_PML * n_pml) / 1e9
+    return {"workload": "large single source %dx%dx%d" % (w["nx"], w["ny"], w["nz"]),
+            "dx_km": w["dx"], "dt_s": w["dt"], "nt": w["nt"], "nm": 3, "na": 20, "receivers": w["nst"],
+            "snapshot": "xy_v every %d steps" % w["ntdec_s"], "parallelism": "replicas x%d" % world,
+            "store": args.store,
+            "l2": "inputs larger than L2: every step streams %.0f GB (model bytes), no flush" % gb}
+
+
 def run_reference(args, w):
     world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
@@ -254,8 +265,7 @@ def run_reference(args, w):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * cb["seconds"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64/f32 (mixed, reference default)", "data": "synthetic",
-        "config": {"workload": "large single source 1024x1024x512 (bounded CPU sample)", "sample": cb["sample"],
-                   "l2": "inputs larger than L2"},
+        "config": dict(arm_config(w, args, 1), sample=cb["sample"]),
         "cpu_baseline": {"value": cb["value"], "unit": "pt/s", "cores": cb["cores"], "kind": "port",
                          "sample": cb["sample"]},
         "e2e": {"value": cb["value"], "unit": "pt/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -367,12 +377,7 @@ def run_gpu(args, w):
             "metric": "grid-pt updates/s", "value": value, "unit": "pt/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "large single source %dx%dx%d" % (w["nx"], w["ny"], w["nz"]),
-                       "dx_km": w["dx"], "dt_s": w["dt"], "nt": w["nt"], "nm": 3, "na": 20, "receivers": w["nst"],
-                       "snapshot": "xy_v every %d steps" % w["ntdec_s"], "parallelism": "replicas x%d" % world,
-                       "store": args.store,
-                       "l2": "inputs larger than L2 (%.0f GB working set), no flush" % (gpu.required_bytes(
-                           gpu.make_dims(w["nx"], w["ny"], w["nz"], w["nt"], w["dx"], w["dx"], w["dx"], w["dt"])) / 1e9)},
+            "config": arm_config(w, args, world),
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
                                   "peak": peak, "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak,
                                   "model": "%d B/interior pt + %d B/PML pt per step" % (b_int, b_pml)},

@@ -126,6 +126,19 @@ int swpc_gpu_add_snapshot(swpc_sim* sim, int section, int kind, int fix, int dec
 int swpc_gpu_query_snapshot(swpc_sim* sim, int section, int kind, int* n1, int* n2, int* nframes);
 int swpc_gpu_fetch_section(swpc_sim* sim, int section, int kind, int frame, float* out);
 
+/* Overwrite one state field (which = 0..8 for Vx Vy Vz Sxx Syy Szz Syz Sxz
+ * Sxy) from a Fortran halo array A(k,i,j) (the layout of the medium arrays):
+ * every cell of the physical columns, including the z halo planes; the x/y
+ * ghost columns stay zero.  Used for the plane-wave initial condition
+ * (pw_setup, m_source.f90:316-466). */
+int swpc_gpu_set_field(swpc_sim* sim, int which, const float* field);
+
+/* Plane-wave mode (pw_mode): before each PML update the lateral ghost
+ * planes are extrapolated linearly from the two outermost cells
+ * (m_absorb_p.f90:137-244, 332-427).  Needs the PML absorber; such
+ * simulations are not batched. */
+int swpc_gpu_set_plane_wave(swpc_sim* sim, int on);
+
 /* Reciprocal Green's-function taps (green__store, m_green.f90:406-551): n
  * grid points at 1-based ijk (3n); every ntdec_w steps the combinations
  * dxUx, dyUy, dzUz, dyUz+dzUy, dxUz+dzUx, dxUy+dyUx of the time-integrated

@@ -163,6 +163,25 @@ def write_green(d, nx=96, ny=96, nz=64, nt=200, cmp="z", bforce=True, n_points=2
     return os.path.join(d, "input.inf")
 
 
+def write_plane_wave(d, nx=96, ny=96, nz=64, nt=200, ps="p", strike=30.0, dip=20.0, rake=0.0, **over):
+    """Plane-wave mode (pw_mode): a P or S plane wave of Kupper shape
+    (pw_zlen = 6 km) whose front starts at 20 km depth, incident with the
+    given strike/dip(/rake), in the two-layer medium of the small plain
+    configuration; 9 surface receivers."""
+    os.makedirs(d, exist_ok=True)
+    keys = base_keys(nx=nx, ny=ny, nz=nz, nt=nt, xbeg=-nx * 0.25, ybeg=-ny * 0.25, pw_mode=True, pw_ztop=20.0,
+                     pw_zlen=6.0, pw_ps=ps, pw_strike=strike, pw_dip=dip, pw_rake=rake, **over)
+    write_inf(os.path.join(d, "input.inf"), keys)
+    write_lhm(os.path.join(d, "lhm.dat"), [(0, 2.7, 5.5, 3.2, 200, 100), (4, 2.9, 6.5, 3.7, 600, 300)])
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        n = 0
+        for y in (-6.0, 0.0, 6.0):
+            for x in (-6.0, 0.0, 6.0):
+                n += 1
+                f.write("  %.3f %.3f 0.0 P%02d fsb\n" % (x, y, n))
+    return os.path.join(d, "input.inf")
+
+
 def write_uniform(d, nx=64, ny=64, nz=64, nt=100, dx=0.5, dt=0.02, vp=6.0, vs=3.5, rho=2.8, q=1e6,
                   source="0.0 0.0 0.0", stations=(("0.0", "0.0", "0.0", "C"),), bf=None, **over):
     """Uniform whole-space medium (no air layer), used by the analytic and

@@ -220,6 +220,10 @@ struct Params {
     double dx, dy, dz, dt, xbeg, ybeg, zbeg, tbeg, clon, clat, phi, fq_min, fq_max, fq_ref, vcut, z0_xy, x0_yz, y0_xz;
     bool bf_mode, sw_v, sw_u, sw_stress, sw_strain, munk;
     int snap_sw[5];  // per section xy yz xz fs ob: bit SWPC_SNAPK_* set when <sec>_<kind>%sw is true
+    // plane-wave mode (m_source.f90:316-466)
+    bool pw_mode = false;
+    std::string pw_ps;
+    double pw_ztop = 1e30, pw_zlen = -1, pw_strike = 0, pw_dip = 0, pw_rake = 0;
     // Green's-function mode (m_green.f90:100-160)
     bool green_mode = false, green_bforce = false;
     std::string green_stnm, green_cmp, fn_glst, green_fmt;
@@ -274,12 +278,22 @@ void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& 
     const size_t n3 = G.n3();
     rho.assign(n3, 0); lam.assign(n3, 0); mu.assign(n3, 0); qp.assign(n3, 0); qs.assign(n3, 0);
     auto zc = [&](int k) { return p.zbeg + (k - 0.5) * p.dz; };
+    // these models depend on depth only: build one column (k fastest, as the
+    // arrays are laid out) and copy it into every (i, j) column at the end
+    const int nk = p.nz + 6;
+    std::vector<float> c_rho(nk), c_lam(nk), c_mu(nk), c_qp(nk), c_qs(nk);
     auto fill = [&](int k, double r, double vp, double vs, double q1, double q2) {
+        const int q = k + 2;
+        c_rho[q] = (float)r; c_mu[q] = (float)(r * vs * vs); c_lam[q] = (float)(r * (vp * vp - 2 * vs * vs));
+        c_qp[q] = (float)q1; c_qs[q] = (float)q2;
+    };
+    auto spread = [&]() {
+        std::vector<float>* dst[5] = {&rho, &lam, &mu, &qp, &qs};
+        const std::vector<float>* src[5] = {&c_rho, &c_lam, &c_mu, &c_qp, &c_qs};
         for (int j = -2; j <= p.ny + 3; ++j)
             for (int i = -2; i <= p.nx + 3; ++i) {
-                size_t q = G.idx(k, i, j);
-                rho[q] = (float)r; mu[q] = (float)(r * vs * vs); lam[q] = (float)(r * (vp * vp - 2 * vs * vs));
-                qp[q] = (float)q1; qs[q] = (float)q2;
+                const size_t b = G.idx(-2, i, j);
+                for (int f = 0; f < 5; ++f) std::copy(src[f]->begin(), src[f]->end(), dst[f]->begin() + b);
             }
     };
     if (inf.b("earth_flattening", false)) throw std::runtime_error("earth_flattening is not supported by this build");
@@ -293,6 +307,7 @@ void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& 
             else if (z > 0) fill(k, 1.0, seawater_vel(z, p.munk), 0, 1e6, 1e6);
             else fill(k, 0.001, 0, 0, 10, 10);
         }
+        spread();
         return;
     }
     if (p.vmodel_type != "lhm" && p.vmodel_type != "lgm")
@@ -335,6 +350,7 @@ void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& 
             fill(k, R, P, S, A, B);
         }
     }
+    spread();
 }
 
 // src/shared/m_fdtool.f90:691-812 in FP64
@@ -505,6 +521,104 @@ void sdr2moment(double strike, double dip, double rake, double* m6) {
     m6[5] = (sd * cl * c2f + s2d * sl * s2f / 2);    // xy
 }
 
+// Source time functions in single precision (src/shared/m_fdtool.f90:339-497)
+float momentrate_h(float t, const std::string& type, float ts, float tr) {
+    const float pi = 3.14159265358979f;
+    if (type == "boxcar") return (ts <= t && t <= ts + tr) ? 1.f / tr : 0.f;
+    if (type == "triangle") {
+        if (ts <= t && t <= ts + tr / 2) return 4 * (t - ts) / (tr * tr);
+        if (ts + tr / 2 < t && t <= ts + tr) return -4 * (t - ts - tr) / (tr * tr);
+        return 0.f;
+    }
+    if (type == "herrmann") {
+        const float t1 = ts + tr / 4, t2 = ts + 3 * tr / 4;
+        if (ts <= t && t < t1) return 16 * (t - ts) * (t - ts) / (tr * tr * tr);
+        if (t1 <= t && t < t2) return -2 * (8 * (t * t + tr * ts + ts * ts - t * tr - 2 * t * ts) + tr * tr) / (tr * tr * tr);
+        if (t2 <= t && t <= ts + tr) return 16 * (ts + tr - t) * (ts + tr - t) / (tr * tr * tr);
+        return 0.f;
+    }
+    if (type == "cosine" || type == "scosine")
+        return (ts <= t && t <= ts + tr) ? (1 - std::cos(2 * pi * (t - ts) / tr)) / tr : 0.f;
+    if (type == "texp") {
+        if (ts > t) return 0.f;
+        const float tt = t - ts;
+        return (2 * pi) * (2 * pi) * tt / (tr * tr) * std::exp(-2 * pi * tt / tr);
+    }
+    if (ts <= t && t <= ts + tr) {  // kupper
+        const float sv = std::sin(pi * (t - ts) / tr);
+        return 3 * pi * sv * sv * sv / (4 * tr);
+    }
+    return 0.f;
+}
+
+// pw_setup (src/swpc_3d/m_source.f90:316-466) in single precision: the
+// initial velocity and stress of a plane P or S wave over the whole halo grid
+// (Vx Vy Vz Sxx Syy Szz Syz Sxz Sxy), and fcut = v / pw_zlen at the centre
+// column at depth pw_ztop.
+double plane_wave(const Params& p, const Grid& G, const std::vector<float>& rho, const std::vector<float>& lam,
+                  const std::vector<float>& mu, std::vector<std::vector<float>>& F) {
+    const float d2r = 3.14159265358979f / 180.f;
+    const float dipr = (float)p.pw_dip * d2r, strr = (float)p.pw_strike * d2r, rakr = (float)p.pw_rake * d2r;
+    const float sd = std::sin(dipr), cd = std::cos(dipr), sf = std::sin(strr), cf = std::cos(strr);
+    const float sl = std::sin(rakr), cl = std::cos(rakr), c2d = std::cos(2 * dipr), c2f = std::cos(2 * strr);
+    const bool P = p.pw_ps == "p" || p.pw_ps == "P";
+    const float xb = (float)p.xbeg, yb = (float)p.ybeg, zb = (float)p.zbeg, dx = (float)p.dx, dy = (float)p.dy;
+    const float dz = (float)p.dz, dt = (float)p.dt, zt = (float)p.pw_ztop, zl = (float)p.pw_zlen;
+    const std::string& st = p.stftype;
+    const float eps = 1.1920928955078125e-07f;
+    F.assign(9, std::vector<float>(G.n3(), 0.f));
+    for (int j = -2; j <= p.ny + 3; ++j)
+        for (int i = -2; i <= p.nx + 3; ++i)
+            for (int k = -2; k <= p.nz + 3; ++k) {
+                const size_t c = G.idx(k, i, j);
+                const float v = P ? std::sqrt((lam[c] + 2 * mu[c]) / rho[c]) : std::sqrt(mu[c] / rho[c]);
+                if (v < eps) continue;
+                const float x0 = xb + ((float)i - 0.5f) * dx, y0 = yb + ((float)j - 0.5f) * dy;
+                const float z0 = zb + ((float)k - 0.5f) * dz - zt;
+                const float x1 = x0 + dx / 2.f, y1 = y0 + dy / 2.f, z1 = z0 + dz / 2.f;
+                const float sh = dt / 2.f * v;
+                auto m = [&](float a) { return momentrate_h(a, st, 0.f, zl); };
+                const float s_ii = m(sd * sf * x0 - sd * cf * y0 + cd * z0);
+                const float s_vx = m(sd * sf * x1 - sd * cf * y0 + cd * z0 + sh);
+                const float s_vy = m(sd * sf * x0 - sd * cf * y1 + cd * z0 + sh);
+                const float s_vz = m(sd * sf * x0 - sd * cf * y0 + cd * z1 + sh);
+                const float s_yz = m(sd * sf * x0 - sd * cf * y1 + cd * z1);
+                const float s_xz = m(sd * sf * x1 - sd * cf * y0 + cd * z1);
+                const float s_xy = m(sd * sf * x1 - sd * cf * y1 + cd * z0);
+                const float la0 = lam[c], mu0 = mu[c];
+                if (P) {
+                    F[0][c] = -sd * sf * s_vx;
+                    F[1][c] = sd * cf * s_vy;
+                    F[2][c] = -cd * s_vz;
+                    F[3][c] = -(la0 + 2 * mu0 * sd * sd * sf * sf) * s_ii / v;
+                    F[4][c] = -(la0 + 2 * mu0 * sd * sd * cf * cf) * s_ii / v;
+                    F[5][c] = -(la0 + 2 * mu0 * cd * cd) * s_ii / v;
+                    F[6][c] = 2 * mu0 * sd * cd * cf * s_yz / v;
+                    F[7][c] = -2 * mu0 * sd * cd * sf * s_xz / v;
+                    F[8][c] = 2 * mu0 * sd * cd * sf * s_xy / v;
+                } else {
+                    F[0][c] = (cl * cf + sl * cd * sf) * s_vx;
+                    F[1][c] = (cl * sf - sl * cd * cf) * s_vy;
+                    F[2][c] = -sl * sd * s_vz;
+                    F[3][c] = 2 * mu0 * sd * sf * (cl * cf + sl * cd * sf) * s_ii / v;
+                    F[4][c] = -2 * mu0 * sd * cf * (cl * sf - sl * cd * cf) * s_ii / v;
+                    F[5][c] = -2 * mu0 * cd * sl * sd * s_ii / v;
+                    F[6][c] = mu0 * (cl * cd * sf - sl * c2d * cf) * s_yz / v;
+                    F[7][c] = mu0 * (cl * cd * cf + sl * c2d * sf) * s_xz / v;
+                    F[8][c] = -mu0 * (cl * sd * c2f + 2 * sl * sd * cd * sf * cf) * s_xy / v;
+                }
+            }
+    const float xe = xb + p.nx * dx, ye = yb + p.ny * dy;
+    const int ic = (int)std::ceil(((xb + xe) / 2 - xb) / dx), jc = (int)std::ceil(((yb + ye) / 2 - yb) / dy);
+    const int kc = (int)std::ceil((zt - zb) / dz);
+    if (1 <= ic && ic <= p.nx && 1 <= jc && jc <= p.ny && -2 <= kc && kc <= p.nz + 3) {
+        const size_t c = G.idx(kc, ic, jc);
+        const float v = P ? std::sqrt((lam[c] + 2 * mu[c]) / rho[c]) : std::sqrt(mu[c] / rho[c]);
+        return (double)(v / zl);
+    }
+    return 0.0;
+}
+
 int stf_code(const std::string& s) {
     const char* names[] = {"boxcar", "triangle", "herrmann", "kupper", "cosine", "texp"};
     for (int q = 0; q < 6; ++q) if (s == names[q]) return q;
@@ -650,6 +764,7 @@ struct Prepared {
     std::vector<double> smo, smij, sf3, sprm;
     int stf = 0, bf_mode = 0, flags = 0, ntdec_w = 1, ntdec_s = 10;
     std::vector<int> gijk;  // Green's-function points, 1-based
+    std::vector<std::vector<float>> pw_fields;  // plane-wave initial fields (halo arrays), Vx .. Sxy
     bool green_bforce = false;
 };
 
@@ -674,7 +789,16 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     p.vmodel_type = inf.s("vmodel_type", "uni"); p.vcut = inf.r("vcut", 0.0);
     p.munk = inf.b("munk_profile", false);
     p.bf_mode = inf.b("bf_mode", false);
-    if (inf.b("pw_mode", false)) throw std::runtime_error("pw_mode is not supported by this build");
+    p.pw_mode = inf.b("pw_mode", false);
+    if (p.pw_mode) {
+        if (inf.b("green_mode", false)) throw std::runtime_error("pw_mode and green_mode exclude each other");
+        p.pw_ztop = inf.r("pw_ztop", 1e30); p.pw_zlen = inf.r("pw_zlen", -1.0);
+        p.pw_ps = inf.s("pw_ps", "");
+        p.pw_strike = inf.r("pw_strike", 0.0); p.pw_dip = inf.r("pw_dip", 0.0); p.pw_rake = inf.r("pw_rake", 0.0);
+        if (!(p.pw_zlen > 0)) throw std::runtime_error("pw_zlen must be positive");
+        if (p.pw_ps != "p" && p.pw_ps != "P" && p.pw_ps != "s" && p.pw_ps != "S") throw std::runtime_error("pw_ps must be p or s");
+        if (inf.s("abc_type", "pml") != "pml") throw std::runtime_error("pw_mode needs abc_type = pml");
+    }
     p.green_mode = inf.b("green_mode", false);
     if (p.green_mode) {
         p.green_stnm = inf.s("green_stnm", ""); p.green_cmp = inf.s("green_cmp", "");
@@ -732,7 +856,7 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     meta.p = p;
     meta.exedate = (long long)std::time(nullptr);
     // m_source.f90:84-91: no regular source grid in Green's-function mode
-    auto rows = p.green_mode ? std::vector<std::string>() : table_rows(inf.path(p.fn_stf));
+    auto rows = (p.green_mode || p.pw_mode) ? std::vector<std::string>() : table_rows(inf.path(p.fn_stf));
     const std::string& f = p.stf_format;
     struct S0 { double x, y, z, t0, tr, mo, m6[6], f3[3]; };
     std::vector<S0> srcs;
@@ -786,12 +910,16 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
         }
         srcs.push_back(s);
     }
-    if (srcs.empty() && !p.green_mode) throw std::runtime_error("no source grid in " + p.fn_stf);
+    if (srcs.empty() && !p.green_mode && !p.pw_mode) throw std::runtime_error("no source grid in " + p.fn_stf);
     double fcut = 0, M0 = 0;
     for (auto& s : srcs) fcut = std::max(fcut, 1.0 / s.tr);
     double UC = 1e-15;
+    std::vector<std::vector<float>> pw_fields;
     if (p.green_mode) {
         M0 = 1;  // m_green.f90:127; fcut stays 0, source__setup never sets it
+    } else if (p.pw_mode) {
+        M0 = (double)(1.0f / (float)UC);  // fictitious moment for output, single precision (m_source.f90:77)
+        fcut = plane_wave(p, G, rho, lam, mu, pw_fields);
     } else if (p.bf_mode) {
         for (auto& s : srcs) M0 += s.f3[0] * s.f3[0] + s.f3[1] * s.f3[1] + s.f3[2] * s.f3[2];
         M0 = std::sqrt(M0);
@@ -932,6 +1060,7 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     P.stf = stf_code(p.stftype);
     P.bf_mode = p.bf_mode || p.green_mode;  // the Green's-function pseudo source is a body force
     P.gijk = std::move(gijk);
+    P.pw_fields = std::move(pw_fields);
     P.green_bforce = p.green_bforce;
     P.rijk.clear();
     for (auto& st : meta.st) P.rijk.insert(P.rijk.end(), {st.i, st.j, st.k});
@@ -1009,6 +1138,9 @@ int materialize(const Prepared& P, swpc_sim** out) {
         return bail(rc);
     if ((rc = swpc_gpu_set_receivers(sim, (int)P.meta.st.size(), P.rijk.data(), P.ntdec_w, P.flags)))
         return bail(rc);
+    for (int w = 0; w < (int)P.pw_fields.size(); ++w)
+        if ((rc = swpc_gpu_set_field(sim, w, P.pw_fields[w].data()))) return bail(rc);
+    if (!P.pw_fields.empty() && (rc = swpc_gpu_set_plane_wave(sim, 1))) return bail(rc);
     if (!P.gijk.empty() &&
         (rc = swpc_gpu_set_green(sim, (int)P.gijk.size() / 3, P.gijk.data(), P.ntdec_w, P.green_bforce ? 1 : 0)))
         return bail(rc);

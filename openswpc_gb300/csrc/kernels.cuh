@@ -1027,6 +1027,46 @@ __global__ void k_scatter_f(const float* src, float* dst, Geo g, int nf, int f, 
     }
 }
 
+// Fortran halo array (k,i,j) -> one field of a device group, physical
+// columns only (every k of the halo range; the x/y ghost columns stay zero)
+__global__ void k_scatter_cols(const float* src, float* dst, Geo g, int nf, int f) {
+    const long long n = (long long)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(p % (g.nz + 6)) - 3;
+        long long q = p / (g.nz + 6);
+        int i = (int)(q % (g.nx + 6)) - 3;
+        int j = (int)(q / (g.nx + 6)) - 3;
+        if (i < 0 || i >= g.nx || j < 0 || j >= g.ny) continue;
+        dst[goff(g, nf, f, i, j, k)] = src[p];
+    }
+}
+
+// Plane-wave mode: the lateral ghost planes of every field of a group are
+// extrapolated linearly from the two outermost cells before the PML update
+// reads them (src/swpc_3d/m_absorb_p.f90:137-244 for S, 332-427 for V):
+// x sides for j = 1..ny, y sides for i = 1..nx, k = 1..nz; corners untouched.
+__global__ void k_pw_ghost(float* F, Geo g, int nf) {
+    const long long nxs = (long long)g.ny * g.nz, nys = (long long)g.nx * g.nz;
+    const long long n = (2 * nxs + 2 * nys) * nf;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(p % nf);
+        long long q = p / nf;
+        int side;
+        if (q < 2 * nxs) { side = (int)(q / nxs); q %= nxs; }
+        else { q -= 2 * nxs; side = 2 + (int)(q / nys); q %= nys; }
+        const int k = (int)(q % g.nz);
+        const int t = (int)(q / g.nz);  // j for the x sides, i for the y sides (0-based)
+        int gi, i1, i2, gj, j1, j2;
+        switch (side) {
+        case 0: gi = -1; i1 = 0; i2 = 1; gj = j1 = j2 = t; break;
+        case 1: gi = g.nx; i1 = g.nx - 1; i2 = g.nx - 2; gj = j1 = j2 = t; break;
+        case 2: gj = -1; j1 = 0; j2 = 1; gi = i1 = i2 = t; break;
+        default: gj = g.ny; j1 = g.ny - 1; j2 = g.ny - 2; gi = i1 = i2 = t; break;
+        }
+        F[goff(g, nf, f, gi, gj, k)] = 2 * F[goff(g, nf, f, i1, j1, k)] - F[goff(g, nf, f, i2, j2, k)];
+    }
+}
+
 // one field of a device group -> Fortran (nz, nx, ny) physical-grid double array
 __global__ void k_gather_d(const float* src, double* dst, Geo g, int nf, int f) {
     const long long n = (long long)g.nz * g.nx * g.ny;

@@ -60,6 +60,7 @@ struct Sim {
     VmaxArgs vmax_args{};
     std::vector<unsigned int> rep_host;
     bool bf_mode = false, medium_ready = false, diverged = false, profiling = false;
+    bool pw = false;        // plane-wave mode: extrapolate the lateral ghost planes before the PML updates
     int it_done = 0;
 
     struct Pending { int cls; cudaEvent_t a, b; };

@@ -183,6 +183,7 @@ int Sim::launch_step(bool timed) {
     targs.z = z;
     const dim3 tblk(32, TTY);
     const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + TTY - 1) / TTY, (p.nzi + kchunk - 1) / kchunk);
+    if (pw && p.pml) { k_pw_ghost<<<256, 256, 0, stream>>>(V, p.g, 3); ++launches; }
     if (two) {
         cudaEventRecord(ev_fork, stream);
         cudaStreamWaitEvent(stream2, ev_fork, 0);
@@ -211,6 +212,7 @@ int Sim::launch_step(bool timed) {
         k_stressglut<<<(src_args.n + 127) / 128, 128, 0, stream>>>(src_args); ++launches;
         ev1(5, stream);
     }
+    if (pw && p.pml) { k_pw_ghost<<<256, 256, 0, stream>>>(S, p.g, 6); ++launches; }
     if (two) {
         cudaEventRecord(ev_fork2, stream);
         cudaStreamWaitEvent(stream2, ev_fork2, 0);
@@ -464,6 +466,31 @@ int swpc_gpu_add_snapshot(swpc_sim* sim, int section, int kind, int fix, int dec
     if (section >= SWPC_SEC_FS) fix = 1;  // the surface maps choose k per column
     if (fix < 1 || fix > lim) return set_err(SWPC_E_ARG, "snapshot section index outside the grid");
     return s->add_snapshot(section, kind, fix, dec1, dec2, ntdec_s);
+}
+
+int swpc_gpu_set_field(swpc_sim* sim, int which, const float* field) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !field || which < 0 || which > 8) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_field");
+    const Geo& g = s->p.g;
+    const size_t n = (size_t)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
+    float* stage = nullptr;
+    CK(cudaMallocAsync(&stage, n * 4, s->stream));
+    CK(cudaMemcpyAsync(stage, field, n * 4, cudaMemcpyHostToDevice, s->stream));
+    if (which < 3) k_scatter_cols<<<2048, 256, 0, s->stream>>>(stage, s->V, g, 3, which);
+    else k_scatter_cols<<<2048, 256, 0, s->stream>>>(stage, s->S, g, 6, which - 3);
+    ++s->launches;
+    CK(cudaFreeAsync(stage, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return 0;
+}
+
+int swpc_gpu_set_plane_wave(swpc_sim* sim, int on) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    if (on && !s->p.pml) return set_err(SWPC_E_ARG, "plane-wave mode needs the PML absorber");
+    s->pw = on != 0;
+    if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+    return 0;
 }
 
 int swpc_gpu_set_green(swpc_sim* sim, int n, const int* ijk, int ntdec_w, int bforce) {
@@ -1235,6 +1262,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         Sim* s = reinterpret_cast<Sim*>(sims[q]);
         if (!s || !s->medium_ready) return fail(set_err(SWPC_E_STATE, "every member must have its medium uploaded"));
         if (s->variant != 0) return fail(set_err(SWPC_E_ARG, "batched members must use the TMA interior kernels"));
+        if (s->pw) return fail(set_err(SWPC_E_ARG, "plane-wave simulations are not batched"));
         if (q && s->dims.store != b->store) return fail(set_err(SWPC_E_ARG, "batched members must share one storage precision"));
         for (int r = 0; r < q; ++r)
             if (b->sims[r] == s) return fail(set_err(SWPC_E_ARG, "a simulation appears twice in the batch"));

@@ -54,7 +54,7 @@ EXPORTS = [
     "swpc_gpu_get_zchunk", "swpc_batch_create", "swpc_batch_run", "swpc_batch_sync", "swpc_batch_stream",
     "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes", "swpc_gpu_selftest_wait",
     "swpc_gpu_add_snapshot", "swpc_gpu_query_snapshot", "swpc_gpu_fetch_section", "swpc_gpu_set_green",
-    "swpc_gpu_fetch_green", "swpc_host_write_green",
+    "swpc_gpu_fetch_green", "swpc_host_write_green", "swpc_gpu_set_field", "swpc_gpu_set_plane_wave",
     "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
@@ -131,6 +131,8 @@ def lib(build=True):
     L.swpc_gpu_set_green.argtypes = [vp, i, ip, i, i]
     L.swpc_gpu_fetch_green.argtypes = [vp, fp, ip, ip, ip]
     L.swpc_host_write_green.argtypes = [vp, ctypes.c_char_p]
+    L.swpc_gpu_set_field.argtypes = [vp, i, fp]
+    L.swpc_gpu_set_plane_wave.argtypes = [vp, i]
     L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_request_bytes.argtypes = [vp]
     L.swpc_host_request_bytes.restype = ctypes.c_longlong

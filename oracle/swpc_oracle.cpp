@@ -226,6 +226,9 @@ struct Params {
     std::string green_stnm, green_cmp, fn_glst, green_fmt;
     double green_trise, green_maxdist;
     bool green_bforce, stabilize_pml;
+    // plane-wave mode (src/swpc_3d/m_source.f90:316-466)
+    double pw_ztop, pw_zlen, pw_strike, pw_dip, pw_rake;
+    std::string pw_ps;
     bool bf_mode, pw_mode, green_mode, sw_wav_v, sw_wav_u, sw_wav_stress, sw_wav_strain, munk, xy_v, xy_u;
 };
 
@@ -256,7 +259,12 @@ static Params read_params(const Ini& ini) {
     p.pw_mode = ini.logical("pw_mode", false);
     p.green_mode = ini.logical("green_mode", false);
     p.bf_mode = ini.logical("bf_mode", false);
-    if (p.pw_mode) throw std::runtime_error("pw_mode is not supported by the oracle");
+    if (p.pw_mode) {
+        p.pw_ztop = ini.real("pw_ztop", 1e30f); p.pw_zlen = ini.real("pw_zlen", -1.0f);
+        p.pw_ps = ini.str("pw_ps", "");
+        p.pw_strike = ini.real("pw_strike", 0.0f); p.pw_dip = ini.real("pw_dip", 0.0f); p.pw_rake = ini.real("pw_rake", 0.0f);
+        if (!(p.pw_zlen > 0)) throw std::runtime_error("pw_zlen must be positive");
+    }
     if (p.green_mode) {
         p.green_stnm = ini.str("green_stnm", ""); p.green_cmp = ini.str("green_cmp", "");
         p.green_trise = ini.real("green_trise", 1.0); p.green_bforce = ini.logical("green_bforce", false);
@@ -378,8 +386,9 @@ struct Sim : SimBase {
         setup_regions();
         setup_medium(inf_dir, vm5);
         kernel_setup();
-        if (!p.green_mode) source_setup(inf_dir);  // m_source.f90:84-91: no regular source grid
-        else dt_dxyz = (MP)dt / (dx * dy * dz);
+        if (p.pw_mode) pw_setup();
+        else if (!p.green_mode) source_setup(inf_dir);  // m_source.f90:84-91: no regular source grid
+        if (p.green_mode || p.pw_mode) dt_dxyz = (MP)dt / (dx * dy * dz);
         absorb_setup();
         wav_setup(inf_dir);
         if (p.green_mode) green_setup(inf_dir);
@@ -1143,7 +1152,82 @@ struct Sim : SimBase {
     }
 
     // src/swpc_3d/m_absorb_p.f90:126-317 (pw_mode ghost extrapolation excluded)
+    // m_absorb_p.f90:137-244 / 332-427: lateral ghost planes extrapolated
+    // linearly in plane-wave mode (x sides for j = 1..ny, then y sides for
+    // i = 1..nx, k = 1..nz)
+    void pw_ghosts(std::initializer_list<F3<MP>*> fs) {
+        for (F3<MP>* f : fs) {
+            F3<MP>& A = *f;
+            for (int j = jbeg; j <= jend; ++j)
+                for (int k = 1; k <= nz; ++k) {
+                    A(k, 0, j) = 2 * A(k, 1, j) - A(k, 2, j);
+                    A(k, nx + 1, j) = 2 * A(k, nx, j) - A(k, nx - 1, j);
+                }
+            for (int i = ibeg; i <= iend; ++i)
+                for (int k = 1; k <= nz; ++k) {
+                    A(k, i, 0) = 2 * A(k, i, 1) - A(k, i, 2);
+                    A(k, i, ny + 1) = 2 * A(k, i, ny) - A(k, i, ny - 1);
+                }
+        }
+    }
+
+    // m_source.f90:316-466
+    void pw_setup() {
+        const SP d2r = (SP)(PI_D / 180.0);
+        const SP dipr = (SP)p.pw_dip * d2r, strr = (SP)p.pw_strike * d2r, rakr = (SP)p.pw_rake * d2r;
+        const SP sd = std::sin(dipr), cd = std::cos(dipr), sf = std::sin(strr), cf = std::cos(strr);
+        const SP sl = std::sin(rakr), cl = std::cos(rakr), c2d = std::cos(2 * dipr), c2f = std::cos(2 * strr);
+        const bool P = p.pw_ps == "p" || p.pw_ps == "P";
+        const int stt = stf_code(p.stftype);
+        const SP zt = (SP)p.pw_ztop, zl = (SP)p.pw_zlen, eps = std::numeric_limits<float>::epsilon();
+        for (int j = jbeg_m; j <= jend_m; ++j)
+            for (int i = ibeg_m; i <= iend_m; ++i)
+                for (int k = kbeg_m; k <= kend_m; ++k) {
+                    const SP v = P ? std::sqrt((lam(k, i, j) + 2 * mu(k, i, j)) / rho(k, i, j)) : std::sqrt(mu(k, i, j) / rho(k, i, j));
+                    if (v < eps) continue;
+                    const SP x0 = xbeg + (SP)(i - (SP)0.5) * (SP)dx, y0 = ybeg + (SP)(j - (SP)0.5) * (SP)dy;
+                    const SP z0 = zbeg + (SP)(k - (SP)0.5) * (SP)dz - zt;
+                    const SP x1 = x0 + (SP)dx / (SP)2, y1 = y0 + (SP)dy / (SP)2, z1 = z0 + (SP)dz / (SP)2;
+                    const SP sh = dt / (SP)2 * v;
+                    auto m = [&](SP a) { return momentrate<SP>(a, stt, (SP)0, zl); };
+                    const SP s_ii = m(sd * sf * x0 - sd * cf * y0 + cd * z0);
+                    const SP s_vx = m(sd * sf * x1 - sd * cf * y0 + cd * z0 + sh);
+                    const SP s_vy = m(sd * sf * x0 - sd * cf * y1 + cd * z0 + sh);
+                    const SP s_vz = m(sd * sf * x0 - sd * cf * y0 + cd * z1 + sh);
+                    const SP s_yz = m(sd * sf * x0 - sd * cf * y1 + cd * z1);
+                    const SP s_xz = m(sd * sf * x1 - sd * cf * y0 + cd * z1);
+                    const SP s_xy = m(sd * sf * x1 - sd * cf * y1 + cd * z0);
+                    const SP la0 = lam(k, i, j), mu0 = mu(k, i, j);
+                    if (P) {
+                        Vx(k, i, j) = -sd * sf * s_vx; Vy(k, i, j) = sd * cf * s_vy; Vz(k, i, j) = -cd * s_vz;
+                        Sxx(k, i, j) = -(la0 + 2 * mu0 * sd * sd * sf * sf) * s_ii / v;
+                        Syy(k, i, j) = -(la0 + 2 * mu0 * sd * sd * cf * cf) * s_ii / v;
+                        Szz(k, i, j) = -(la0 + 2 * mu0 * cd * cd) * s_ii / v;
+                        Syz(k, i, j) = 2 * mu0 * sd * cd * cf * s_yz / v;
+                        Sxz(k, i, j) = -2 * mu0 * sd * cd * sf * s_xz / v;
+                        Sxy(k, i, j) = 2 * mu0 * sd * cd * sf * s_xy / v;
+                    } else {
+                        Vx(k, i, j) = (cl * cf + sl * cd * sf) * s_vx; Vy(k, i, j) = (cl * sf - sl * cd * cf) * s_vy;
+                        Vz(k, i, j) = -sl * sd * s_vz;
+                        Sxx(k, i, j) = 2 * mu0 * sd * sf * (cl * cf + sl * cd * sf) * s_ii / v;
+                        Syy(k, i, j) = -2 * mu0 * sd * cf * (cl * sf - sl * cd * cf) * s_ii / v;
+                        Szz(k, i, j) = -2 * mu0 * cd * sl * sd * s_ii / v;
+                        Syz(k, i, j) = mu0 * (cl * cd * sf - sl * c2d * cf) * s_yz / v;
+                        Sxz(k, i, j) = mu0 * (cl * cd * cf + sl * c2d * sf) * s_xz / v;
+                        Sxy(k, i, j) = -mu0 * (cl * sd * c2f + 2 * sl * sd * cd * sf * cf) * s_xy / v;
+                    }
+                }
+        const int ic = x2i((xbeg + xend) / 2, xbeg, (SP)dx), jc = x2i((ybeg + yend) / 2, ybeg, (SP)dy);
+        const int kc = x2i(zt, zbeg, (SP)dz);
+        fcut = 0;
+        if (ibeg <= ic && ic <= iend && jbeg <= jc && jc <= jend)
+            fcut = (float)((P ? std::sqrt((lam(kc, ic, jc) + 2 * mu(kc, ic, jc)) / rho(kc, ic, jc))
+                              : std::sqrt(mu(kc, ic, jc) / rho(kc, ic, jc))) / zl);
+        M0 = 1.0f / UC;  // fictitious moment for output
+    }
+
     void pml_vel() {
+        if (p.pw_mode) pw_ghosts({&Sxx, &Syy, &Szz, &Syz, &Sxz, &Sxy});
 #pragma omp parallel for schedule(dynamic)
         for (int j = jbeg; j <= jend; ++j)
             for (int i = ibeg; i <= iend; ++i)
@@ -1184,6 +1268,7 @@ struct Sim : SimBase {
 
     // src/swpc_3d/m_absorb_p.f90:319-531
     void pml_stress() {
+        if (p.pw_mode) pw_ghosts({&Vx, &Vy, &Vz});
         const SP epsl = std::numeric_limits<float>::epsilon();
 #pragma omp parallel for schedule(dynamic)
         for (int j = jbeg; j <= jend; ++j)
