@@ -135,8 +135,7 @@ int swpc_gpu_set_field(swpc_sim* sim, int which, const float* field);
 
 /* Plane-wave mode (pw_mode): before each PML update the lateral ghost
  * planes are extrapolated linearly from the two outermost cells
- * (m_absorb_p.f90:137-244, 332-427).  Needs the PML absorber; such
- * simulations are not batched. */
+ * (m_absorb_p.f90:137-244, 332-427).  Needs the PML absorber. */
 int swpc_gpu_set_plane_wave(swpc_sim* sim, int on);
 
 /* Reciprocal Green's-function taps (green__store, m_green.f90:406-551): n

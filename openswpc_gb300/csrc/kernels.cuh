@@ -597,16 +597,21 @@ __device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
 }
 
 // one thread per shell point; batched: block b covers points
-// [256 e.y, 256 e.y + 256) of simulation e.x, e = blocks[b]
-__global__ void __launch_bounds__(256) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * 256LL + threadIdx.x); }
-__global__ void __launch_bounds__(256) k_vel_pml(const PArgs a) { vel_pml_pt(a, blockIdx.x * 256LL + threadIdx.x); }
-__global__ void __launch_bounds__(256) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+// [PTPB e.y, PTPB e.y + PTPB) of simulation e.x, e = blocks[b]
+// threads (shell points) per block of the PML kernels
+#ifndef PML_TPB
+#define PML_TPB 256
+#endif
+constexpr int PTPB = PML_TPB;
+__global__ void __launch_bounds__(PTPB) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
+__global__ void __launch_bounds__(PTPB) k_vel_pml(const PArgs a) { vel_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
+__global__ void __launch_bounds__(PTPB) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
     const int2 e = blocks[blockIdx.x];
-    stress_pml_pt(all[e.x], e.y * 256LL + threadIdx.x);
+    stress_pml_pt(all[e.x], e.y * (long long)PTPB + threadIdx.x);
 }
-__global__ void __launch_bounds__(256) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+__global__ void __launch_bounds__(PTPB) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
     const int2 e = blocks[blockIdx.x];
-    vel_pml_pt(all[e.x], e.y * 256LL + threadIdx.x);
+    vel_pml_pt(all[e.x], e.y * (long long)PTPB + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------

@@ -190,7 +190,7 @@ int Sim::launch_step(bool timed) {
     }
     if (p.pml) {
         ev0(2, sp);
-        k_stress_pml<<<(unsigned)((p.npml + 255) / 256), 256, 0, sp>>>(pml_args); ++launches;
+        k_stress_pml<<<(unsigned)((p.npml + PTPB - 1) / PTPB), PTPB, 0, sp>>>(pml_args); ++launches;
         ev1(2, sp);
         if (two) cudaEventRecord(ev_join, stream2);
     }
@@ -219,7 +219,7 @@ int Sim::launch_step(bool timed) {
     }
     if (p.pml) {
         ev0(3, sp);
-        k_vel_pml<<<(unsigned)((p.npml + 255) / 256), 256, 0, sp>>>(pml_args); ++launches;
+        k_vel_pml<<<(unsigned)((p.npml + PTPB - 1) / PTPB), PTPB, 0, sp>>>(pml_args); ++launches;
         ev1(3, sp);
         if (two) cudaEventRecord(ev_join2, stream2);
     }
@@ -1176,6 +1176,7 @@ struct Batch {
     SnapArgs* d_snap = nullptr;
     GreenArgs* d_green = nullptr;
     int max_green = 0;
+    std::vector<Sim*> pw_members;  // plane-wave members: lateral ghost extrapolation before the PML updates
     VmaxArgs* d_vmax = nullptr;
     int** d_its = nullptr;
     int4* d_tblocks = nullptr;
@@ -1209,10 +1210,11 @@ struct Batch {
         if (max_green) { k_green_batch<<<dim3((max_green + 127) / 128, n), 128, 0, stream>>>(d_green); ++launches; }
         if (any_snap) { k_snap_batch<<<dim3((max_pix + 127) / 128, max_planes, n), 128, 0, stream>>>(d_snap); ++launches; }
         const dim3 tblk(32, TTY);
+        for (Sim* m : pw_members) { k_pw_ghost<<<256, 256, 0, stream>>>(m->V, m->p.g, 3); ++launches; }
         if (n_pblocks) {
             cudaEventRecord(ev[0], stream);
             cudaStreamWaitEvent(stream2, ev[0], 0);
-            k_stress_pml_batch<<<n_pblocks, 256, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
+            k_stress_pml_batch<<<n_pblocks, PTPB, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
             cudaEventRecord(ev[1], stream2);
         }
         if (rbytes == 4) k_stress_tma_batch<float><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
@@ -1221,10 +1223,11 @@ struct Batch {
         ++launches;
         if (n_pblocks) cudaStreamWaitEvent(stream, ev[1], 0);
         if (any_mt) { k_stressglut_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
+        for (Sim* m : pw_members) { k_pw_ghost<<<256, 256, 0, stream>>>(m->S, m->p.g, 6); ++launches; }
         if (n_pblocks) {
             cudaEventRecord(ev[2], stream);
             cudaStreamWaitEvent(stream2, ev[2], 0);
-            k_vel_pml_batch<<<n_pblocks, 256, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
+            k_vel_pml_batch<<<n_pblocks, PTPB, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
             cudaEventRecord(ev[3], stream2);
         }
         k_vel_tma_batch<<<n_tblocks, tblk, smem_vel, stream>>>(d_targs, d_tblocks); ++launches;
@@ -1262,7 +1265,6 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         Sim* s = reinterpret_cast<Sim*>(sims[q]);
         if (!s || !s->medium_ready) return fail(set_err(SWPC_E_STATE, "every member must have its medium uploaded"));
         if (s->variant != 0) return fail(set_err(SWPC_E_ARG, "batched members must use the TMA interior kernels"));
-        if (s->pw) return fail(set_err(SWPC_E_ARG, "plane-wave simulations are not batched"));
         if (q && s->dims.store != b->store) return fail(set_err(SWPC_E_ARG, "batched members must share one storage precision"));
         for (int r = 0; r < q; ++r)
             if (b->sims[r] == s) return fail(set_err(SWPC_E_ARG, "a simulation appears twice in the batch"));
@@ -1299,6 +1301,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         sn[q] = s->snap_args;
         gr[q] = s->green_args;
         b->max_green = std::max(b->max_green, s->green_args.n);
+        if (s->pw && s->p.pml) b->pw_members.push_back(s);
         vm[q] = s->vmax_args;
         its[q] = s->d_it;
         const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + TTY - 1) / TTY, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
@@ -1306,7 +1309,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
             for (int by = 0; by < gy; ++by)
                 for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
         if (s->p.pml)
-            for (long long bk = 0; bk < (s->p.npml + 255) / 256; ++bk) pb.push_back(make_int2(q, (int)bk));
+            for (long long bk = 0; bk < (s->p.npml + PTPB - 1) / PTPB; ++bk) pb.push_back(make_int2(q, (int)bk));
         b->max_nst = std::max(b->max_nst, s->tap_args.n);
         b->max_src = std::max(b->max_src, s->src_args.n);
         if (s->src_args.n > 0) { if (s->bf_mode) b->any_bf = true; else b->any_mt = true; }

@@ -38,3 +38,22 @@ def test_plane_wave_host_setup(tmp_path):
     assert h["nsrc"] == 0
     assert abs(h["fcut"] - o.fcut) < 1e-6 * o.fcut
     assert h["M0"] == np.float32(o.M0)
+
+
+@pytest.mark.gpu
+def test_plane_wave_batched_equals_alone(tmp_path):
+    inf = configs.write_plane_wave(str(tmp_path), ps="s", nt=120)
+    a = gpu.Simulation.from_inf(inf)
+    a.run(1, 120)
+    a.sync()
+    alone = a.waveforms()
+    a.close()
+    sims = [gpu.Simulation.from_inf(inf), gpu.Simulation.from_inf(inf)]
+    b = gpu.Batch(sims)
+    b.run(120)
+    b.sync()
+    for q in sims:
+        assert np.array_equal(q.waveforms(), alone)
+    b.close()
+    for q in sims:
+        q.close()
