@@ -600,7 +600,7 @@ __device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
 // [PTPB e.y, PTPB e.y + PTPB) of simulation e.x, e = blocks[b]
 // threads (shell points) per block of the PML kernels
 #ifndef PML_TPB
-#define PML_TPB 256
+#define PML_TPB 128
 #endif
 constexpr int PTPB = PML_TPB;
 __global__ void __launch_bounds__(PTPB) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
