@@ -99,6 +99,16 @@ int swpc_gpu_upload_medium(swpc_sim* sim, const float* rho, const float* lam, co
                            const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot,
                            const int* kob_top, const int* kob_bot, const double* ts);
 
+/* The same upload for a medium that depends on depth only (the uni, lhm
+ * and lgm models of m_vmodel_*): rho .. taus are single columns of nz+6
+ * values (k = -2 .. nz+3) after the medium post-processing, which the device
+ * copies into every (i, j); the surface maps are full 2-D arrays as above.
+ * Spares the host building and sending nx*ny copies of the column. */
+int swpc_gpu_upload_medium_column(swpc_sim* sim, const float* rho, const float* lam, const float* mu,
+                                  const float* taup, const float* taus,
+                                  const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot,
+                                  const int* kob_top, const int* kob_bot, const double* ts);
+
 /* Sources (replaces source__stressglut / source__bodyforce state,
  * m_source.f90:26-36).  ijk: 3n grid indices.  mo: n normalised moments
  * (mo/M0).  mij: 6n components xx yy zz yz xz xy.  fxyz: 3n normalised body

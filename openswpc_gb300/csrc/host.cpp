@@ -757,7 +757,9 @@ std::string tar_entry(const std::string& name, const std::string& data, long lon
 struct Prepared {
     Meta meta;
     swpc_dims d{};
-    std::vector<float> rho, lam, mu, tp, tsv;
+    std::vector<float> rho, lam, mu, tp, tsv;   // full halo arrays, or empty in column mode
+    bool colmode = false;
+    std::vector<float> col[5];                  // column mode: one processed column per field
     std::vector<int> kfs, kob, kft, kfb, kot, kobb;
     double ts[3] = {0, 0, 0};
     std::vector<int> sijk, rijk;
@@ -843,13 +845,55 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     Grid G{p.nx, p.ny, p.nz};
     std::vector<float> rho, lam, mu, tp, tsv;
     double bd0 = 0;
-    vmodel(inf, p, G, rho, lam, mu, tp, tsv, bd0);
     std::vector<int> kfs(G.n2()), kob(G.n2()), kft(G.n2()), kfb(G.n2()), kot(G.n2()), kobb(G.n2());
     double ts[3];
-    medium_post(p.nx, p.ny, p.nz, p.na, p.fq_min, p.fq_max, p.fq_ref, rho.data(), lam.data(),
-                mu.data(), tp.data(), tsv.data(), kfs.data(), kob.data(), kft.data(), kfb.data(), kot.data(), kobb.data(), ts);
-    if (inf.b("stabilize_pml", false))  // m_medium.f90:218-222, after surface detection
-        stabilize_absorber(p.nx, p.ny, p.nz, p.na, rho.data(), lam.data(), mu.data(), tp.data(), tsv.data(), kfs.data());
+    // Depth-only models (uni, lhm, lgm) give the same processed column at
+    // every (i, j): the medium set-up runs on a small grid of the same depth,
+    // one column of it goes to the device, which spreads it over the grid
+    // (swpc_gpu_upload_medium_column).  Models that vary laterally, the
+    // absorber conditioning and the plane-wave set-up keep full host arrays.
+    const bool stabilize = inf.b("stabilize_pml", false);
+    const bool colmode = (p.vmodel_type == "uni" || p.vmodel_type == "lhm" || p.vmodel_type == "lgm") && !stabilize &&
+                         !p.pw_mode;
+    std::vector<float> col[5];  // processed column k = -2 .. nz+3: rho lam mu taup taus
+    if (colmode) {
+        const int nr = 2 * p.na + 6, ic = p.na + 3;
+        Params pr = p;
+        pr.nx = pr.ny = nr;
+        Grid Gr{nr, nr, p.nz};
+        std::vector<float> r5[5];
+        vmodel(inf, pr, Gr, r5[0], r5[1], r5[2], r5[3], r5[4], bd0);
+        std::vector<int> m6[6];
+        for (auto& m : m6) m.assign(Gr.n2(), 0);
+        medium_post(nr, nr, p.nz, p.na, p.fq_min, p.fq_max, p.fq_ref, r5[0].data(), r5[1].data(), r5[2].data(),
+                    r5[3].data(), r5[4].data(), m6[0].data(), m6[1].data(), m6[2].data(), m6[3].data(), m6[4].data(),
+                    m6[5].data(), ts);
+        for (int f = 0; f < 5; ++f) {
+            col[f].resize(p.nz + 6);
+            for (int k = -2; k <= p.nz + 3; ++k) col[f][k + 2] = r5[f][Gr.idx(k, ic, ic)];
+        }
+        // the maps as the surface detection fills them over the full grid
+        const int v_fs = m6[0][Gr.idx2(ic, ic)], v_ob = m6[1][Gr.idx2(ic, ic)];
+        for (int j = 0; j <= p.ny + 2; ++j)
+            for (int i = 0; i <= p.nx + 2; ++i) { kfs[G.idx2(i, j)] = v_fs; kob[G.idx2(i, j)] = v_ob; }
+        for (int j = 1; j <= p.ny; ++j)
+            for (int i = 1; i <= p.nx; ++i) {
+                const size_t q = G.idx2(i, j), r = Gr.idx2(ic, ic);
+                kft[q] = m6[2][r]; kfb[q] = std::min(m6[3][r], p.nz); kot[q] = m6[4][r]; kobb[q] = std::min(m6[5][r], p.nz);
+            }
+    } else {
+        vmodel(inf, p, G, rho, lam, mu, tp, tsv, bd0);
+        medium_post(p.nx, p.ny, p.nz, p.na, p.fq_min, p.fq_max, p.fq_ref, rho.data(), lam.data(),
+                    mu.data(), tp.data(), tsv.data(), kfs.data(), kob.data(), kft.data(), kfb.data(), kot.data(), kobb.data(), ts);
+        if (stabilize)  // m_medium.f90:218-222, after surface detection
+            stabilize_absorber(p.nx, p.ny, p.nz, p.na, rho.data(), lam.data(), mu.data(), tp.data(), tsv.data(), kfs.data());
+    }
+    // medium value f (0 rho, 1 lam, 2 mu) at cell (k, i, j) in either form
+    auto medv = [&](int f, int k, int i, int j) -> float {
+        if (colmode) return col[f][k + 2];
+        const std::vector<float>& a = f == 0 ? rho : f == 1 ? lam : mu;
+        return a[G.idx(k, i, j)];
+    };
 
     // sources (src/swpc_3d/m_source.f90:41-314, 468-774)
     Meta meta;
@@ -897,7 +941,7 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
                 sdr2moment(R(7) - p.phi, R(8), R(9), s.m6);
                 int is = x2i(s.x, p.xbeg, p.dx), js = x2i(s.y, p.ybeg, p.dy), ks = x2i(s.z, p.zbeg, p.dz);
                 s.mo = (is >= -2 && is <= p.nx + 3 && js >= -2 && js <= p.ny + 3 && ks >= -2 && ks <= p.nz + 3)
-                           ? 1e9 * mu[G.idx(ks, is, js)] * D * Sa : 0.0;
+                           ? 1e9 * medv(2, ks, is, js) * D * Sa : 0.0;
             } else {
                 throw std::runtime_error("invalid source type " + f);
             }
@@ -1052,6 +1096,8 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     meta.flags = flags;
 
     P.rho = std::move(rho); P.lam = std::move(lam); P.mu = std::move(mu); P.tp = std::move(tp); P.tsv = std::move(tsv);
+    P.colmode = colmode;
+    for (int f = 0; f < 5; ++f) P.col[f] = std::move(col[f]);
     P.kfs = std::move(kfs); P.kob = std::move(kob); P.kft = std::move(kft); P.kfb = std::move(kfb);
     P.kot = std::move(kot); P.kobb = std::move(kobb);
     for (int m = 0; m < 3; ++m) P.ts[m] = ts[m];
@@ -1068,6 +1114,12 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     P.ntdec_w = std::max(1, p.ntdec_w);
     P.ntdec_s = p.ntdec_s;
     meta.bd0 = bd0;
+    // the medium now lives in P: read it there
+    auto pmedv = [&](int f, int k, int i, int j) -> float {
+        if (P.colmode) return P.col[f][k + 2];
+        const std::vector<float>& a = f == 0 ? P.rho : f == 1 ? P.lam : P.mu;
+        return a[G.idx(k, i, j)];
+    };
     {  // snap__setup and newfile_* (m_snap.f90:131-160, 324-473)
         const int idec = p.idec, jdec = p.jdec, kdec = p.kdec;
         const int nxs = (p.nx + idec / 2) / idec, nys = (p.ny + jdec / 2) / jdec, nzs = (p.nz + kdec / 2) / kdec;
@@ -1110,10 +1162,10 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
                         i = ca; j = cb;
                         k = sec == SWPC_SEC_XY ? S.fix : (sec == SWPC_SEC_FS ? P.kfs : P.kob)[G.idx2(i, j)] + 1;
                     }
-                    const size_t q = (size_t)(b - 1) * S.n1 + (a - 1), c = G.idx(k, i, j);
-                    S.med[q] = P.rho[c];
-                    S.med[pl + q] = P.lam[c];
-                    S.med[2 * pl + q] = P.mu[c];
+                    const size_t q = (size_t)(b - 1) * S.n1 + (a - 1);
+                    S.med[q] = pmedv(0, k, i, j);
+                    S.med[pl + q] = pmedv(1, k, i, j);
+                    S.med[2 * pl + q] = pmedv(2, k, i, j);
                 }
             meta.snaps.push_back(std::move(S));
         }
@@ -1129,10 +1181,15 @@ int materialize(const Prepared& P, swpc_sim** out) {
     int rc = swpc_gpu_create(&P.d, &sim);
     if (rc) return rc;
     auto bail = [&](int code) { swpc_gpu_destroy(sim); return code; };
-    if ((rc = swpc_gpu_upload_medium(sim, P.rho.data(), P.lam.data(), P.mu.data(), P.tp.data(), P.tsv.data(),
-                                     P.kfs.data(), P.kob.data(), P.kft.data(), P.kfb.data(), P.kot.data(),
-                                     P.kobb.data(), P.ts)))
-        return bail(rc);
+    if (P.colmode)
+        rc = swpc_gpu_upload_medium_column(sim, P.col[0].data(), P.col[1].data(), P.col[2].data(), P.col[3].data(),
+                                           P.col[4].data(), P.kfs.data(), P.kob.data(), P.kft.data(), P.kfb.data(),
+                                           P.kot.data(), P.kobb.data(), P.ts);
+    else
+        rc = swpc_gpu_upload_medium(sim, P.rho.data(), P.lam.data(), P.mu.data(), P.tp.data(), P.tsv.data(),
+                                    P.kfs.data(), P.kob.data(), P.kft.data(), P.kfb.data(), P.kot.data(),
+                                    P.kobb.data(), P.ts);
+    if (rc) return bail(rc);
     if ((rc = swpc_gpu_set_sources(sim, (int)P.smo.size(), P.sijk.data(), P.smo.data(), P.smij.data(), P.sf3.data(),
                                    P.sprm.data(), P.stf, P.bf_mode)))
         return bail(rc);

@@ -1032,6 +1032,20 @@ __global__ void k_scatter_f(const float* src, float* dst, Geo g, int nf, int f, 
     }
 }
 
+// Depth-only medium: five columns of nz + 6 values (k = -2 .. nz+3; rho lam
+// mu taup taus) copied into every (i, j) of the halo grid of the M group.
+__global__ void k_spread_col(const float* col, float* M, Geo g) {
+    const long long nk = g.nz + 6;
+    const long long n = nk * (g.nx + 6) * (g.ny + 6);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(p % nk) - 3;
+        long long q = p / nk;
+        int i = (int)(q % (g.nx + 6)) - 3;
+        int j = (int)(q / (g.nx + 6)) - 3;
+        for (int f = 0; f < 5; ++f) M[goff(g, 5, f, i, j, k)] = col[f * nk + k + 3];
+    }
+}
+
 // Fortran halo array (k,i,j) -> one field of a device group, physical
 // columns only (every k of the halo range; the x/y ghost columns stay zero)
 __global__ void k_scatter_cols(const float* src, float* dst, Geo g, int nf, int f) {

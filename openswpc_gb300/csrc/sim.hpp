@@ -74,7 +74,7 @@ struct Sim {
     int allocate();
     int upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
                       const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
-                      const int* kob_bot, const double* ts);
+                      const int* kob_bot, const double* ts, bool column);
     int set_sources(int n, const int* ijk, const double* mo, const double* mij, const double* fxyz, const double* prm,
                     int stftype, bool bf);
     int set_receivers(int n, const int* ijk, int ntdec_w, int flags);

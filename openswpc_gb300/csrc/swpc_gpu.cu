@@ -427,7 +427,16 @@ int swpc_gpu_upload_medium(swpc_sim* sim, const float* rho, const float* lam, co
     if (!s || !rho || !lam || !mu || !taup || !taus || !kob || !kfs_top || !kfs_bot || !kob_top || !kob_bot || !ts)
         return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium");
     if (!kfs) return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium");
-    return s->upload_medium(rho, lam, mu, taup, taus, kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts);
+    return s->upload_medium(rho, lam, mu, taup, taus, kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts, false);
+}
+
+int swpc_gpu_upload_medium_column(swpc_sim* sim, const float* rho, const float* lam, const float* mu, const float* taup,
+                                  const float* taus, const int* kfs, const int* kob, const int* kfs_top,
+                                  const int* kfs_bot, const int* kob_top, const int* kob_bot, const double* ts) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !rho || !lam || !mu || !taup || !taus || !kfs || !kob || !kfs_top || !kfs_bot || !kob_top || !kob_bot || !ts)
+        return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium_column");
+    return s->upload_medium(rho, lam, mu, taup, taus, kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts, true);
 }
 
 int swpc_gpu_set_sources(swpc_sim* sim, int n, const int* ijk, const double* mo, const double* mij, const double* fxyz,
@@ -864,18 +873,29 @@ int Sim::allocate() {
 
 int Sim::upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
                        const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
-                       const int* kob_bot, const double* ts) {
+                       const int* kob_bot, const double* ts, bool column) {
     const Geo& g = p.g;
-    const size_t n3 = (size_t)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
-    float* stage = nullptr;
-    CK(cudaMallocAsync((void**)&stage, n3 * 4, stream));
     const float* fields[5] = {rho, lam, mu, taup, taus};
-    for (int f = 0; f < 5; ++f) {
-        CK(cudaMemcpyAsync(stage, fields[f], n3 * 4, cudaMemcpyHostToDevice, stream));
-        k_scatter_f<<<2048, 256, 0, stream>>>(stage, M, g, 5, f, 0, nullptr);
+    if (column) {  // one column of nz + 6 values per field, spread over every (i, j) on the device
+        const size_t nc = (size_t)g.nz + 6;
+        float* stage = nullptr;
+        CK(cudaMallocAsync((void**)&stage, 5 * nc * 4, stream));
+        for (int f = 0; f < 5; ++f)
+            CK(cudaMemcpyAsync(stage + f * nc, fields[f], nc * 4, cudaMemcpyHostToDevice, stream));
+        k_spread_col<<<2048, 256, 0, stream>>>(stage, M, g);
         ++launches;
+        CK(cudaFreeAsync(stage, stream));
+    } else {
+        const size_t n3 = (size_t)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
+        float* stage = nullptr;
+        CK(cudaMallocAsync((void**)&stage, n3 * 4, stream));
+        for (int f = 0; f < 5; ++f) {
+            CK(cudaMemcpyAsync(stage, fields[f], n3 * 4, cudaMemcpyHostToDevice, stream));
+            k_scatter_f<<<2048, 256, 0, stream>>>(stage, M, g, 5, f, 0, nullptr);
+            ++launches;
+        }
+        CK(cudaFreeAsync(stage, stream));
     }
-    CK(cudaFreeAsync(stage, stream));
     // band table over the interior columns and the kob map
     const int mx = g.nx + 6;
     auto at = [&](const int* m, int i, int j) { return m[(size_t)(j + 2) * mx + (i + 2)]; };  // 1-based i, j

@@ -55,6 +55,7 @@ EXPORTS = [
     "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes", "swpc_gpu_selftest_wait",
     "swpc_gpu_add_snapshot", "swpc_gpu_query_snapshot", "swpc_gpu_fetch_section", "swpc_gpu_set_green",
     "swpc_gpu_fetch_green", "swpc_host_write_green", "swpc_gpu_set_field", "swpc_gpu_set_plane_wave",
+    "swpc_gpu_upload_medium_column",
     "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
@@ -133,6 +134,7 @@ def lib(build=True):
     L.swpc_host_write_green.argtypes = [vp, ctypes.c_char_p]
     L.swpc_gpu_set_field.argtypes = [vp, i, fp]
     L.swpc_gpu_set_plane_wave.argtypes = [vp, i]
+    L.swpc_gpu_upload_medium_column.argtypes = [vp] + [fp] * 5 + [ip] * 6 + [dp]
     L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_request_bytes.argtypes = [vp]
     L.swpc_host_request_bytes.restype = ctypes.c_longlong
@@ -316,6 +318,18 @@ class Simulation:
         code = FIELDS.index(name) if name in FIELDS else 9 + MEDIUM_FIELDS.index(name)
         _ck(lib().swpc_gpu_fetch_field(self._h, code, out.ctypes.data))
         return out
+
+    def set_field(self, name, halo):
+        """Overwrite a state field from a (ny+6, nx+6, nz+6) halo-grid array
+        (Fortran A(k,i,j)): the physical columns including the z halo planes
+        are taken, the x/y ghost columns stay zero."""
+        d = self.dims
+        if d is None:
+            raise SwpcError(-1, "set_field() needs the dims the simulation was created with")
+        a = np.ascontiguousarray(halo, dtype=np.float32)
+        if a.shape != (d.ny + 6, d.nx + 6, d.nz + 6):
+            raise SwpcError(-1, "set_field(): expected shape %s" % ((d.ny + 6, d.nx + 6, d.nz + 6),))
+        _ck(lib().swpc_gpu_set_field(self._h, FIELDS.index(name), a.ctypes.data))
 
     def field_static(self, name):
         """field() through the library's fixed scratch array: no device

@@ -64,6 +64,7 @@ def lib():
         L.oracle_stations.argtypes = [vp, ctypes.c_void_p]
         L.oracle_field.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
         L.oracle_medium.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_set_field.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
         L.oracle_vmax.argtypes = [vp, ctypes.c_void_p]
         L.oracle_snap_xy_v.argtypes = [vp, ctypes.c_void_p]
         L.oracle_snap.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
@@ -127,6 +128,15 @@ class Oracle:
         if self._L.oracle_field(self.h, FIELDS.index(name), out.ctypes.data) != 0:
             raise RuntimeError(self._L.oracle_last_error().decode())
         return out
+
+    def set_field(self, name, halo):
+        """Overwrite a state field from a (ny+6, nx+6, nz+6) halo-grid
+        array: the physical columns including the z halo planes are taken,
+        the x/y ghost columns are zeroed."""
+        a = np.ascontiguousarray(halo, dtype=np.float32)
+        assert a.shape == (self.ny + 6, self.nx + 6, self.nz + 6)
+        if self._L.oracle_set_field(self.h, FIELDS.index(name), a.ctypes.data) != 0:
+            raise RuntimeError(self._L.oracle_last_error().decode())
 
     def medium(self, name):
         w = MEDIA.index(name)

@@ -318,6 +318,7 @@ struct SimBase {
     virtual int get_sources(int* ijk, double* vals) = 0;
     virtual void step(int it) = 0;
     virtual void get_field(int which, double* out) = 0;
+    virtual void set_field(int which, const float* halo) = 0;
     virtual void get_medium(int which, float* out) = 0;
     virtual int green_out(int* ng_ncmp_ntw, float* out) = 0;
     Params p;
@@ -1583,6 +1584,22 @@ struct Sim : SimBase {
         size_t q = 0;
         for (int j = 1; j <= ny; ++j) for (int i = 1; i <= nx; ++i) for (int k = 1; k <= nz; ++k) out[q++] = (double)A(k, i, j);
     }
+    // overwrite one state field from a halo-grid array A(k,i,j) (k fastest):
+    // every cell of the physical columns i in [1,nx], j in [1,ny] including
+    // the z halo planes; the x/y ghost columns stay zero, as after a halo
+    // exchange on a single rank
+    void set_field(int which, const float* halo) override {
+        F3<MP>* f[9] = {&Vx, &Vy, &Vz, &Sxx, &Syy, &Szz, &Syz, &Sxz, &Sxy};
+        if (which < 0 || which >= 9) throw std::runtime_error("bad field id");
+        F3<MP>& A = *f[which];
+        const long hk = nz + 6, hki = hk * (nx + 6);
+        for (int j = A.jb; j <= A.je; ++j)
+            for (int i = A.ib; i <= A.ie; ++i)
+                for (int k = A.kb; k <= A.ke; ++k) {
+                    const bool phys = i >= 1 && i <= nx && j >= 1 && j <= ny && k >= -2 && k <= nz + 3;
+                    A(k, i, j) = phys ? (MP)halo[(size_t)(j + 2) * hki + (size_t)(i + 2) * hk + (k + 2)] : MP(0);
+                }
+    }
     // medium / maps over the halo grid [-2..nz+3]x[-2..nx+3]x[-2..ny+3]
     void get_medium(int which, float* out) override {
         F3<SP>* f[5] = {&rho, &lam, &mu, &taup, &taus};
@@ -1681,6 +1698,9 @@ void oracle_stations(void* h, int* ijk) {
 
 int oracle_field(void* h, int which, double* out) {
     try { ((SimBase*)h)->get_field(which, out); return 0; } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+int oracle_set_field(void* h, int which, const float* halo) {
+    try { ((SimBase*)h)->set_field(which, halo); return 0; } catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
 int oracle_medium(void* h, int which, float* out) {
     try { ((SimBase*)h)->get_medium(which, out); return 0; } catch (const std::exception& e) { g_err = e.what(); return -1; }
