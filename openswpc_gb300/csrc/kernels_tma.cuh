@@ -85,11 +85,24 @@ struct StressSmem {
     int bad;
 };
 
+// Velocity kernel S ring: planes k .. k+2 are live (the tile of plane k for
+// the x/y stencils, single values of k+1 and k+2 for the z stencil rolled in
+// registers), the other VRING - 3 slots are in flight.  VRING = 5 keeps the
+// block at 74 KB so three blocks fit on an SM.
+#ifndef VEL_RING
+#define VEL_RING 5
+#endif
+#ifndef VEL_MINB
+#define VEL_MINB 3
+#endif
+constexpr int VRING = VEL_RING;
+constexpr int VMINB = VEL_MINB;
+static_assert(VRING >= 5, "the velocity S ring needs planes k-2 .. k+2 at start-up");
 struct VelSmem {
-    Slot3<float, TTY + 4, 6, 40> S[8];
+    Slot3<float, TTY + 4, 6, 40> S[VRING];
     Slot2<float, TTY + 1, 36> M[3];
     Slot3<float, TTY, 3, 32> V[4];
-    alignas(8) uint64_t barS[8], barM[3], barV[4];
+    alignas(8) uint64_t barS[VRING], barM[3], barV[4];
     int bad;
 };
 static_assert(sizeof(Slot3<float, TTY + 1, 4, 36>) % 128 == 0, "slot size");
@@ -359,7 +372,8 @@ __device__ __forceinline__ void stress_tma_tile(const TArgs& ta, const int bx, c
 
 // ---------------------------------------------------------------------------
 // Interior velocity update (m_kernel.f90:75-140), TMA pipeline.
-//   S ring:   8 planes (k-2 .. k+2 for the z stencil, k+3 .. k+5 in flight)
+//   S ring:   VRING planes (k .. k+2 live, k+3 .. k+VRING-1 in flight; the
+//             start-up planes k-2, k-1 only seed the register z columns)
 //   rho ring: 3 planes (k, k+1, k+2 in flight)
 //   V ring:   4 planes (k, k+1 .. k+3 in flight)
 // ---------------------------------------------------------------------------
@@ -380,7 +394,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
 
     constexpr uint32_t BSH = 4 * (TTY + 4) * 6 * 40, BRHO = 4 * (TTY + 1) * 36, BVC = 4 * TTY * 3 * 32;
     if (tid == 0) {
-        for (int s = 0; s < 8; ++s) mbar_init(&sm.barS[s], 1);
+        for (int s = 0; s < VRING; ++s) mbar_init(&sm.barS[s], 1);
         for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
         for (int s = 0; s < 4; ++s) mbar_init(&sm.barV[s], 1);
         fence_barrier_init();
@@ -389,7 +403,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
     const int gx = xt + g.hx, gy = yt + HYT;
     if (tid == 0) {
         bool ok = true;
-        for (int s = 0; s < 8; ++s) ok &= tma_ok(&sm.S[s], gx - 4, 4);
+        for (int s = 0; s < VRING; ++s) ok &= tma_ok(&sm.S[s], gx - 4, 4);
         for (int s = 0; s < 3; ++s) ok &= tma_ok(&sm.M[s], gx, 4);
         for (int s = 0; s < 4; ++s) ok &= tma_ok(&sm.V[s], gx, 4);
         if (!ok) { bad = 1; atomicExch(ta.err, 2); }
@@ -398,7 +412,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
     if (bad) return;
 
     int nS = kz0 - 2, nM = kz0, nV = kz0;
-    RingPos<8> pS{0, 0u};
+    RingPos<VRING> pS{0, 0u};
     RingPos<3> pM{0, 0u};
     RingPos<4> pV{0, 0u};
     FillLog lS, lM, lV;
@@ -427,7 +441,8 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
         ++nV;
     };
     if (tid == 0) {
-        while (nS <= min(kz0 + 5, kz1 + 1)) issueS();
+        // every slot: planes kz0-2 .. kz0+VRING-3
+        while (nS <= min(kz0 + VRING - 3, kz1 + 1)) issueS();
         while (nM <= min(kz0 + 2, kz1)) issueM();
         while (nV <= min(kz0 + 3, kz1 - 1)) issueV();
     }
@@ -442,7 +457,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
 
     // consumer positions: S of plane k+2 (slots of k-2 .. k+1 ride along),
     // rho of plane k+1 (slot of rho(k) rides along), V of plane k
-    RingPos<8> cS2{4, 0u};
+    RingPos<VRING> cS2{4, 0u};
     RingPos<3> cM1{1, 0u};
     RingPos<4> cV{0, 0u};
     int sS[5] = {0, 1, 2, 3, 4}, sM0 = 0;
@@ -457,6 +472,18 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
         cyz[q] = sm.S[q].d[ly][3][lx];
     }
     for (int q = 0; q < 3; ++q) czz[q] = sm.S[q + 1].d[ly][2][lx];
+    // planes kz0-2 and kz0-1 only seeded the columns: refill their slots
+    // (unless a start-up wait ran out, when a copy may still be landing)
+    const bool all_ok = __syncthreads_and(ok);
+    if (tid == 0) {
+        if (!all_ok) {
+            bad = 1;
+        } else {
+            fence_proxy_async();
+            for (int q = 0; q < 2; ++q)
+                if (nS <= kz1 + 1) issueS();
+        }
+    }
 
     for (int k = kz0; k < kz1; ++k) {
         ok &= mbar_wait(&sm.barS[cS2.slot], cS2.par);
@@ -504,7 +531,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
             const long long oV = bV + k * planeV;
             Vg[oV] = vx; Vg[oV + P] = vy; Vg[oV + 2 * P] = vz;
         }
-        __syncthreads();  // every thread is done with S(k-2), rho(k), V(k)
+        __syncthreads();  // every thread is done with S(k), rho(k), V(k)
         if (bad) break;
         if (tid == 0) {
             fence_proxy_async();
@@ -528,7 +555,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
     }
     if (bad && tid == 0) {
         atomicExch(ta.err, 1);
-        lS.drain(sm.barS, 8);
+        lS.drain(sm.barS, VRING);
         lM.drain(sm.barM, 3);
         lV.drain(sm.barV, 4);
     }
@@ -538,7 +565,7 @@ template <class RT>
 __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constant__ TArgs ta) {
     stress_tma_tile<RT>(ta, blockIdx.x, blockIdx.y, blockIdx.z);
 }
-__global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma(const __grid_constant__ TArgs ta) {
+__global__ void __launch_bounds__(32 * TTY, VMINB) k_vel_tma(const __grid_constant__ TArgs ta) {
     vel_tma_tile(ta, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
@@ -582,7 +609,7 @@ __global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma_batch(const TArgs* _
     tmaps_acquire(all[e.x]);
     stress_tma_tile<RT>(all[e.x], e.y, e.z, e.w);
 }
-__global__ void __launch_bounds__(32 * TTY, 2) k_vel_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
+__global__ void __launch_bounds__(32 * TTY, VMINB) k_vel_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
     const int4 e = blocks[blockIdx.x];
     tmaps_acquire(all[e.x]);
     vel_tma_tile(all[e.x], e.y, e.z, e.w);

@@ -77,7 +77,7 @@ static int plan(const swpc_dims* d, Plan& p) {
             if (bx[b][3] <= 0 || bx[b][4] <= 0 || bx[b][5] <= 0) continue;
             PmlBox& B = p.box[p.nbox++];
             B.x0 = bx[b][0]; B.y0 = bx[b][1]; B.z0 = bx[b][2]; B.nx = bx[b][3]; B.ny = bx[b][4]; B.nz = bx[b][5];
-            B.pitch = (int)rup(B.nx, 32);
+            B.pitch = B.nx;  // rows of one point contiguous: no partly used lines in the 20-wide x-side boxes
             B.off = p.nade;
             B.first = first;
             B.tiles_x = (B.nx + 31) / 32;
@@ -351,6 +351,10 @@ int Sim::build_tensor_maps() {
     CK(cudaFuncSetAttribute(k_stress_tma_batch<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sizeof(StressSmem<__nv_bfloat16>)));
     CK(cudaFuncSetAttribute(k_vel_tma_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(VelSmem)));
+    // the velocity kernel is sized for VMINB blocks per SM: ask for the
+    // largest shared-memory carve-out
+    CK(cudaFuncSetAttribute(k_vel_tma, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared));
+    CK(cudaFuncSetAttribute(k_vel_tma_batch, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared));
     return 0;
 }
 

@@ -65,6 +65,7 @@ def lib():
         L.oracle_field.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
         L.oracle_medium.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
         L.oracle_set_field.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_coefs.argtypes = [vp, ctypes.c_void_p]
         L.oracle_vmax.argtypes = [vp, ctypes.c_void_p]
         L.oracle_snap_xy_v.argtypes = [vp, ctypes.c_void_p]
         L.oracle_snap.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
@@ -128,6 +129,23 @@ class Oracle:
         if self._L.oracle_field(self.h, FIELDS.index(name), out.ctypes.data) != 0:
             raise RuntimeError(self._L.oracle_last_error().decode())
         return out
+
+    def coefs(self):
+        """Zener coefficients c1, c2, d1 (nm), d2 and, with the PML, the
+        damping profiles gxc, gxe, gyc, gye, gzc, gze as (n, 4) arrays."""
+        nm = 3
+        out = np.zeros(4 * nm + 1 + 8 * (self.nx + self.ny + self.nz), np.float64)
+        n = self._L.oracle_coefs(self.h, out.ctypes.data)
+        if n < 0:
+            raise RuntimeError(self._L.oracle_last_error().decode())
+        r = {"c1": out[0:nm], "c2": out[nm:2 * nm], "d1": out[2 * nm:3 * nm], "d2": out[3 * nm]}
+        q = 3 * nm + 1
+        if n > q:
+            for name, m in (("gxc", self.nx), ("gxe", self.nx), ("gyc", self.ny), ("gye", self.ny),
+                            ("gzc", self.nz), ("gze", self.nz)):
+                r[name] = out[q:q + 4 * m].reshape(m, 4)
+                q += 4 * m
+        return r
 
     def set_field(self, name, halo):
         """Overwrite a state field from a (ny+6, nx+6, nz+6) halo-grid

@@ -321,6 +321,7 @@ struct SimBase {
     virtual void set_field(int which, const float* halo) = 0;
     virtual void get_medium(int which, float* out) = 0;
     virtual int green_out(int* ng_ncmp_ntw, float* out) = 0;
+    virtual int coefs(double* out) = 0;
     Params p;
     int nt_done = 0;
     int nst = 0, ntw = 0;
@@ -1584,6 +1585,19 @@ struct Sim : SimBase {
         size_t q = 0;
         for (int j = 1; j <= ny; ++j) for (int i = 1; i <= nx; ++i) for (int k = 1; k <= nz; ++k) out[q++] = (double)A(k, i, j);
     }
+    // Zener coefficients c1, c2, d1 (nm each), d2, then with the PML the
+    // damping profiles gxc, gxe (4 x nx), gyc, gye (4 x ny), gzc, gze
+    // (4 x nz), l fastest; returns the number of values written
+    int coefs(double* out) override {
+        int q = 0;
+        for (const std::vector<SP>* v : {&c1, &c2, &d1})
+            for (SP x : *v) out[q++] = (double)x;
+        out[q++] = (double)d2;
+        if (pml)
+            for (const std::vector<SP>* v : {&gxc, &gxe, &gyc, &gye, &gzc, &gze})
+                for (SP x : *v) out[q++] = (double)x;
+        return q;
+    }
     // overwrite one state field from a halo-grid array A(k,i,j) (k fastest):
     // every cell of the physical columns i in [1,nx], j in [1,ny] including
     // the z halo planes; the x/y ghost columns stay zero, as after a halo
@@ -1698,6 +1712,9 @@ void oracle_stations(void* h, int* ijk) {
 
 int oracle_field(void* h, int which, double* out) {
     try { ((SimBase*)h)->get_field(which, out); return 0; } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+int oracle_coefs(void* h, double* out) {
+    try { return ((SimBase*)h)->coefs(out); } catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
 int oracle_set_field(void* h, int which, const float* halo) {
     try { ((SimBase*)h)->set_field(which, halo); return 0; } catch (const std::exception& e) { g_err = e.what(); return -1; }

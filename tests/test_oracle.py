@@ -131,3 +131,53 @@ def test_oracle_reproduces_golden_traces(tmp_path):
     # the three builds agree to the expected orders
     assert misfit(g["fp32"], g["fp64"]) < 1e-5
     assert misfit(g["mixed"], g["fp64"]) < 1e-6
+
+
+def _zener_closed_form(nm, fmin, fmax, dt):
+    """visco_set_relaxtime (m_fdtool.f90:691-727) and kernel__setup's Zener
+    coefficients (m_kernel.f90:58-67), in FP64."""
+    wa, wb = 2 * np.pi * fmin, 2 * np.pi * fmax
+    ts = 1 / (wa * (wb / wa) ** (np.arange(nm) / (nm - 1)))
+    c1 = (2 * ts - dt) / (2 * ts + dt)
+    c2 = 2 / (2 * ts + dt) / nm
+    d1 = 2 * ts / (2 * ts - dt)
+    d2 = np.sum(dt / (2 * ts - dt)) / nm
+    return c1, c2, d1, d2
+
+
+def _damping_closed_form(x, H, xb, xe, na, fcut, dt):
+    """damping_profile (m_absorb_p.f90:533-573): ADE-CFS g1..g4, in FP64."""
+    R0 = 10 ** (-(np.log10(na) - 1) / np.log10(2.0) - 3.0)
+    d0 = -(1 / (2 * H)) * 2 * 6.0 * np.log(R0)
+    a0, b0 = np.pi * fcut, 7.0
+    xx = np.where(x <= xb + H, (xb + H) - x, np.where(x >= xe - H, x - (xe - H), 0.0))
+    r = np.abs(xx / H)
+    d, a, b = d0 * r, a0 * (1 - r), 1 + (b0 - 1) * r * r
+    den = 1 + dt / 2 * (a + d / b)
+    return np.stack([((1 + dt / 2 * a) / b) / den, (-1 / b) / den, (1 - dt / 2 * (a + d / b)) / den, (d / b) / den], 1)
+
+
+@pytest.mark.parametrize("mode,rtol", [("fp64", 1e-12), ("fp32", 3e-6)])
+def test_zener_and_pml_coefficients_closed_form(tmp_path, mode, rtol):
+    """The oracle's Zener coefficients and PML damping profiles against the
+    closed forms in FP64 (exact in fp64 mode, within single-precision
+    rounding in fp32 mode, which evaluates them as the reference does)."""
+    inf = configs.write_plain_small(str(tmp_path), nt=2)
+    o = pyoracle.Oracle(inf, mode)
+    cf = o.coefs()
+    c1, c2, d1, d2 = _zener_closed_form(3, 0.05, 5.0, o.dt)
+    for name, ref in (("c1", c1), ("c2", c2), ("d1", d1)):
+        assert np.allclose(cf[name], ref, rtol=rtol, atol=0), name
+    assert abs(cf["d2"] / d2 - 1) < rtol
+    for ax, n, beg, h in (("x", o.nx, o.xbeg, o.dx), ("y", o.ny, o.ybeg, o.dy), ("z", o.nz, o.zbeg, o.dz)):
+        xc = beg + (np.arange(1, n + 1) - 0.5) * h  # i2x (m_fdtool.f90:639-680)
+        H, xe = o.na * h, beg + n * h
+        for stag, x in (("c", xc), ("e", xc + h / 2)):
+            ref = _damping_closed_form(x, H, beg, xe, o.na, o.fcut, o.dt)
+            got = cf["g%s%s" % (ax, stag)]
+            assert np.allclose(got, ref, rtol=rtol, atol=rtol * np.abs(ref).max()), (ax, stag)
+    # outside the layer d = 0: g1 = 1 (plain derivative) and g4 = 0 (the
+    # auxiliary variables get no source and stay zero)
+    mid = cf["gxc"][o.nx // 2]
+    assert abs(mid[0] - 1) < rtol and mid[3] == 0
+    o.close()
