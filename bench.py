@@ -431,7 +431,7 @@ def run_batch(args):
         sims = [gpu.Simulation.from_inf(f) for f in infs]
         pts = [int(np.prod(s)) for s in sizes]
         t0 = time.time()
-        rec = autotune.tune(sims, steps=3)
+        rec = autotune.tune(sims)
         t_tune = time.time() - t0
         b = gpu.Batch(sims)
         st = torch.cuda.ExternalStream(b.stream())
@@ -468,7 +468,7 @@ def run_batch(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batched many-instance: %d simulations, axes in {96..256}, nt=%d" % (n, nt_full),
-                       "points_total": int(sum(pts)), "zchunk": rec["zchunk"]},
+                       "points_total": int(sum(pts)), "zchunk": [rec["zchunk"], rec["zchunk_vel"]]},
             "sequential_solves_per_s": solves_seq, "speedup_vs_sequential": solves_batch / solves_seq,
             "grid_pt_updates_per_s": sum(pts) / (ms_batch / 1e3), "autotune": rec, "autotune_s": t_tune,
             "gpu_launches": launches}

@@ -1,12 +1,14 @@
-"""Autotuner of the z-sweep depth of the interior kernels.
+"""Autotuner of the z-sweep depths of the interior kernels.
 
 Each interior block sweeps a chunk of z planes.  Long chunks amortise the
 pipeline prologue (the first planes of every ring are loaded before any
 compute); short chunks create more blocks, which small grids need to fill the
-GPU.  The best depth depends on the grid shape and on what else shares the
-GPU (a batch), so it is measured: every candidate depth is timed on the real
-simulations with CUDA events on the launching stream, then the simulations
-are reset to their initial state.  Results are cached in a JSON file keyed by
+GPU, and keep neighbouring blocks on the same planes so that they share halo
+rows in L2.  The stress and velocity kernels weigh these differently, so each
+gets its own depth.  The best depths depend on the grid shape and on what
+else shares the GPU (a batch), so they are measured: every candidate depth is
+timed on the real simulations with CUDA events on the launching stream, then
+the simulations are reset to their initial state.  Results are cached in a JSON file keyed by
 the shape class (interior extents rounded up to 32, storage precision, batch
 size), so later runs with the same shapes skip the measurement.
 """
@@ -57,25 +59,30 @@ def _time(runner, stream, steps):
     return e0.elapsed_time(e1) / steps
 
 
-def tune(sims, store="fp32", warmup=2, steps=6, cache=DEFAULT_CACHE, candidates=CANDIDATES, batch=None):
-    """Pick the z-sweep depth for `sims` (one simulation, or the members of a
-    batch when len(sims) > 1), apply it to every member and return
-    {"zchunk": depth, "ms_per_step": {depth: ms}}.
+def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=CANDIDATES, batch=None):
+    """Pick the z-sweep depths of the stress and velocity kernels for `sims`
+    (one simulation, or the members of a batch when len(sims) > 1), apply
+    them to every member and return {"zchunk": stress depth, "zchunk_vel":
+    velocity depth, "ms_per_step": {depth: ms}, "ms_per_step_vel": {depth:
+    ms}} (0 = the library's automatic choice).
 
+    The stress depth is swept first with the velocity kernel at its automatic
+    depth, then the velocity depth with the stress depth fixed at its best.
+    The warm-up builds the CUDA graph of the step (8 steps), so the timed
+    steps replay it as a production run does.
     The members are stepped while timing and reset afterwards, so call this
     after set-up and before the production run.
     """
     key = _shape_key(sims, store)
     db = _load(cache) if cache else {}
-    if key in db:
-        z = db[key]["zchunk"]
+    if key in db and "zchunk_vel" in db[key]:
         for s in sims:
-            s.set_zchunk(z)
+            s.set_zchunks(db[key]["zchunk"], db[key]["zchunk_vel"])
         return db[key]
-    times = {}
-    for z in candidates:
+
+    def measure(ks, kv):
         for s in sims:
-            s.set_zchunk(z)
+            s.set_zchunks(ks, kv)
         if len(sims) == 1:
             s = sims[0]
             it = [1]
@@ -86,19 +93,25 @@ def tune(sims, store="fp32", warmup=2, steps=6, cache=DEFAULT_CACHE, candidates=
 
             runner(warmup)
             s.sync()
-            times[z] = _time(runner, s.stream(), steps)
+            ms = _time(runner, s.stream(), steps)
         else:
             b = gpu.Batch(sims)
             b.run(warmup)
             b.sync()
-            times[z] = _time(b.run, b.stream(), steps)
+            ms = _time(b.run, b.stream(), steps)
             b.close()
         for s in sims:
             s.reset()
-    best = min(times, key=times.get)
+        return ms
+
+    t_s = {z: measure(z, 0) for z in candidates}
+    best_s = min(t_s, key=t_s.get)
+    t_v = {z: measure(best_s, z) for z in candidates}
+    best_v = min(t_v, key=t_v.get)
     for s in sims:
-        s.set_zchunk(best)
-    rec = {"zchunk": best, "ms_per_step": {str(k): float(v) for k, v in times.items()}}
+        s.set_zchunks(best_s, best_v)
+    rec = {"zchunk": best_s, "zchunk_vel": best_v, "ms_per_step": {str(k): float(v) for k, v in t_s.items()},
+           "ms_per_step_vel": {str(k): float(v) for k, v in t_v.items()}}
     if cache:
         db = _load(cache)
         db[key] = rec

@@ -70,7 +70,8 @@ struct ZArgs {
     const int4* band;  // per interior column: kfs_top, kfs_bot, kob_top, kob_bot (1-based k)
     int x0, y0, nxi, nyi;  // interior box (0-based origin, extent)
     int kz_end;            // interior planes [0, kz_end)
-    int kchunk;            // planes per block in z
+    int kchunk;            // planes per block in z (stress kernels)
+    int kchunk_v;          // planes per block in z (velocity kernels)
     int rpitch;            // R row pitch (elements)
     const float* cer;      // Cerjan profiles (null for PML): xc xb yc yb zc zb, each padded
     int cer_off[6];
@@ -301,8 +302,8 @@ __global__ void __launch_bounds__(TBX * TBY, 2) k_vel_interior(const ZArgs a) {
     const int xt = a.x0 + blockIdx.x * TBX, yt = a.y0 + blockIdx.y * TBY;
     const int ix = xt + tx, jy = yt + ty;
     const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
-    const int kz0 = blockIdx.z * a.kchunk;
-    const int kz1 = min(kz0 + a.kchunk, a.kz_end);
+    const int kz0 = blockIdx.z * a.kchunk_v;
+    const int kz1 = min(kz0 + a.kchunk_v, a.kz_end);
     if (kz0 >= kz1) return;
 
     const long long planeV = 3LL * g.pitch * g.nyp;
@@ -1019,44 +1020,48 @@ __global__ void k_advance_batch(int* const* __restrict__ its, int n) {
     if (q < n) *its[q] += 1;
 }
 
-// Fortran (k,i,j) halo array -> one field of a device group (upload)
-__global__ void k_scatter_f(const float* src, float* dst, Geo g, int nf, int f, int store_kind, void* dst16) {
-    const long long n = (long long)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-        int k = (int)(p % (g.nz + 6)) - 3;
-        long long q = p / (g.nz + 6);
-        int i = (int)(q % (g.nx + 6)) - 3;
-        int j = (int)(q / (g.nx + 6)) - 3;
-        dst[goff(g, nf, f, i, j, k)] = src[p];
-        (void)store_kind; (void)dst16;
+// Fortran (k,i,j) halo array -> one field of a device group, as a tiled
+// transpose: a block stages a 32 (k) x 32 (i) tile of one j row in shared
+// memory, reading along k and writing along x, so that both the read and the
+// write are coalesced.  cols_only leaves the x/y ghost columns untouched
+// (every k of the halo range is written).  Grid (ceil((nz+6)/32),
+// ceil((nx+6)/32), ny+6), block (32, 8).
+__global__ void __launch_bounds__(256) k_scatter_t(const float* __restrict__ src, float* __restrict__ dst, Geo g, int nf,
+                                                    int f, int cols_only) {
+    __shared__ float t[32][33];
+    const int nk = g.nz + 6, ni = g.nx + 6;
+    const int k0 = blockIdx.x * 32, i0 = blockIdx.y * 32, jh = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int r = ty; r < 32; r += 8) {
+        const int ih = i0 + r, kh = k0 + tx;
+        if (ih < ni && kh < nk) t[r][tx] = src[((size_t)jh * ni + ih) * nk + kh];
+    }
+    __syncthreads();
+    const int j = jh - 3;
+    if (cols_only && (j < 0 || j >= g.ny)) return;
+    for (int r = ty; r < 32; r += 8) {
+        const int kh = k0 + r, ih = i0 + tx;
+        if (kh >= nk || ih >= ni) continue;
+        const int i = ih - 3;
+        if (cols_only && (i < 0 || i >= g.nx)) continue;
+        dst[goff(g, nf, f, i, j, kh - 3)] = t[tx][r];
     }
 }
 
 // Depth-only medium: five columns of nz + 6 values (k = -2 .. nz+3; rho lam
-// mu taup taus) copied into every (i, j) of the halo grid of the M group.
-__global__ void k_spread_col(const float* col, float* M, Geo g) {
-    const long long nk = g.nz + 6;
-    const long long n = nk * (g.nx + 6) * (g.ny + 6);
+// mu taup taus) copied into every (i, j) of the halo grid of the M group,
+// walking the destination in its own order (x fastest).
+__global__ void k_spread_col(const float* __restrict__ col, float* __restrict__ M, Geo g) {
+    const int nk = g.nz + 6, ni = g.nx + 6, nj = g.ny + 6;
+    const long long n = (long long)nk * nj * 5 * ni;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-        int k = (int)(p % nk) - 3;
-        long long q = p / nk;
-        int i = (int)(q % (g.nx + 6)) - 3;
-        int j = (int)(q / (g.nx + 6)) - 3;
-        for (int f = 0; f < 5; ++f) M[goff(g, 5, f, i, j, k)] = col[f * nk + k + 3];
-    }
-}
-
-// Fortran halo array (k,i,j) -> one field of a device group, physical
-// columns only (every k of the halo range; the x/y ghost columns stay zero)
-__global__ void k_scatter_cols(const float* src, float* dst, Geo g, int nf, int f) {
-    const long long n = (long long)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-        int k = (int)(p % (g.nz + 6)) - 3;
-        long long q = p / (g.nz + 6);
-        int i = (int)(q % (g.nx + 6)) - 3;
-        int j = (int)(q / (g.nx + 6)) - 3;
-        if (i < 0 || i >= g.nx || j < 0 || j >= g.ny) continue;
-        dst[goff(g, nf, f, i, j, k)] = src[p];
+        const int ih = (int)(p % ni);
+        long long q = p / ni;
+        const int f = (int)(q % 5);
+        q /= 5;
+        const int jh = (int)(q % nj);
+        const int kh = (int)(q / nj);
+        M[goff(g, 5, f, ih - 3, jh - 3, kh - 3)] = col[f * nk + kh];
     }
 }
 
@@ -1086,15 +1091,22 @@ __global__ void k_pw_ghost(float* F, Geo g, int nf) {
     }
 }
 
-// one field of a device group -> Fortran (nz, nx, ny) physical-grid double array
-__global__ void k_gather_d(const float* src, double* dst, Geo g, int nf, int f) {
-    const long long n = (long long)g.nz * g.nx * g.ny;
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-        int k = (int)(p % g.nz);
-        long long q = p / g.nz;
-        int i = (int)(q % g.nx);
-        int j = (int)(q / g.nx);
-        dst[p] = (double)src[goff(g, nf, f, i, j, k)];
+// one field of a device group -> Fortran (nz, nx, ny) physical-grid double
+// array, as a tiled transpose (read along x, write along k).  Grid
+// (ceil(nz/32), ceil(nx/32), ny), block (32, 8).
+__global__ void __launch_bounds__(256) k_gather_d(const float* __restrict__ src, double* __restrict__ dst, Geo g, int nf,
+                                                   int f) {
+    __shared__ float t[32][33];
+    const int k0 = blockIdx.x * 32, i0 = blockIdx.y * 32, j = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int r = ty; r < 32; r += 8) {
+        const int k = k0 + r, i = i0 + tx;
+        if (k < g.nz && i < g.nx) t[r][tx] = src[goff(g, nf, f, i, j, k)];
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int i = i0 + r, k = k0 + tx;
+        if (k < g.nz && i < g.nx) dst[((size_t)j * g.nx + i) * g.nz + k] = (double)t[tx][r];
     }
 }
 

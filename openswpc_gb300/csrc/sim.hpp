@@ -47,7 +47,8 @@ struct Sim {
     int* d_kfs = nullptr;
     int* d_err = nullptr;   // set by a kernel whose bounded wait ran out
     Coef coef{};
-    int kchunk = 1, kchunk_auto = 1;
+    int kchunk = 1, kchunk_auto = 1;      // z-sweep depth of the stress kernels
+    int kchunk_v = 1, kchunk_v_auto = 1;  // and of the velocity kernels
     int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
     size_t smem_stress = 0, smem_vel = 0;

@@ -139,7 +139,7 @@ void Sim::fill_zargs(ZArgs& z) const {
     z.g = p.g;
     z.V = V; z.S = S; z.M = M; z.R = R; z.band = band;
     z.x0 = p.x0; z.y0 = p.y0; z.nxi = p.nxi; z.nyi = p.nyi; z.kz_end = p.nzi;
-    z.kchunk = kchunk; z.rpitch = p.rpitch;
+    z.kchunk = kchunk; z.kchunk_v = kchunk_v; z.rpitch = p.rpitch;
     z.cer = p.pml ? nullptr : cer;
     for (int q = 0; q < 6; ++q) z.cer_off[q] = cer_off[q];
     z.c = coef;
@@ -148,6 +148,7 @@ void Sim::fill_zargs(ZArgs& z) const {
 int Sim::launch_step(bool timed) {
     const dim3 blk(TBX, TBY);
     const dim3 grd((p.nxi + TBX - 1) / TBX, (p.nyi + TBY - 1) / TBY, (p.nzi + kchunk - 1) / kchunk);
+    const dim3 grd_v(grd.x, grd.y, (p.nzi + kchunk_v - 1) / kchunk_v);
     // timed: an event pair on the launching stream around each kernel, read
     // back later by drain_events() so the launches are not serialised
     cudaEvent_t e_a[6] = {};
@@ -183,6 +184,7 @@ int Sim::launch_step(bool timed) {
     targs.z = z;
     const dim3 tblk(32, TTY);
     const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + TTY - 1) / TTY, (p.nzi + kchunk - 1) / kchunk);
+    const dim3 tgrd_v(tgrd.x, tgrd.y, (p.nzi + kchunk_v - 1) / kchunk_v);
     if (pw && p.pml) { k_pw_ghost<<<256, 256, 0, stream>>>(V, p.g, 3); ++launches; }
     if (two) {
         cudaEventRecord(ev_fork, stream);
@@ -224,8 +226,8 @@ int Sim::launch_step(bool timed) {
         if (two) cudaEventRecord(ev_join2, stream2);
     }
     ev0(1, stream);
-    if (variant == 0) k_vel_tma<<<tgrd, tblk, smem_vel, stream>>>(targs);
-    else k_vel_interior<<<grd, blk, 0, stream>>>(z);
+    if (variant == 0) k_vel_tma<<<tgrd_v, tblk, smem_vel, stream>>>(targs);
+    else k_vel_interior<<<grd_v, blk, 0, stream>>>(z);
     ++launches;
     ev1(1, stream);
     if (two) cudaStreamWaitEvent(stream, ev_join2, 0);
@@ -489,8 +491,9 @@ int swpc_gpu_set_field(swpc_sim* sim, int which, const float* field) {
     float* stage = nullptr;
     CK(cudaMallocAsync(&stage, n * 4, s->stream));
     CK(cudaMemcpyAsync(stage, field, n * 4, cudaMemcpyHostToDevice, s->stream));
-    if (which < 3) k_scatter_cols<<<2048, 256, 0, s->stream>>>(stage, s->V, g, 3, which);
-    else k_scatter_cols<<<2048, 256, 0, s->stream>>>(stage, s->S, g, 6, which - 3);
+    const dim3 tg((g.nz + 6 + 31) / 32, (g.nx + 6 + 31) / 32, g.ny + 6), tb(32, 8);
+    if (which < 3) k_scatter_t<<<tg, tb, 0, s->stream>>>(stage, s->V, g, 3, which, 1);
+    else k_scatter_t<<<tg, tb, 0, s->stream>>>(stage, s->S, g, 6, which - 3, 1);
     ++s->launches;
     CK(cudaFreeAsync(stage, s->stream));
     CK(cudaStreamSynchronize(s->stream));
@@ -648,9 +651,10 @@ int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out) {
     size_t n = (size_t)g.nx * g.ny * g.nz;
     double* d = nullptr;
     CK(cudaMallocAsync(&d, n * 8, s->stream));
-    if (which < 3) k_gather_d<<<1024, 256, 0, s->stream>>>(s->V, d, g, 3, which);
-    else if (which < 9) k_gather_d<<<1024, 256, 0, s->stream>>>(s->S, d, g, 6, which - 3);
-    else k_gather_d<<<1024, 256, 0, s->stream>>>(s->M, d, g, 5, which - 9);
+    const dim3 tg((g.nz + 31) / 32, (g.nx + 31) / 32, g.ny), tb(32, 8);
+    if (which < 3) k_gather_d<<<tg, tb, 0, s->stream>>>(s->V, d, g, 3, which);
+    else if (which < 9) k_gather_d<<<tg, tb, 0, s->stream>>>(s->S, d, g, 6, which - 3);
+    else k_gather_d<<<tg, tb, 0, s->stream>>>(s->M, d, g, 5, which - 9);
     ++s->launches;
     CK(cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaFreeAsync(d, s->stream));
@@ -706,8 +710,9 @@ extern "C" int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out
     if (rc) return rc;
     // every one of the n elements copied back is written by the gather first,
     // so the array needs no clearing
-    if (which < 3) k_gather_d<<<1024, 256, 0, s->stream>>>(s->V, d, g, 3, which);
-    else k_gather_d<<<1024, 256, 0, s->stream>>>(s->S, d, g, 6, which - 3);
+    const dim3 tg((g.nz + 31) / 32, (g.nx + 31) / 32, g.ny), tb(32, 8);
+    if (which < 3) k_gather_d<<<tg, tb, 0, s->stream>>>(s->V, d, g, 3, which);
+    else k_gather_d<<<tg, tb, 0, s->stream>>>(s->S, d, g, 6, which - 3);
     ++s->launches;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, d, n * 8, cudaMemcpyDeviceToHost, s->stream));
@@ -852,15 +857,25 @@ int Sim::allocate() {
     if ((rc = dalloc((void**)&d_it, 16))) return rc;
     if ((rc = dalloc((void**)&d_kob, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     if ((rc = dalloc((void**)&d_kfs, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
-    // z chunking: enough blocks to fill the GPU at least ~4 times
+    // z chunking: enough blocks to fill the GPU at least ~8 times; then the
+    // stress kernels take chunks of at most 8 planes (neighbouring blocks
+    // sweep the same planes at the same time and share their V halo rows in
+    // L2: 1024x1024x512 stress 17.6, 16.2, 16.0 ms with 492, 16, 8 planes) and
+    // the velocity kernels chunks of at most 128 planes (its longer start-up
+    // costs more: 4.67 ms at 492, 4.54 at 123, 4.95 at 16 planes)
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     long long cols = (long long)((p.nxi + TBX - 1) / TBX) * ((p.nyi + TBY - 1) / TBY);
     long long want = 8LL * nsm;
     int nchunk = (int)std::max(1LL, std::min((long long)(p.nzi / 8), (want + cols - 1) / cols));
-    kchunk = (p.nzi + nchunk - 1) / nchunk;
-    kchunk_auto = kchunk;
+    const int kfill = (p.nzi + nchunk - 1) / nchunk;
+    auto even = [&](int cap) {  // equal chunks of at most cap planes
+        const int nc = (p.nzi + cap - 1) / cap;
+        return (p.nzi + nc - 1) / nc;
+    };
+    kchunk = kchunk_auto = even(std::min(kfill, 8));
+    kchunk_v = kchunk_v_auto = even(std::min(kfill, 128));
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
     variant = dims.reserved[0] == 1 ? 1 : 0;
@@ -868,11 +883,25 @@ int Sim::allocate() {
     // cannot fill the GPU by itself (measured: 128x128x64 0.134 vs 0.16 ms per
     // step; 1024x1024x512 27.9 serial vs 28.3 ms concurrent)
     {
-        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + TTY - 1) / TTY) * ((p.nzi + kchunk - 1) / kchunk);
+        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + TTY - 1) / TTY) * ((p.nzi + kfill - 1) / kfill);
         concurrent = dims.reserved[1] == 2 || (dims.reserved[1] == 0 && tiles < 4LL * nsm);
     }
     if ((rc = build_tensor_maps())) return rc;
     return 0;
+}
+
+// Device address of a pinned (page-locked, device-mapped) host array, or
+// null for any other memory.  The transpose kernels read pinned arrays
+// directly over the CPU-GPU link instead of staging them in device memory
+// first; the callers synchronise before they return, as the ABI's copy
+// semantics require.
+static const float* pinned_view(const float* h) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost && at.devicePointer ? static_cast<const float*>(at.devicePointer) : nullptr;
 }
 
 int Sim::upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
@@ -892,13 +921,17 @@ int Sim::upload_medium(const float* rho, const float* lam, const float* mu, cons
     } else {
         const size_t n3 = (size_t)(g.nz + 6) * (g.nx + 6) * (g.ny + 6);
         float* stage = nullptr;
-        CK(cudaMallocAsync((void**)&stage, n3 * 4, stream));
         for (int f = 0; f < 5; ++f) {
-            CK(cudaMemcpyAsync(stage, fields[f], n3 * 4, cudaMemcpyHostToDevice, stream));
-            k_scatter_f<<<2048, 256, 0, stream>>>(stage, M, g, 5, f, 0, nullptr);
+            const float* src = pinned_view(fields[f]);
+            if (!src) {
+                if (!stage) CK(cudaMallocAsync((void**)&stage, n3 * 4, stream));
+                CK(cudaMemcpyAsync(stage, fields[f], n3 * 4, cudaMemcpyHostToDevice, stream));
+                src = stage;
+            }
+            k_scatter_t<<<dim3((g.nz + 6 + 31) / 32, (g.nx + 6 + 31) / 32, g.ny + 6), dim3(32, 8), 0, stream>>>(src, M, g, 5, f, 0);
             ++launches;
         }
-        CK(cudaFreeAsync(stage, stream));
+        if (stage) CK(cudaFreeAsync(stage, stream));
     }
     // band table over the interior columns and the kob map
     const int mx = g.nx + 6;
@@ -1203,9 +1236,10 @@ struct Batch {
     std::vector<Sim*> pw_members;  // plane-wave members: lateral ghost extrapolation before the PML updates
     VmaxArgs* d_vmax = nullptr;
     int** d_its = nullptr;
-    int4* d_tblocks = nullptr;
+    int4* d_tblocks = nullptr;   // stress tiles
+    int4* d_tblocks_v = nullptr; // velocity tiles
     int2* d_pblocks = nullptr;
-    int n_tblocks = 0, n_pblocks = 0, max_nst = 0, max_src = 0, max_pix = 0, max_planes = 0;
+    int n_tblocks = 0, n_tblocks_v = 0, n_pblocks = 0, max_nst = 0, max_src = 0, max_pix = 0, max_planes = 0;
     bool any_vmax = false, any_snap = false, any_bf = false, any_mt = false;
     size_t smem_stress = 0, smem_vel = 0;
     long long launches = 0, launches_per_graph = 0;
@@ -1254,7 +1288,7 @@ struct Batch {
             k_vel_pml_batch<<<n_pblocks, PTPB, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
             cudaEventRecord(ev[3], stream2);
         }
-        k_vel_tma_batch<<<n_tblocks, tblk, smem_vel, stream>>>(d_targs, d_tblocks); ++launches;
+        k_vel_tma_batch<<<n_tblocks_v, tblk, smem_vel, stream>>>(d_targs, d_tblocks_v); ++launches;
         if (n_pblocks) cudaStreamWaitEvent(stream, ev[3], 0);
         if (any_bf) { k_bodyforce_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
         k_advance_batch<<<(n + 127) / 128, 128, 0, stream>>>(d_its, n); ++launches;
@@ -1266,12 +1300,24 @@ struct Batch {
 
 extern "C" {
 
-int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk) {
+int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel) {
     Sim* s = reinterpret_cast<Sim*>(sim);
-    if (!s || kchunk < 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_zchunk");
-    if (kchunk == 0) kchunk = s->kchunk_auto;
-    s->kchunk = std::max(1, std::min(kchunk, s->p.nzi));
+    if (!s || kstress < 0 || kvel < 0) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_set_zchunks");
+    if (kstress == 0) kstress = s->kchunk_auto;
+    if (kvel == 0) kvel = s->kchunk_v_auto;
+    s->kchunk = std::max(1, std::min(kstress, s->p.nzi));
+    s->kchunk_v = std::max(1, std::min(kvel, s->p.nzi));
     if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+    return 0;
+}
+
+int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk) { return swpc_gpu_set_zchunks(sim, kchunk, kchunk); }
+
+int swpc_gpu_get_zchunks(swpc_sim* sim, int* kstress, int* kvel) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !kstress || !kvel) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_get_zchunks");
+    *kstress = s->kchunk;
+    *kvel = s->kchunk_v;
     return 0;
 }
 
@@ -1309,7 +1355,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     std::vector<GreenArgs> gr(n);
     std::vector<VmaxArgs> vm(n);
     std::vector<int*> its(n);
-    std::vector<int4> tb;
+    std::vector<int4> tb, tbv;
     std::vector<int2> pb;
     for (int q = 0; q < n; ++q) {
         Sim* s = b->sims[q];
@@ -1329,9 +1375,13 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         vm[q] = s->vmax_args;
         its[q] = s->d_it;
         const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + TTY - 1) / TTY, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
+        const int gzv = (s->p.nzi + s->kchunk_v - 1) / s->kchunk_v;
         for (int bz = 0; bz < gz; ++bz)
             for (int by = 0; by < gy; ++by)
                 for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
+        for (int bz = 0; bz < gzv; ++bz)
+            for (int by = 0; by < gy; ++by)
+                for (int bx = 0; bx < gx; ++bx) tbv.push_back(make_int4(q, bx, by, bz));
         if (s->p.pml)
             for (long long bk = 0; bk < (s->p.npml + PTPB - 1) / PTPB; ++bk) pb.push_back(make_int2(q, (int)bk));
         b->max_nst = std::max(b->max_nst, s->tap_args.n);
@@ -1347,10 +1397,11 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     int rc;
     if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_pargs, pa)) || (rc = b->upload(&b->d_src, sa)) ||
         (rc = b->upload(&b->d_tap, tp)) || (rc = b->upload(&b->d_snap, sn)) || (rc = b->upload(&b->d_green, gr)) || (rc = b->upload(&b->d_vmax, vm)) ||
-        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_pblocks, pb)))
+        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_tblocks_v, tbv)) || (rc = b->upload(&b->d_pblocks, pb)))
         return fail(rc);
     if (((uintptr_t)b->d_targs & 127) != 0) return fail(set_err(SWPC_E_CUDA, "tensor-map table is not 128-byte aligned"));
     b->n_tblocks = (int)tb.size();
+    b->n_tblocks_v = (int)tbv.size();
     b->n_pblocks = (int)pb.size();
     b->smem_stress = b->sims[0]->smem_stress;
     b->smem_vel = b->sims[0]->smem_vel;

@@ -50,7 +50,7 @@ EXPORTS = [
     "swpc_gpu_fetch_field", "swpc_gpu_profile", "swpc_gpu_profile_read", "swpc_gpu_stream",
     "swpc_gpu_launch_count", "swpc_gpu_destroy", "swpc_gpu_last_error", "swpc_host_prepare",
     "swpc_host_write_sac", "swpc_host_write_snp", "swpc_host_nt", "swpc_host_medium",
-    "swpc_host_check", "swpc_gpu_fetch_field_static", "swpc_gpu_reset", "swpc_gpu_get_dims", "swpc_gpu_set_zchunk",
+    "swpc_host_check", "swpc_gpu_fetch_field_static", "swpc_gpu_reset", "swpc_gpu_get_dims", "swpc_gpu_set_zchunk", "swpc_gpu_set_zchunks", "swpc_gpu_get_zchunks",
     "swpc_gpu_get_zchunk", "swpc_batch_create", "swpc_batch_run", "swpc_batch_sync", "swpc_batch_stream",
     "swpc_batch_launch_count", "swpc_batch_destroy", "swpc_host_load", "swpc_host_request_bytes", "swpc_gpu_selftest_wait",
     "swpc_gpu_add_snapshot", "swpc_gpu_query_snapshot", "swpc_gpu_fetch_section", "swpc_gpu_set_green",
@@ -117,6 +117,8 @@ def lib(build=True):
     L.swpc_gpu_get_dims.argtypes = [vp, ctypes.POINTER(Dims)]
     L.swpc_gpu_set_zchunk.argtypes = [vp, i]
     L.swpc_gpu_get_zchunk.argtypes = [vp]
+    L.swpc_gpu_set_zchunks.argtypes = [vp, i, i]
+    L.swpc_gpu_get_zchunks.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.swpc_batch_create.argtypes = [ctypes.c_void_p, i, ctypes.POINTER(vp)]
     L.swpc_batch_run.argtypes = [vp, i]
     L.swpc_batch_sync.argtypes = [vp]
@@ -372,6 +374,15 @@ class Simulation:
 
     def zchunk(self):
         return int(lib().swpc_gpu_get_zchunk(self._h))
+
+    def set_zchunks(self, kstress, kvel):
+        """z-sweep depths of the stress and velocity kernels (0: automatic)."""
+        _ck(lib().swpc_gpu_set_zchunks(self._h, int(kstress), int(kvel)))
+
+    def zchunks(self):
+        ks, kv = ctypes.c_int(), ctypes.c_int()
+        _ck(lib().swpc_gpu_get_zchunks(self._h, ctypes.byref(ks), ctypes.byref(kv)))
+        return ks.value, kv.value
 
     def write_sac(self, odir=None):
         _ck(lib().swpc_host_write_sac(self._h, os.fsencode(odir) if odir else None))

@@ -67,7 +67,7 @@ def test_reset_and_autotune_leave_results_unchanged(infs, tmp_path):
     alone = [_alone(f) for f in infs]
     sims = [gpu.Simulation.from_inf(f) for f in infs]
     rec = autotune.tune(sims, cache=str(tmp_path / "tune.json"), steps=3, candidates=(8, 0))
-    assert rec["zchunk"] in (8, 0)
+    assert rec["zchunk"] in (8, 0) and rec["zchunk_vel"] in (8, 0)
     b = gpu.Batch(sims)
     b.run(NT)
     b.sync()
@@ -75,5 +75,7 @@ def test_reset_and_autotune_leave_results_unchanged(infs, tmp_path):
         assert np.array_equal(s.waveforms(), w)
     # a second tuning call is served from the cache
     rec2 = autotune.tune(sims, cache=str(tmp_path / "tune.json"), steps=3, candidates=(8, 0))
-    assert rec2["zchunk"] == rec["zchunk"]
+    assert (rec2["zchunk"], rec2["zchunk_vel"]) == (rec["zchunk"], rec["zchunk_vel"])
+    if rec["zchunk"] and rec["zchunk_vel"]:
+        assert sims[0].zchunks() == (rec["zchunk"], rec["zchunk_vel"])
     b.close()
