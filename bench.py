@@ -249,6 +249,28 @@ def cpu_sample(steps=8, warmup=2, n=(512, 512, 256), dx=0.5, dt=0.02, mode="mixe
                 seconds=el)
 
 
+def parity_statement():
+    """Receiver misfit of the drop-in path (input.inf -> host set-up -> GPU)
+    on the small plain configuration (128x128x64, 200 steps) against the
+    committed golden traces of the oracle's fp32 and fp64 builds, so that
+    every bench line states its error against both."""
+    from openswpc_gb300 import configs, gpu
+    g = np.load(os.path.join(ROOT, "tests", "golden", "plain_small_nt200.npz"))
+    with tempfile.TemporaryDirectory() as d:
+        inf = configs.write_plain_small(d, seed=int(g["seed"]), nt=int(g["nt"]))
+        s = gpu.Simulation.from_inf(inf)
+        s.run(1, int(g["nt"]))
+        s.sync()
+        w = s.waveforms()
+        s.close()
+
+    def mis(a, b):
+        return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+
+    return {"case": "plain 128x128x64, 200 steps, golden traces of the oracle", "metric": "relative L2 receiver misfit",
+            "vs_oracle_fp32": mis(w, g["fp32"]), "vs_oracle_fp64": mis(w, g["fp64"]), "bar": 1e-5}
+
+
 def arm_config(w, args, world):
     """The workload description both arms print."""
     n_int, n_pml = counts(w)
@@ -394,6 +416,7 @@ def run_gpu(args, w):
             "gpu_launches": launches,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "parity": parity_statement(),
             "setup_s": t_setup,
         }
         print(json.dumps(line), flush=True)

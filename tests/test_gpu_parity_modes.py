@@ -67,3 +67,22 @@ def test_body_force_source(tmp_path):
 def test_source_time_functions(tmp_path, stf):
     m = _compare(_shallow(tmp_path, stftype=stf))
     assert max(m.values()) <= 1e-5, (stf, m)
+
+
+@pytest.mark.gpu
+def test_point_force_matches_analytic_whole_space(tmp_path):
+    """The drop-in path against the complete analytic solution of a point
+    force in a uniform whole space (the same case the oracle is pinned on):
+    Vz 8 km along x (S) and along z (P) within 5 % after one common scale,
+    the two scales equal to 1.5 %."""
+    from tests.helpers import point_force_fit, write_point_force_case
+    inf = write_point_force_case(tmp_path)
+    s = gpu.Simulation.from_inf(inf)
+    s.run(1, 300)
+    s.sync()
+    w = s.waveforms()
+    s.close()
+    (a_s, r_s), (a_p, r_p) = point_force_fit(w, 0.02, [np.array([8.0, 0, 0]), np.array([0, 0, 8.0])])
+    print("point force (GPU): S residual %.3f, P residual %.3f, scale ratio %.4f" % (r_s, r_p, a_s / a_p))
+    assert r_s < 0.05 and r_p < 0.05
+    assert abs(a_s / a_p - 1) < 0.015

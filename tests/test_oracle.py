@@ -181,3 +181,24 @@ def test_zener_and_pml_coefficients_closed_form(tmp_path, mode, rtol):
     mid = cf["gxc"][o.nx // 2]
     assert abs(mid[0] - 1) < rtol and mid[3] == 0
     o.close()
+
+
+def test_point_force_matches_analytic_whole_space(tmp_path):
+    """A vertical point force in a uniform whole space against the complete
+    analytic solution (near field, far P, far S): the Vz traces 8 km along x
+    (S) and along z (P) fit it to a few per cent after one common amplitude
+    scale, and the two receivers need the same scale to 1.5 %, so the P/S
+    amplitude ratio, radiation pattern and arrival times are right."""
+    from tests.helpers import point_force_fit, write_point_force_case
+    inf = write_point_force_case(tmp_path)
+    o = pyoracle.Oracle(inf, "fp32")
+    o.run(o.nt)
+    w = o.waveforms()
+    (ijk,), _ = o.sources()
+    st = o.stations()
+    offsets = [((st[q] - ijk) * 0.5).astype(np.float64) for q in range(2)]
+    assert np.allclose(offsets[0], [8, 0, 0]) and np.allclose(offsets[1], [0, 0, 8])
+    (a_s, r_s), (a_p, r_p) = point_force_fit(w, o.dt, offsets)
+    print("point force: S residual %.3f, P residual %.3f, scale ratio %.4f" % (r_s, r_p, a_s / a_p))
+    assert r_s < 0.05 and r_p < 0.05
+    assert abs(a_s / a_p - 1) < 0.015
