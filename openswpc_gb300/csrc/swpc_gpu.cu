@@ -858,9 +858,11 @@ int Sim::allocate() {
     if ((rc = dalloc((void**)&d_kob, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     if ((rc = dalloc((void**)&d_kfs, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     // z chunking: enough blocks to fill the GPU at least ~8 times; then the
-    // stress kernels take chunks of at most 8 planes (neighbouring blocks
-    // sweep the same planes at the same time and share their V halo rows in
-    // L2: 1024x1024x512 stress 17.6, 16.2, 16.0 ms with 492, 16, 8 planes) and
+    // stress kernels take chunks of at most 8 planes with FP32 memory
+    // variables, 32 with 16-bit ones (neighbouring blocks sweep the same
+    // planes at the same time and share their V halo rows in L2:
+    // 1024x1024x512 FP32 stress 17.6, 16.2, 16.0 ms with 492, 16, 8 planes;
+    // FP16 12.18, 11.57, 11.35 ms with 8, 16, 32 planes) and
     // the velocity kernels chunks of at most 128 planes (its longer start-up
     // costs more: 4.67 ms at 492, 4.54 at 123, 4.95 at 16 planes)
     int dev = 0, nsm = 148;
@@ -874,7 +876,7 @@ int Sim::allocate() {
         const int nc = (p.nzi + cap - 1) / cap;
         return (p.nzi + nc - 1) / nc;
     };
-    kchunk = kchunk_auto = even(std::min(kfill, 8));
+    kchunk = kchunk_auto = even(std::min(kfill, p.rbytes == 4 ? 8 : 32));
     kchunk_v = kchunk_v_auto = even(std::min(kfill, 128));
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
