@@ -483,9 +483,15 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     const float lamv = M[P], m000 = M[2 * P], m100 = M[2 * P + planeM], m010 = M[2 * P + 1];
     const float m110 = M[2 * P + planeM + 1], m001 = M[2 * P + rowM], m011 = M[2 * P + rowM + 1];
     const float m101 = M[2 * P + planeM + rowM];
+    // an auxiliary variable whose axis has no damping here (g4 = 0, the
+    // point lies outside that axis's layer) starts at zero and its update
+    // g3 * 0 + 0 keeps it zero: it is neither loaded nor stored.  Order:
+    // axVx ayVy azVz ayVx azVx axVy azVy axVz ayVz
+    const bool live[9] = {gxc.w != 0.f, gyc.w != 0.f, gzc.w != 0.f, gye.w != 0.f, gze.w != 0.f,
+                          gxe.w != 0.f, gze.w != 0.f, gxe.w != 0.f, gye.w != 0.f};
     float ad[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) ad[q] = A[q * AP];
+    for (int q = 0; q < 9; ++q) ad[q] = live[q] ? A[q * AP] : 0.f;
     float sv[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) sv[q] = S[q * P];
@@ -502,9 +508,9 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     S[0] = sv[0] + (lam2mu * dxa + lamR * (dya + dza)) * a.dt;
     S[P] = sv[1] + (lam2mu * dya + lamR * (dxa + dza)) * a.dt;
     S[2 * P] = sv[2] + (lam2mu * dza + lamR * (dxa + dya)) * a.dt;
-    A[0] = gxc.z * ad[0] + gxc.w * dxVx * a.dt;
-    A[AP] = gyc.z * ad[1] + gyc.w * dyVy * a.dt;
-    A[2 * AP] = gzc.z * ad[2] + gzc.w * dzVz * a.dt;
+    if (live[0]) A[0] = gxc.z * ad[0] + gxc.w * dxVx * a.dt;
+    if (live[1]) A[AP] = gyc.z * ad[1] + gyc.w * dyVy * a.dt;
+    if (live[2]) A[2 * AP] = gzc.z * ad[2] + gzc.w * dzVz * a.dt;
     // shear part (m_absorb_p.f90:477-518)
     const float dxVy = (vye - vy) * a.r20x;
     const float dxVz = (vze - vz) * a.r20x;
@@ -522,12 +528,12 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     S[3 * P] = sv[3] + muyz * (gye.x * dyVz + gze.x * dzVy + gye.y * ayVz + gze.y * azVy) * a.dt;
     S[4 * P] = sv[4] + muxz * (gxe.x * dxVz + gze.x * dzVx + gxe.y * axVz + gze.y * azVx) * a.dt;
     S[5 * P] = sv[5] + muxy * (gxe.x * dxVy + gye.x * dyVx + gxe.y * axVy + gye.y * ayVx) * a.dt;
-    A[3 * AP] = gye.z * ayVx + gye.w * dyVx * a.dt;
-    A[4 * AP] = gze.z * azVx + gze.w * dzVx * a.dt;
-    A[5 * AP] = gxe.z * axVy + gxe.w * dxVy * a.dt;
-    A[6 * AP] = gze.z * azVy + gze.w * dzVy * a.dt;
-    A[7 * AP] = gxe.z * axVz + gxe.w * dxVz * a.dt;
-    A[8 * AP] = gye.z * ayVz + gye.w * dyVz * a.dt;
+    if (live[3]) A[3 * AP] = gye.z * ayVx + gye.w * dyVx * a.dt;
+    if (live[4]) A[4 * AP] = gze.z * azVx + gze.w * dzVx * a.dt;
+    if (live[5]) A[5 * AP] = gxe.z * axVy + gxe.w * dxVy * a.dt;
+    if (live[6]) A[6 * AP] = gze.z * azVy + gze.w * dzVy * a.dt;
+    if (live[7]) A[7 * AP] = gxe.z * axVz + gxe.w * dxVz * a.dt;
+    if (live[8]) A[8 * AP] = gye.z * ayVz + gye.w * dyVz * a.dt;
 }
 
 // PML velocity update (m_absorb_p.f90:246-317) at shell point c, loads first.
@@ -557,9 +563,13 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     const float sxzw = S[4 * P - 1], sxzu = S[4 * P - planeS];
     const float sxyw = S[5 * P - 1], sxys = S[5 * P - rowS];
     const float r0 = M[0], rx = M[1], ry = M[rowM], rz = M[planeM];
+    // auxiliaries of undamped axes stay zero (as in the stress update).
+    // Order: axSxx aySxy azSxz axSxy aySyy azSyz axSxz aySyz azSzz
+    const bool live[9] = {gxe.w != 0.f, gyc.w != 0.f, gzc.w != 0.f, gxc.w != 0.f, gye.w != 0.f,
+                          gzc.w != 0.f, gxc.w != 0.f, gyc.w != 0.f, gze.w != 0.f};
     float ad[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) ad[q] = A[q * AP];
+    for (int q = 0; q < 9; ++q) ad[q] = live[q] ? A[q * AP] : 0.f;
     const float v0 = V[0], v1 = V[P], v2 = V[2 * P];
     // m_absorb_p.f90:265-305
     const float dxSxx = (sxxe - sxx) * a.r20x;
@@ -579,15 +589,15 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     V[0] = v0 + bx * (gxe.x * dxSxx + gyc.x * dySxy + gzc.x * dzSxz + gxe.y * axSxx + gyc.y * aySxy + gzc.y * azSxz) * a.dt;
     V[P] = v1 + by * (gxc.x * dxSxy + gye.x * dySyy + gzc.x * dzSyz + gxc.y * axSxy + gye.y * aySyy + gzc.y * azSyz) * a.dt;
     V[2 * P] = v2 + bz * (gxc.x * dxSxz + gyc.x * dySyz + gze.x * dzSzz + gxc.y * axSxz + gyc.y * aySyz + gze.y * azSzz) * a.dt;
-    A[0] = gxe.z * axSxx + gxe.w * dxSxx * a.dt;
-    A[AP] = gyc.z * aySxy + gyc.w * dySxy * a.dt;
-    A[2 * AP] = gzc.z * azSxz + gzc.w * dzSxz * a.dt;
-    A[3 * AP] = gxc.z * axSxy + gxc.w * dxSxy * a.dt;
-    A[4 * AP] = gye.z * aySyy + gye.w * dySyy * a.dt;
-    A[5 * AP] = gzc.z * azSyz + gzc.w * dzSyz * a.dt;
-    A[6 * AP] = gxc.z * axSxz + gxc.w * dxSxz * a.dt;
-    A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
-    A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
+    if (live[0]) A[0] = gxe.z * axSxx + gxe.w * dxSxx * a.dt;
+    if (live[1]) A[AP] = gyc.z * aySxy + gyc.w * dySxy * a.dt;
+    if (live[2]) A[2 * AP] = gzc.z * azSxz + gzc.w * dzSxz * a.dt;
+    if (live[3]) A[3 * AP] = gxc.z * axSxy + gxc.w * dxSxy * a.dt;
+    if (live[4]) A[4 * AP] = gye.z * aySyy + gye.w * dySyy * a.dt;
+    if (live[5]) A[5 * AP] = gzc.z * azSyz + gzc.w * dzSyz * a.dt;
+    if (live[6]) A[6 * AP] = gxc.z * axSxz + gxc.w * dxSxz * a.dt;
+    if (live[7]) A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
+    if (live[8]) A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
 }
 
 __device__ __forceinline__ void stress_pml_pt(const PArgs& a, const long long p) {
