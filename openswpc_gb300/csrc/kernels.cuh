@@ -614,9 +614,12 @@ __device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
 #define PML_TPB 128
 #endif
 constexpr int PTPB = PML_TPB;
-__global__ void __launch_bounds__(PTPB) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
+// the stress PML fits 72 registers without spilling, so 7 blocks (28 warps)
+// stay resident per SM instead of 6: 11 % faster (the velocity PML spills at
+// 80 and stays at 94 registers)
+__global__ void __launch_bounds__(PTPB, 7) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
 __global__ void __launch_bounds__(PTPB) k_vel_pml(const PArgs a) { vel_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
-__global__ void __launch_bounds__(PTPB) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+__global__ void __launch_bounds__(PTPB, 7) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
     const int2 e = blocks[blockIdx.x];
     stress_pml_pt(all[e.x], e.y * (long long)PTPB + threadIdx.x);
 }
