@@ -407,11 +407,9 @@ __global__ void __launch_bounds__(TBX * TBY, 2) k_vel_interior(const ZArgs a) {
 // ---------------------------------------------------------------------------
 struct PmlBox {
     int x0, y0, z0, nx, ny, nz;
-    int pitch;           // ADE row pitch
+    int pitch;           // ADE row pitch (= nx: rows stored without padding)
     long long off;       // offset of this box in the ADE buffers (elements)
     long long first;     // first point of this box in the shell (points are counted box by box)
-    // launch tiling: 32 x TBY column tiles, each sweeping a chunk of zc planes
-    int tiles_x, tiles_y, zc, nzc, first_block;
 };
 
 struct PArgs {

@@ -21,7 +21,6 @@ struct Plan {
     long long nV, nS, nM, nR, nade, npml, bytes;
     PmlBox box[5];
     int nbox;
-    int pml_blocks;
 };
 
 struct Sim {

@@ -67,7 +67,6 @@ static int plan(const swpc_dims* d, Plan& p) {
     // PML shell boxes
     p.nbox = 0;
     p.nade = 0;
-    p.pml_blocks = 0;
     long long first = 0;
     if (p.pml) {
         const int na = d->na, nx = d->nx, ny = d->ny, nz = d->nz;
@@ -80,12 +79,6 @@ static int plan(const swpc_dims* d, Plan& p) {
             B.pitch = B.nx;  // rows of one point contiguous: no partly used lines in the 20-wide x-side boxes
             B.off = p.nade;
             B.first = first;
-            B.tiles_x = (B.nx + 31) / 32;
-            B.tiles_y = (B.ny + TBY - 1) / TBY;
-            B.zc = std::min(B.nz, 32);
-            B.nzc = (B.nz + B.zc - 1) / B.zc;
-            B.first_block = p.pml_blocks;
-            p.pml_blocks += B.tiles_x * B.tiles_y * B.nzc;
             p.nade += 9LL * B.pitch * B.ny * B.nz;
             first += (long long)B.nx * B.ny * B.nz;
         }
