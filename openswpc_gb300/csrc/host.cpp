@@ -296,7 +296,7 @@ void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& 
                 for (int f = 0; f < 5; ++f) std::copy(src[f]->begin(), src[f]->end(), dst[f]->begin() + b);
             }
     };
-    if (inf.b("earth_flattening", false)) throw std::runtime_error("earth_flattening is not supported by this build");
+    if (inf.b("earth_flattening", false)) throw std::runtime_error("earth_flattening is not supported by openswpc_gb300");
     if (p.vmodel_type == "uni") {
         double vp0 = inf.r("vp0", 5.0), vs0 = inf.r("vs0", vp0 / std::sqrt(3.0)), rho0 = inf.r("rho0", 2.7);
         double qp0 = inf.r("qp0", 1e6), qs0 = inf.r("qs0", 1e6), topo0 = inf.r("topo0", 0.0);
@@ -311,7 +311,7 @@ void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& 
         return;
     }
     if (p.vmodel_type != "lhm" && p.vmodel_type != "lgm")
-        throw std::runtime_error("vmodel_type '" + p.vmodel_type + "' is not supported by this build (uni, lhm, lgm)");
+        throw std::runtime_error("vmodel_type '" + p.vmodel_type + "' is not supported by openswpc_gb300 (uni, lhm, lgm)");
     auto rows = table_rows(inf.path(inf.s("fn_lhm", "")));
     const int nl = (int)rows.size();
     if (nl < 1) throw std::runtime_error("empty layer table");
@@ -777,7 +777,7 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     Inf inf(inf_path);
     inf.strict = inf.b("strict_mode", false);
     Params p;
-    if (inf.b("benchmark_mode", false)) throw std::runtime_error("benchmark_mode is not supported by this build");
+    if (inf.b("benchmark_mode", false)) throw std::runtime_error("benchmark_mode is not supported by openswpc_gb300");
     p.title = inf.s("title", "swpc3d"); p.odir = inf.s("odir", "./out");
     p.nx = inf.i("nx", 256); p.ny = inf.i("ny", 256); p.nz = inf.i("nz", 256); p.nt = inf.i("nt", 1000);
     p.dx = inf.r("dx", 0.5); p.dy = inf.r("dy", 0.5); p.dz = inf.r("dz", 0.5); p.dt = inf.r("dt", 0.01);
@@ -839,7 +839,7 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     if (p.idec < 1 || p.jdec < 1 || p.kdec < 1 || p.ntdec_s < 1)
         throw std::runtime_error("idec, jdec, kdec and ntdec_s must be positive");
     if (inf.s("snp_format", "native") != "native")
-        std::fprintf(stderr, "swpc: snp_format other than native is written as native by this build\n");
+        std::fprintf(stderr, "swpc: snp_format other than native is written as native by openswpc_gb300\n");
     if (p.nt < 1) throw std::runtime_error("nt must be positive");
 
     Grid G{p.nx, p.ny, p.nz};
@@ -1448,7 +1448,7 @@ int swpc_host_write_green(swpc_sim* sim, const char* odir) {
                                image(n, c));
             }
         } else {
-            return swpc::set_err(SWPC_E_ARG, "Green's-function output is written as sac or csf by this build");
+            return swpc::set_err(SWPC_E_ARG, "Green's-function output is written as sac or csf by openswpc_gb300");
         }
         return 0;
     } catch (const std::exception& e) {

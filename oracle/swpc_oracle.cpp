@@ -1,7 +1,7 @@
 // swpc_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
 //
-// A plain CPU restatement of OpenSWPC's swpc_3d time-stepping path, used as
-// the checker for the CUDA implementation in openswpc_gb300/.  Nothing in the
+// A plain CPU restatement of OpenSWPC's swpc_3d time-stepping path, against
+// which the tests compare the CUDA implementation in openswpc_gb300/.  Nothing in the
 // product links or calls this file; only tests/, __graft_entry__.smoke() and
 // bench.py's CPU baseline (and its --impl reference arm) load it.
 //
