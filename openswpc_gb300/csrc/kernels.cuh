@@ -409,7 +409,23 @@ struct PmlBox {
     int x0, y0, z0, nx, ny, nz;
     int pitch;           // ADE row pitch (= nx: rows stored without padding)
     long long off;       // offset of this box in the ADE buffers (elements)
-    long long first;     // first point of this box in the shell (points are counted box by box)
+};
+
+// threads (shell points) per block of the PML kernels
+#ifndef PML_TPB
+#define PML_TPB 128
+#endif
+constexpr int PTPB = PML_TPB;
+
+// A launch of a PML kernel covers a list of parts: sub-boxes of the five ADE
+// boxes in which the set of damped axes is the same at every point.  Each
+// part starts on a block boundary, so a block belongs to one part.
+constexpr int PML_MAXPART = 40;
+struct PmlPart {
+    int b;             // parent box (ADE storage and origin)
+    int x0, y0, z0;    // origin inside the parent box
+    int nx, ny, nz;    // extents
+    int first_block;   // first block of this part in its launch
 };
 
 struct PArgs {
@@ -423,36 +439,55 @@ struct PArgs {
     int pxc, pxe, pyc, pye, pzc, pze;  // offsets of each profile (array of 4*n, l fastest)
     PmlBox box[5];
     int nbox;
-    long long npts;
+    PmlPart part[PML_MAXPART];
+    int npart;
+    int nblocks;        // blocks of this launch (0: nothing to do)
     float r20x, r20y, r20z, dt;
 };
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
-// Shell point p -> (box, x, y, z): points are numbered box by box, x fastest.
-// The per-box count fits in 32 bits, so the decomposition is two 32-bit
-// divisions by the box extents.
+// Block blk, thread t of a launch -> shell point (box, x, y, z in the box):
+// the block's part is found by a binary search over the parts' first blocks
+// (the same for every thread of the block); inside the part, points run x
+// fastest.  False for the threads past the end of the part.
 struct PmlPt {
     int b, lx, ly, lz;
 };
-__device__ __forceinline__ PmlPt pml_point(const PArgs& a, long long p) {
-    PmlPt r;
-    r.b = 0;
-#pragma unroll
-    for (int q = 1; q < 5; ++q)
-        if (q < a.nbox && p >= a.box[q].first) r.b = q;
-    const PmlBox& B = a.box[r.b];
-    const unsigned q = (unsigned)(p - B.first);
-    const unsigned t = q / (unsigned)B.nx;
-    r.lx = (int)(q - t * (unsigned)B.nx);
-    r.lz = (int)(t / (unsigned)B.ny);
-    r.ly = (int)(t - (unsigned)r.lz * (unsigned)B.ny);
-    return r;
+__device__ __forceinline__ bool pml_point(const PArgs& a, int blk, int t, PmlPt& r) {
+    int lo = 0, hi = a.npart - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.part[mid].first_block <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    const PmlPart& P = a.part[lo];
+    const unsigned q = (unsigned)((blk - P.first_block) * PTPB + t);
+    if (q >= (unsigned)P.nx * (unsigned)P.ny * (unsigned)P.nz) return false;
+    const unsigned u = q / (unsigned)P.nx;
+    const unsigned lz = u / (unsigned)P.ny;
+    r.b = P.b;
+    r.lx = P.x0 + (int)(q - u * (unsigned)P.nx);
+    r.ly = P.y0 + (int)(u - lz * (unsigned)P.ny);
+    r.lz = P.z0 + (int)lz;
+    return true;
+}
+
+// Damping profile (g1 g2 g3 g4) of one axis at index i.  An axis that is not
+// damped anywhere in a part (bit clear in MASK) has g1 = 1 and g4 = 0 at
+// every point of it, so its ADE auxiliaries stay zero: it takes the constant
+// (1, -1, 1, 0) instead of loading, which yields the same results bit for
+// bit (g2 and g3 only ever multiply the zero auxiliaries).
+template <int MASK, int AX>
+__device__ __forceinline__ float4 pml_prof(const PArgs& a, int off, int i) {
+    if (MASK & (1 << AX)) return ld4(a.prof + off + 4 * i);
+    return make_float4(1.f, -1.f, 1.f, 0.f);
 }
 
 // PML stress update (m_absorb_p.f90:429-531) at shell point c.  Every load
 // is issued before any arithmetic or store, so a thread has all of its ~40
 // independent loads in flight at once (the kernel is bound by load latency).
+template <int MASK>
 __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
@@ -471,9 +506,9 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     float* __restrict__ A = a.adeV + oA;
     const int AP = B.pitch;
     // loads
-    const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
-    const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
-    const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
+    const float4 gxc = pml_prof<MASK, 0>(a, a.pxc, ix), gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
+    const float4 gyc = pml_prof<MASK, 1>(a, a.pyc, jy), gye = pml_prof<MASK, 1>(a, a.pye, jy);
+    const float4 gzc = pml_prof<MASK, 2>(a, a.pzc, kz), gze = pml_prof<MASK, 2>(a, a.pze, kz);
     const float vx = V[0], vy = V[P], vz = V[2 * P];
     const float vxw = V[-1], vys = V[P - rowV], vzu = V[2 * P - planeV];
     const float vye = V[P + 1], vze = V[2 * P + 1], vxn = V[rowV], vzn = V[2 * P + rowV];
@@ -493,48 +528,68 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     float sv[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) sv[q] = S[q * P];
+    // every operation below is an explicitly rounded intrinsic, so that the
+    // kernels specialised to one damped axis (profile constants 1, -1, 1, 0)
+    // and the general kernel produce the same bits: the compiler may not
+    // contract or reorder them differently around the constants
+    const float dt = a.dt;
     // normal part (m_absorb_p.f90:453-474)
-    const float dxVx = (vx - vxw) * a.r20x;
-    const float dyVy = (vy - vys) * a.r20y;
-    const float dzVz = (vz - vzu) * a.r20z;
-    const float muv = m000;
-    const float lam2mu = lamv + 2.f * muv;
-    const float lamR = lam2mu - 2.f * muv;
-    const float dxa = gxc.x * dxVx + gxc.y * ad[0];
-    const float dya = gyc.x * dyVy + gyc.y * ad[1];
-    const float dza = gzc.x * dzVz + gzc.y * ad[2];
-    S[0] = sv[0] + (lam2mu * dxa + lamR * (dya + dza)) * a.dt;
-    S[P] = sv[1] + (lam2mu * dya + lamR * (dxa + dza)) * a.dt;
-    S[2 * P] = sv[2] + (lam2mu * dza + lamR * (dxa + dya)) * a.dt;
-    if (live[0]) A[0] = gxc.z * ad[0] + gxc.w * dxVx * a.dt;
-    if (live[1]) A[AP] = gyc.z * ad[1] + gyc.w * dyVy * a.dt;
-    if (live[2]) A[2 * AP] = gzc.z * ad[2] + gzc.w * dzVz * a.dt;
+    const float dxVx = __fmul_rn(__fsub_rn(vx, vxw), a.r20x);
+    const float dyVy = __fmul_rn(__fsub_rn(vy, vys), a.r20y);
+    const float dzVz = __fmul_rn(__fsub_rn(vz, vzu), a.r20z);
+    const float lam2mu = __fmaf_rn(2.f, m000, lamv);
+    const float lamR = __fmaf_rn(-2.f, m000, lam2mu);
+    const float dxa = __fmaf_rn(gxc.y, ad[0], __fmul_rn(gxc.x, dxVx));
+    const float dya = __fmaf_rn(gyc.y, ad[1], __fmul_rn(gyc.x, dyVy));
+    const float dza = __fmaf_rn(gzc.y, ad[2], __fmul_rn(gzc.x, dzVz));
+    S[0] = __fmaf_rn(__fmaf_rn(lam2mu, dxa, __fmul_rn(lamR, __fadd_rn(dya, dza))), dt, sv[0]);
+    S[P] = __fmaf_rn(__fmaf_rn(lam2mu, dya, __fmul_rn(lamR, __fadd_rn(dxa, dza))), dt, sv[1]);
+    S[2 * P] = __fmaf_rn(__fmaf_rn(lam2mu, dza, __fmul_rn(lamR, __fadd_rn(dxa, dya))), dt, sv[2]);
+    auto ade = [dt](float4 gp, float aux, float d) { return __fmaf_rn(gp.z, aux, __fmul_rn(__fmul_rn(gp.w, d), dt)); };
+    if (live[0]) A[0] = ade(gxc, ad[0], dxVx);
+    if (live[1]) A[AP] = ade(gyc, ad[1], dyVy);
+    if (live[2]) A[2 * AP] = ade(gzc, ad[2], dzVz);
     // shear part (m_absorb_p.f90:477-518)
-    const float dxVy = (vye - vy) * a.r20x;
-    const float dxVz = (vze - vz) * a.r20x;
-    const float dyVx = (vxn - vx) * a.r20y;
-    const float dyVz = (vzn - vz) * a.r20y;
-    const float dzVx = (vxd - vx) * a.r20z;
-    const float dzVy = (vyd - vy) * a.r20z;
-    const float muxz = 4.f * m000 * m100 * m010 * m110 /
-                       (m000 * m100 * m010 + m000 * m100 * m110 + m000 * m010 * m110 + m100 * m010 * m110 + eps);
-    const float muxy = 4.f * m000 * m010 * m001 * m011 /
-                       (m000 * m010 * m001 + m000 * m010 * m011 + m000 * m001 * m011 + m010 * m001 * m011 + eps);
-    const float muyz = 4.f * m000 * m100 * m001 * m101 /
-                       (m000 * m100 * m001 + m000 * m100 * m101 + m000 * m001 * m101 + m100 * m001 * m101 + eps);
+    const float dxVy = __fmul_rn(__fsub_rn(vye, vy), a.r20x);
+    const float dxVz = __fmul_rn(__fsub_rn(vze, vz), a.r20x);
+    const float dyVx = __fmul_rn(__fsub_rn(vxn, vx), a.r20y);
+    const float dyVz = __fmul_rn(__fsub_rn(vzn, vz), a.r20y);
+    const float dzVx = __fmul_rn(__fsub_rn(vxd, vx), a.r20z);
+    const float dzVy = __fmul_rn(__fsub_rn(vyd, vy), a.r20z);
+    // harmonic mean of four moduli: 4 m1 m2 m3 m4 / (sum of the triple products + eps)
+    auto hmean = [eps](float m1, float m2, float m3, float m4) {
+        const float num = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(4.f, m1), m2), m3), m4);
+        const float m12 = __fmul_rn(m1, m2);
+        float den = __fmul_rn(m12, m3);
+        den = __fadd_rn(den, __fmul_rn(m12, m4));
+        den = __fadd_rn(den, __fmul_rn(__fmul_rn(m1, m3), m4));
+        den = __fadd_rn(den, __fmul_rn(__fmul_rn(m2, m3), m4));
+        return __fdiv_rn(num, __fadd_rn(den, eps));
+    };
+    const float muxz = hmean(m000, m100, m010, m110);
+    const float muxy = hmean(m000, m010, m001, m011);
+    const float muyz = hmean(m000, m100, m001, m101);
     const float ayVx = ad[3], azVx = ad[4], axVy = ad[5], azVy = ad[6], axVz = ad[7], ayVz = ad[8];
-    S[3 * P] = sv[3] + muyz * (gye.x * dyVz + gze.x * dzVy + gye.y * ayVz + gze.y * azVy) * a.dt;
-    S[4 * P] = sv[4] + muxz * (gxe.x * dxVz + gze.x * dzVx + gxe.y * axVz + gze.y * azVx) * a.dt;
-    S[5 * P] = sv[5] + muxy * (gxe.x * dxVy + gye.x * dyVx + gxe.y * axVy + gye.y * ayVx) * a.dt;
-    if (live[3]) A[3 * AP] = gye.z * ayVx + gye.w * dyVx * a.dt;
-    if (live[4]) A[4 * AP] = gze.z * azVx + gze.w * dzVx * a.dt;
-    if (live[5]) A[5 * AP] = gxe.z * axVy + gxe.w * dxVy * a.dt;
-    if (live[6]) A[6 * AP] = gze.z * azVy + gze.w * dzVy * a.dt;
-    if (live[7]) A[7 * AP] = gxe.z * axVz + gxe.w * dxVz * a.dt;
-    if (live[8]) A[8 * AP] = gye.z * ayVz + gye.w * dyVz * a.dt;
+    // (g1 d1 + g1' d2 + g2 a1 + g2' a2) in a fixed order
+    auto sum4 = [](float4 p, float d1, float4 q, float d2, float a1, float a2) {
+        float t = __fmul_rn(p.x, d1);
+        t = __fmaf_rn(q.x, d2, t);
+        t = __fmaf_rn(p.y, a1, t);
+        return __fmaf_rn(q.y, a2, t);
+    };
+    S[3 * P] = __fmaf_rn(__fmul_rn(muyz, sum4(gye, dyVz, gze, dzVy, ayVz, azVy)), dt, sv[3]);
+    S[4 * P] = __fmaf_rn(__fmul_rn(muxz, sum4(gxe, dxVz, gze, dzVx, axVz, azVx)), dt, sv[4]);
+    S[5 * P] = __fmaf_rn(__fmul_rn(muxy, sum4(gxe, dxVy, gye, dyVx, axVy, ayVx)), dt, sv[5]);
+    if (live[3]) A[3 * AP] = ade(gye, ayVx, dyVx);
+    if (live[4]) A[4 * AP] = ade(gze, azVx, dzVx);
+    if (live[5]) A[5 * AP] = ade(gxe, axVy, dxVy);
+    if (live[6]) A[6 * AP] = ade(gze, azVy, dzVy);
+    if (live[7]) A[7 * AP] = ade(gxe, axVz, dxVz);
+    if (live[8]) A[8 * AP] = ade(gye, ayVz, dyVz);
 }
 
 // PML velocity update (m_absorb_p.f90:246-317) at shell point c, loads first.
+template <int MASK>
 __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
@@ -552,9 +607,9 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     float* __restrict__ A = a.adeS + oA;
     const int AP = B.pitch;
     // loads
-    const float4 gxc = ld4(a.prof + a.pxc + 4 * ix), gxe = ld4(a.prof + a.pxe + 4 * ix);
-    const float4 gyc = ld4(a.prof + a.pyc + 4 * jy), gye = ld4(a.prof + a.pye + 4 * jy);
-    const float4 gzc = ld4(a.prof + a.pzc + 4 * kz), gze = ld4(a.prof + a.pze + 4 * kz);
+    const float4 gxc = pml_prof<MASK, 0>(a, a.pxc, ix), gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
+    const float4 gyc = pml_prof<MASK, 1>(a, a.pyc, jy), gye = pml_prof<MASK, 1>(a, a.pye, jy);
+    const float4 gzc = pml_prof<MASK, 2>(a, a.pzc, kz), gze = pml_prof<MASK, 2>(a, a.pze, kz);
     const float sxx = S[0], syy = S[P], szz = S[2 * P], syz = S[3 * P], sxz = S[4 * P], sxy = S[5 * P];
     const float sxxe = S[1], syyn = S[P + rowS], szzd = S[2 * P + planeS];
     const float syzs = S[3 * P - rowS], syzu = S[3 * P - planeS];
@@ -569,62 +624,78 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
 #pragma unroll
     for (int q = 0; q < 9; ++q) ad[q] = live[q] ? A[q * AP] : 0.f;
     const float v0 = V[0], v1 = V[P], v2 = V[2 * P];
+    // explicitly rounded operations, as in the stress update
+    const float dt = a.dt;
     // m_absorb_p.f90:265-305
-    const float dxSxx = (sxxe - sxx) * a.r20x;
-    const float dySyy = (syyn - syy) * a.r20y;
-    const float dzSzz = (szzd - szz) * a.r20z;
-    const float dySyz = (syz - syzs) * a.r20y;
-    const float dzSyz = (syz - syzu) * a.r20z;
-    const float dxSxz = (sxz - sxzw) * a.r20x;
-    const float dzSxz = (sxz - sxzu) * a.r20z;
-    const float dxSxy = (sxy - sxyw) * a.r20x;
-    const float dySxy = (sxy - sxys) * a.r20y;
-    const float bx = 2.f / (r0 + rx);
-    const float by = 2.f / (r0 + ry);
-    const float bz = 2.f / (r0 + rz);
+    const float dxSxx = __fmul_rn(__fsub_rn(sxxe, sxx), a.r20x);
+    const float dySyy = __fmul_rn(__fsub_rn(syyn, syy), a.r20y);
+    const float dzSzz = __fmul_rn(__fsub_rn(szzd, szz), a.r20z);
+    const float dySyz = __fmul_rn(__fsub_rn(syz, syzs), a.r20y);
+    const float dzSyz = __fmul_rn(__fsub_rn(syz, syzu), a.r20z);
+    const float dxSxz = __fmul_rn(__fsub_rn(sxz, sxzw), a.r20x);
+    const float dzSxz = __fmul_rn(__fsub_rn(sxz, sxzu), a.r20z);
+    const float dxSxy = __fmul_rn(__fsub_rn(sxy, sxyw), a.r20x);
+    const float dySxy = __fmul_rn(__fsub_rn(sxy, sxys), a.r20y);
+    const float bx = __fdiv_rn(2.f, __fadd_rn(r0, rx));
+    const float by = __fdiv_rn(2.f, __fadd_rn(r0, ry));
+    const float bz = __fdiv_rn(2.f, __fadd_rn(r0, rz));
     const float axSxx = ad[0], aySxy = ad[1], azSxz = ad[2], axSxy = ad[3], aySyy = ad[4];
     const float azSyz = ad[5], axSxz = ad[6], aySyz = ad[7], azSzz = ad[8];
-    V[0] = v0 + bx * (gxe.x * dxSxx + gyc.x * dySxy + gzc.x * dzSxz + gxe.y * axSxx + gyc.y * aySxy + gzc.y * azSxz) * a.dt;
-    V[P] = v1 + by * (gxc.x * dxSxy + gye.x * dySyy + gzc.x * dzSyz + gxc.y * axSxy + gye.y * aySyy + gzc.y * azSyz) * a.dt;
-    V[2 * P] = v2 + bz * (gxc.x * dxSxz + gyc.x * dySyz + gze.x * dzSzz + gxc.y * axSxz + gyc.y * aySyz + gze.y * azSzz) * a.dt;
-    if (live[0]) A[0] = gxe.z * axSxx + gxe.w * dxSxx * a.dt;
-    if (live[1]) A[AP] = gyc.z * aySxy + gyc.w * dySxy * a.dt;
-    if (live[2]) A[2 * AP] = gzc.z * azSxz + gzc.w * dzSxz * a.dt;
-    if (live[3]) A[3 * AP] = gxc.z * axSxy + gxc.w * dxSxy * a.dt;
-    if (live[4]) A[4 * AP] = gye.z * aySyy + gye.w * dySyy * a.dt;
-    if (live[5]) A[5 * AP] = gzc.z * azSyz + gzc.w * dzSyz * a.dt;
-    if (live[6]) A[6 * AP] = gxc.z * axSxz + gxc.w * dxSxz * a.dt;
-    if (live[7]) A[7 * AP] = gyc.z * aySyz + gyc.w * dySyz * a.dt;
-    if (live[8]) A[8 * AP] = gze.z * azSzz + gze.w * dzSzz * a.dt;
+    // (g1 d1 + g1' d2 + g1'' d3 + g2 a1 + g2' a2 + g2'' a3) in a fixed order
+    auto sum6 = [](float4 p, float d1, float4 q, float d2, float4 r, float d3, float a1, float a2, float a3) {
+        float t = __fmul_rn(p.x, d1);
+        t = __fmaf_rn(q.x, d2, t);
+        t = __fmaf_rn(r.x, d3, t);
+        t = __fmaf_rn(p.y, a1, t);
+        t = __fmaf_rn(q.y, a2, t);
+        return __fmaf_rn(r.y, a3, t);
+    };
+    V[0] = __fmaf_rn(__fmul_rn(bx, sum6(gxe, dxSxx, gyc, dySxy, gzc, dzSxz, axSxx, aySxy, azSxz)), dt, v0);
+    V[P] = __fmaf_rn(__fmul_rn(by, sum6(gxc, dxSxy, gye, dySyy, gzc, dzSyz, axSxy, aySyy, azSyz)), dt, v1);
+    V[2 * P] = __fmaf_rn(__fmul_rn(bz, sum6(gxc, dxSxz, gyc, dySyz, gze, dzSzz, axSxz, aySyz, azSzz)), dt, v2);
+    auto ade = [dt](float4 gp, float aux, float d) { return __fmaf_rn(gp.z, aux, __fmul_rn(__fmul_rn(gp.w, d), dt)); };
+    if (live[0]) A[0] = ade(gxe, axSxx, dxSxx);
+    if (live[1]) A[AP] = ade(gyc, aySxy, dySxy);
+    if (live[2]) A[2 * AP] = ade(gzc, azSxz, dzSxz);
+    if (live[3]) A[3 * AP] = ade(gxc, axSxy, dxSxy);
+    if (live[4]) A[4 * AP] = ade(gye, aySyy, dySyy);
+    if (live[5]) A[5 * AP] = ade(gzc, azSyz, dzSyz);
+    if (live[6]) A[6 * AP] = ade(gxc, axSxz, dxSxz);
+    if (live[7]) A[7 * AP] = ade(gyc, aySyz, dySyz);
+    if (live[8]) A[8 * AP] = ade(gze, azSzz, dzSzz);
 }
 
-__device__ __forceinline__ void stress_pml_pt(const PArgs& a, const long long p) {
-    if (p < a.npts) stress_pml_at(a, pml_point(a, p));
+// One thread per shell point.  MASK: the axes damped somewhere in the parts
+// of the launch (7 = any, checked per point).  With one damped axis the
+// kernels skip two thirds of the auxiliaries and profiles and fit 64
+// registers without spilling (8 blocks per SM); the general stress kernel
+// fits 72 (7 blocks), the general velocity kernel needs 94.
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_stress_pml(const PArgs a) {
+    PmlPt c;
+    if (pml_point(a, blockIdx.x, threadIdx.x, c)) stress_pml_at<MASK>(a, c);
 }
-__device__ __forceinline__ void vel_pml_pt(const PArgs& a, const long long p) {
-    if (p < a.npts) vel_pml_at(a, pml_point(a, p));
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml(const PArgs a) {
+    PmlPt c;
+    if (pml_point(a, blockIdx.x, threadIdx.x, c)) vel_pml_at<MASK>(a, c);
 }
-
-// one thread per shell point; batched: block b covers points
-// [PTPB e.y, PTPB e.y + PTPB) of simulation e.x, e = blocks[b]
-// threads (shell points) per block of the PML kernels
-#ifndef PML_TPB
-#define PML_TPB 128
-#endif
-constexpr int PTPB = PML_TPB;
-// the stress PML fits 72 registers without spilling, so 7 blocks (28 warps)
-// stay resident per SM instead of 6: 11 % faster (the velocity PML spills at
-// 80 and stays at 94 registers)
-__global__ void __launch_bounds__(PTPB, 7) k_stress_pml(const PArgs a) { stress_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
-__global__ void __launch_bounds__(PTPB) k_vel_pml(const PArgs a) { vel_pml_pt(a, blockIdx.x * (long long)PTPB + threadIdx.x); }
-__global__ void __launch_bounds__(PTPB, 7) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+// batched: block b is block e.y of member e.x's launch, e = blocks[b]
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
     const int2 e = blocks[blockIdx.x];
-    stress_pml_pt(all[e.x], e.y * (long long)PTPB + threadIdx.x);
+    PmlPt c;
+    if (pml_point(all[e.x], e.y, threadIdx.x, c)) stress_pml_at<MASK>(all[e.x], c);
 }
-__global__ void __launch_bounds__(PTPB) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
     const int2 e = blocks[blockIdx.x];
-    vel_pml_pt(all[e.x], e.y * (long long)PTPB + threadIdx.x);
+    PmlPt c;
+    if (pml_point(all[e.x], e.y, threadIdx.x, c)) vel_pml_at<MASK>(all[e.x], c);
 }
+// the launch classes: x only, y only, z only, any
+constexpr int PML_NCLASS = 4;
+constexpr int PML_CLASS_MASK[PML_NCLASS] = {1, 2, 4, 7};
 
 // ---------------------------------------------------------------------------
 // Sources, receivers, snapshots, divergence check

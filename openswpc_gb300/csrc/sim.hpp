@@ -52,7 +52,10 @@ struct Sim {
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
     size_t smem_stress = 0, smem_vel = 0;
 
-    PArgs pml_args{};
+    PArgs pml_args{};                 // pointers, profiles and boxes of the PML kernels
+    PArgs pml_cls[PML_NCLASS]{};      // the same with the parts of each launch class
+    PArgs pml_all{};                  // the same with the whole boxes, for one general launch
+    bool pml_split = false;           // launch the classes separately
     SrcArgs src_args{};
     TapArgs tap_args{};
     SnapArgs snap_args{};
@@ -72,6 +75,8 @@ struct Sim {
     ~Sim();
     int dalloc(void** ptr, size_t bytes);
     int allocate();
+    void plan_pml_parts(const std::vector<float>& prof);
+    void launch_pml(bool stress, cudaStream_t st);
     int upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
                       const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
                       const int* kob_bot, const double* ts, bool column);

@@ -78,7 +78,6 @@ static int plan(const swpc_dims* d, Plan& p) {
             B.x0 = bx[b][0]; B.y0 = bx[b][1]; B.z0 = bx[b][2]; B.nx = bx[b][3]; B.ny = bx[b][4]; B.nz = bx[b][5];
             B.pitch = B.nx;  // rows of one point contiguous: no partly used lines in the 20-wide x-side boxes
             B.off = p.nade;
-            B.first = first;
             p.nade += 9LL * B.pitch * B.ny * B.nz;
             first += (long long)B.nx * B.ny * B.nz;
         }
@@ -138,6 +137,30 @@ void Sim::fill_zargs(ZArgs& z) const {
     z.c = coef;
 }
 
+// the PML stress (or velocity) update: one launch per class that has parts
+void Sim::launch_pml(bool stress, cudaStream_t st) {
+    if (!pml_split) {
+        if (pml_all.nblocks == 0) return;
+        const unsigned nb = (unsigned)pml_all.nblocks;
+        if (stress) k_stress_pml<7><<<nb, PTPB, 0, st>>>(pml_all);
+        else k_vel_pml<7><<<nb, PTPB, 0, st>>>(pml_all);
+        ++launches;
+        return;
+    }
+    for (int q = 0; q < PML_NCLASS; ++q) {
+        const PArgs& a = pml_cls[q];
+        if (a.nblocks == 0) continue;
+        const unsigned nb = (unsigned)a.nblocks;
+        switch (PML_CLASS_MASK[q]) {
+        case 1: stress ? k_stress_pml<1><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<1><<<nb, PTPB, 0, st>>>(a); break;
+        case 2: stress ? k_stress_pml<2><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<2><<<nb, PTPB, 0, st>>>(a); break;
+        case 4: stress ? k_stress_pml<4><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<4><<<nb, PTPB, 0, st>>>(a); break;
+        default: stress ? k_stress_pml<7><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<7><<<nb, PTPB, 0, st>>>(a); break;
+        }
+        ++launches;
+    }
+}
+
 int Sim::launch_step(bool timed) {
     const dim3 blk(TBX, TBY);
     const dim3 grd((p.nxi + TBX - 1) / TBX, (p.nyi + TBY - 1) / TBY, (p.nzi + kchunk - 1) / kchunk);
@@ -185,7 +208,7 @@ int Sim::launch_step(bool timed) {
     }
     if (p.pml) {
         ev0(2, sp);
-        k_stress_pml<<<(unsigned)((p.npml + PTPB - 1) / PTPB), PTPB, 0, sp>>>(pml_args); ++launches;
+        launch_pml(true, sp);
         ev1(2, sp);
         if (two) cudaEventRecord(ev_join, stream2);
     }
@@ -214,7 +237,7 @@ int Sim::launch_step(bool timed) {
     }
     if (p.pml) {
         ev0(3, sp);
-        k_vel_pml<<<(unsigned)((p.npml + PTPB - 1) / PTPB), PTPB, 0, sp>>>(pml_args); ++launches;
+        launch_pml(false, sp);
         ev1(3, sp);
         if (two) cudaEventRecord(ev_join2, stream2);
     }
@@ -899,6 +922,95 @@ static const float* pinned_view(const float* h) {
     return at.type == cudaMemoryTypeHost && at.devicePointer ? static_cast<const float*>(at.devicePointer) : nullptr;
 }
 
+// Split the PML boxes into parts with the same damped axes at every point
+// and sort the parts into the launch classes of PML_CLASS_MASK (x, y or z
+// alone; anything else).  An axis index counts as damped when g4 of its
+// centre or edge profile is not zero, read from the profiles themselves, so
+// the split is exact whatever the rounding of the layer edges.  When the
+// damped indices of an axis are not its two end runs, or a class would hold
+// more than PML_MAXPART parts, every box goes to the general class whole.
+void Sim::plan_pml_parts(const std::vector<float>& prof) {
+    const PArgs& a = pml_args;
+    const int n[3] = {p.g.nx, p.g.ny, p.g.nz};
+    const int oc[3] = {a.pxc, a.pyc, a.pzc}, oe[3] = {a.pxe, a.pye, a.pze};
+    std::vector<char> damp[3];
+    bool ends_only = true;
+    for (int ax = 0; ax < 3; ++ax) {
+        damp[ax].resize(n[ax]);
+        for (int i = 0; i < n[ax]; ++i)
+            damp[ax][i] = prof[oc[ax] + 4 * i + 3] != 0.f || prof[oe[ax] + 4 * i + 3] != 0.f;
+        int i = 0;  // damped run at the start, undamped middle, damped run at the end
+        while (i < n[ax] && damp[ax][i]) ++i;
+        while (i < n[ax] && !damp[ax][i]) ++i;
+        while (i < n[ax] && damp[ax][i]) ++i;
+        if (i != n[ax]) ends_only = false;
+    }
+    std::vector<PmlPart> cls[PML_NCLASS];
+    bool fits = ends_only;
+    if (ends_only) {
+        for (int b = 0; b < p.nbox; ++b) {
+            const PmlBox& B = p.box[b];
+            const int o[3] = {B.x0, B.y0, B.z0}, m[3] = {B.nx, B.ny, B.nz};
+            std::vector<int> cut[3];  // run boundaries of damped-ness along each axis of the box
+            for (int ax = 0; ax < 3; ++ax) {
+                cut[ax].push_back(0);
+                for (int i = 1; i < m[ax]; ++i)
+                    if (damp[ax][o[ax] + i] != damp[ax][o[ax] + i - 1]) cut[ax].push_back(i);
+                cut[ax].push_back(m[ax]);
+            }
+            for (size_t kz = 0; kz + 1 < cut[2].size(); ++kz)
+                for (size_t jy = 0; jy + 1 < cut[1].size(); ++jy)
+                    for (size_t ix = 0; ix + 1 < cut[0].size(); ++ix) {
+                        PmlPart P{};
+                        P.b = b;
+                        P.x0 = cut[0][ix]; P.nx = cut[0][ix + 1] - P.x0;
+                        P.y0 = cut[1][jy]; P.ny = cut[1][jy + 1] - P.y0;
+                        P.z0 = cut[2][kz]; P.nz = cut[2][kz + 1] - P.z0;
+                        const int mask = (damp[0][o[0] + P.x0] ? 1 : 0) | (damp[1][o[1] + P.y0] ? 2 : 0) |
+                                         (damp[2][o[2] + P.z0] ? 4 : 0);
+                        int c = PML_NCLASS - 1;
+                        for (int q = 0; q < PML_NCLASS - 1; ++q)
+                            if (PML_CLASS_MASK[q] == mask) c = q;
+                        cls[c].push_back(P);
+                    }
+        }
+        for (int q = 0; q < PML_NCLASS; ++q)
+            if ((int)cls[q].size() > PML_MAXPART) fits = false;
+    }
+    if (!fits) {
+        for (auto& v : cls) v.clear();
+        for (int b = 0; b < p.nbox; ++b) {
+            const PmlBox& B = p.box[b];
+            cls[PML_NCLASS - 1].push_back(PmlPart{b, 0, 0, 0, B.nx, B.ny, B.nz, 0});
+        }
+    }
+    // a single simulation's step launches the classes separately only when
+    // its shell is large enough for each launch to fill the GPU; a small
+    // shell takes one launch of the general kernel over the whole boxes
+    // (the batched form always splits: its launches span every member)
+    pml_all = pml_args;
+    pml_all.npart = p.nbox;
+    pml_all.nblocks = 0;
+    for (int b = 0; b < p.nbox; ++b) {
+        const PmlBox& B = p.box[b];
+        pml_all.part[b] = PmlPart{b, 0, 0, 0, B.nx, B.ny, B.nz, pml_all.nblocks};
+        pml_all.nblocks += (int)(((long long)B.nx * B.ny * B.nz + PTPB - 1) / PTPB);
+    }
+    pml_split = p.npml >= 4000000LL;
+    for (int q = 0; q < PML_NCLASS; ++q) {
+        PArgs& c = pml_cls[q];
+        c = pml_args;
+        c.npart = (int)cls[q].size();
+        c.nblocks = 0;
+        for (int t = 0; t < c.npart; ++t) {
+            c.part[t] = cls[q][t];
+            c.part[t].first_block = c.nblocks;
+            const long long np = (long long)c.part[t].nx * c.part[t].ny * c.part[t].nz;
+            c.nblocks += (int)((np + PTPB - 1) / PTPB);
+        }
+    }
+}
+
 int Sim::upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
                        const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
                        const int* kob_bot, const double* ts, bool column) {
@@ -1002,8 +1114,10 @@ int Sim::upload_medium(const float* rho, const float* lam, const float* mu, cons
         a.g = g; a.V = V; a.S = S; a.M = M; a.adeV = adeV; a.adeS = adeS; a.prof = dp;
         a.nbox = p.nbox;
         for (int b = 0; b < p.nbox; ++b) a.box[b] = p.box[b];
-        a.npts = p.npml;
+        a.npart = 0;
+        a.nblocks = 0;
         a.r20x = (float)(1.0 / dx); a.r20y = (float)(1.0 / dy); a.r20z = (float)(1.0 / dz); a.dt = (float)dt;
+        plan_pml_parts(prof);
     } else {
         std::vector<float> c, b, all;
         int n[3] = {g.nx, g.ny, g.nz};
@@ -1222,7 +1336,7 @@ struct Batch {
     int rbytes = 4, store = 0;
     std::vector<void*> allocs;
     TArgs* d_targs = nullptr;
-    PArgs* d_pargs = nullptr;
+    PArgs* d_pargs[PML_NCLASS] = {};  // per launch class: every member's PML arguments
     SrcArgs* d_src = nullptr;
     TapArgs* d_tap = nullptr;
     SnapArgs* d_snap = nullptr;
@@ -1233,8 +1347,9 @@ struct Batch {
     int** d_its = nullptr;
     int4* d_tblocks = nullptr;   // stress tiles
     int4* d_tblocks_v = nullptr; // velocity tiles
-    int2* d_pblocks = nullptr;
-    int n_tblocks = 0, n_tblocks_v = 0, n_pblocks = 0, max_nst = 0, max_src = 0, max_pix = 0, max_planes = 0;
+    int2* d_pblocks[PML_NCLASS] = {}; // per launch class: (member, block of its launch)
+    int n_pblocks[PML_NCLASS] = {};
+    int n_tblocks = 0, n_tblocks_v = 0, max_nst = 0, max_src = 0, max_pix = 0, max_planes = 0;
     bool any_vmax = false, any_snap = false, any_bf = false, any_mt = false;
     size_t smem_stress = 0, smem_vel = 0;
     long long launches = 0, launches_per_graph = 0;
@@ -1256,6 +1371,26 @@ struct Batch {
         *dst = (T*)q;
         return 0;
     }
+    bool any_pml() const {
+        for (int q = 0; q < PML_NCLASS; ++q)
+            if (n_pblocks[q]) return true;
+        return false;
+    }
+    void launch_pml(bool stress) {
+        for (int q = 0; q < PML_NCLASS; ++q) {
+            if (!n_pblocks[q]) continue;
+            const unsigned nb = (unsigned)n_pblocks[q];
+            const PArgs* a = d_pargs[q];
+            const int2* t = d_pblocks[q];
+            switch (PML_CLASS_MASK[q]) {
+            case 1: stress ? k_stress_pml_batch<1><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<1><<<nb, PTPB, 0, stream2>>>(a, t); break;
+            case 2: stress ? k_stress_pml_batch<2><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<2><<<nb, PTPB, 0, stream2>>>(a, t); break;
+            case 4: stress ? k_stress_pml_batch<4><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<4><<<nb, PTPB, 0, stream2>>>(a, t); break;
+            default: stress ? k_stress_pml_batch<7><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<7><<<nb, PTPB, 0, stream2>>>(a, t); break;
+            }
+            ++launches;
+        }
+    }
     int launch_step() {
         const int n = (int)sims.size();
         if (any_vmax) { k_vmax_batch<<<dim3(64, n), 256, 0, stream>>>(d_vmax); ++launches; }
@@ -1264,27 +1399,28 @@ struct Batch {
         if (any_snap) { k_snap_batch<<<dim3((max_pix + 127) / 128, max_planes, n), 128, 0, stream>>>(d_snap); ++launches; }
         const dim3 tblk(32, TTY);
         for (Sim* m : pw_members) { k_pw_ghost<<<256, 256, 0, stream>>>(m->V, m->p.g, 3); ++launches; }
-        if (n_pblocks) {
+        const bool pml = any_pml();
+        if (pml) {
             cudaEventRecord(ev[0], stream);
             cudaStreamWaitEvent(stream2, ev[0], 0);
-            k_stress_pml_batch<<<n_pblocks, PTPB, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
+            launch_pml(true);
             cudaEventRecord(ev[1], stream2);
         }
         if (rbytes == 4) k_stress_tma_batch<float><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
         else if (store == SWPC_STORE_FP16) k_stress_tma_batch<__half><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
         else k_stress_tma_batch<__nv_bfloat16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
         ++launches;
-        if (n_pblocks) cudaStreamWaitEvent(stream, ev[1], 0);
+        if (pml) cudaStreamWaitEvent(stream, ev[1], 0);
         if (any_mt) { k_stressglut_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
         for (Sim* m : pw_members) { k_pw_ghost<<<256, 256, 0, stream>>>(m->S, m->p.g, 6); ++launches; }
-        if (n_pblocks) {
+        if (pml) {
             cudaEventRecord(ev[2], stream);
             cudaStreamWaitEvent(stream2, ev[2], 0);
-            k_vel_pml_batch<<<n_pblocks, PTPB, 0, stream2>>>(d_pargs, d_pblocks); ++launches;
+            launch_pml(false);
             cudaEventRecord(ev[3], stream2);
         }
         k_vel_tma_batch<<<n_tblocks_v, tblk, smem_vel, stream>>>(d_targs, d_tblocks_v); ++launches;
-        if (n_pblocks) cudaStreamWaitEvent(stream, ev[3], 0);
+        if (pml) cudaStreamWaitEvent(stream, ev[3], 0);
         if (any_bf) { k_bodyforce_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
         k_advance_batch<<<(n + 127) / 128, 128, 0, stream>>>(d_its, n); ++launches;
         cudaError_t e = cudaGetLastError();
@@ -1343,7 +1479,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     for (auto& e : b->ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(set_err(SWPC_E_CUDA, "event creation failed"));
     std::vector<TArgs> ta(n);
-    std::vector<PArgs> pa(n);
+    std::vector<PArgs> pa[PML_NCLASS];
     std::vector<SrcArgs> sa(n);
     std::vector<TapArgs> tp(n);
     std::vector<SnapArgs> sn(n);
@@ -1351,7 +1487,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     std::vector<VmaxArgs> vm(n);
     std::vector<int*> its(n);
     std::vector<int4> tb, tbv;
-    std::vector<int2> pb;
+    std::vector<int2> pb[PML_NCLASS];
     for (int q = 0; q < n; ++q) {
         Sim* s = b->sims[q];
         CK(cudaStreamSynchronize(s->stream));
@@ -1359,8 +1495,11 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         s->fill_zargs(z);
         ta[q] = s->targs;
         ta[q].z = z;
-        pa[q] = s->pml_args;
-        if (!s->p.pml) pa[q].npts = 0;
+        for (int c = 0; c < PML_NCLASS; ++c) {
+            pa[c].push_back(s->pml_cls[c]);
+            if (!s->p.pml) pa[c].back().nblocks = 0;
+            for (int bk = 0; bk < pa[c].back().nblocks; ++bk) pb[c].push_back(make_int2(q, bk));
+        }
         sa[q] = s->src_args;
         tp[q] = s->tap_args;
         sn[q] = s->snap_args;
@@ -1377,8 +1516,6 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         for (int bz = 0; bz < gzv; ++bz)
             for (int by = 0; by < gy; ++by)
                 for (int bx = 0; bx < gx; ++bx) tbv.push_back(make_int4(q, bx, by, bz));
-        if (s->p.pml)
-            for (long long bk = 0; bk < (s->p.npml + PTPB - 1) / PTPB; ++bk) pb.push_back(make_int2(q, (int)bk));
         b->max_nst = std::max(b->max_nst, s->tap_args.n);
         b->max_src = std::max(b->max_src, s->src_args.n);
         if (s->src_args.n > 0) { if (s->bf_mode) b->any_bf = true; else b->any_mt = true; }
@@ -1390,14 +1527,16 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         }
     }
     int rc;
-    if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_pargs, pa)) || (rc = b->upload(&b->d_src, sa)) ||
+    for (int c = 0; c < PML_NCLASS; ++c)
+        if ((rc = b->upload(&b->d_pargs[c], pa[c])) || (rc = b->upload(&b->d_pblocks[c], pb[c]))) return fail(rc);
+    if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_src, sa)) ||
         (rc = b->upload(&b->d_tap, tp)) || (rc = b->upload(&b->d_snap, sn)) || (rc = b->upload(&b->d_green, gr)) || (rc = b->upload(&b->d_vmax, vm)) ||
-        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_tblocks_v, tbv)) || (rc = b->upload(&b->d_pblocks, pb)))
+        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_tblocks_v, tbv)))
         return fail(rc);
     if (((uintptr_t)b->d_targs & 127) != 0) return fail(set_err(SWPC_E_CUDA, "tensor-map table is not 128-byte aligned"));
     b->n_tblocks = (int)tb.size();
     b->n_tblocks_v = (int)tbv.size();
-    b->n_pblocks = (int)pb.size();
+    for (int c = 0; c < PML_NCLASS; ++c) b->n_pblocks[c] = (int)pb[c].size();
     b->smem_stress = b->sims[0]->smem_stress;
     b->smem_vel = b->sims[0]->smem_vel;
     *out = reinterpret_cast<swpc_batch*>(b);
