@@ -214,9 +214,10 @@ int Sim::launch_step(bool timed) {
     }
     ev0(0, stream);
     if (variant == 0) {
-        if (p.rbytes == 4) k_stress_tma<float><<<tgrd, tblk, smem_stress, stream>>>(targs);
-        else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half><<<tgrd, tblk, smem_stress, stream>>>(targs);
-        else k_stress_tma<__nv_bfloat16><<<tgrd, tblk, smem_stress, stream>>>(targs);
+        const unsigned nlin = tgrd.x * tgrd.y * tgrd.z;  // 1-D grid, grouped block order
+        if (p.rbytes == 4) k_stress_tma<float><<<nlin, tblk, smem_stress, stream>>>(targs);
+        else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half><<<nlin, tblk, smem_stress, stream>>>(targs);
+        else k_stress_tma<__nv_bfloat16><<<nlin, tblk, smem_stress, stream>>>(targs);
     } else {
         if (p.rbytes == 4) k_stress_interior<float><<<grd, blk, 0, stream>>>(z);
         else if (dims.store == SWPC_STORE_FP16) k_stress_interior<__half><<<grd, blk, 0, stream>>>(z);
@@ -1510,9 +1511,11 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         its[q] = s->d_it;
         const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + TTY - 1) / TTY, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
         const int gzv = (s->p.nzi + s->kchunk_v - 1) / s->kchunk_v;
-        for (int bz = 0; bz < gz; ++bz)
-            for (int by = 0; by < gy; ++by)
-                for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
+        // stress tiles in the grouped order of the single-simulation launch
+        for (int y0 = 0; y0 < gy; y0 += STRESS_YGROUP)
+            for (int bz = 0; bz < gz; ++bz)
+                for (int by = y0; by < std::min(gy, y0 + STRESS_YGROUP); ++by)
+                    for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
         for (int bz = 0; bz < gzv; ++bz)
             for (int by = 0; by < gy; ++by)
                 for (int bx = 0; bx < gx; ++bx) tbv.push_back(make_int4(q, bx, by, bz));
