@@ -85,3 +85,35 @@ def test_drop_in_path_matches_golden_traces(tmp_path):
     print("drop-in path: misfit vs fp32 oracle %.3e, vs fp64 oracle %.3e" % (m32, m64))
     assert m32 <= 1e-5
     assert m64 <= 1e-5
+
+
+@pytest.mark.gpu
+def test_simulations_driven_from_two_threads(tmp_path):
+    """One host thread per simulation (each with its own streams): two
+    simulations stepped concurrently from two threads give the same traces,
+    bit for bit, as the same simulations run one after the other."""
+    import threading
+    infs = [configs.write_plain_small(str(tmp_path / n), nt=120, nx=n2, ny=n2, nz=48, xbeg=-n2 / 4, ybeg=-n2 / 4)
+            for n, n2 in (("a", 96), ("b", 112))]
+
+    def run(inf):
+        s = gpu.Simulation.from_inf(inf)
+        s.run(1, 120)
+        s.sync()
+        w = s.waveforms()
+        s.close()
+        return w
+
+    alone = [run(f) for f in infs]
+    out = [None, None]
+
+    def worker(q):
+        out[q] = run(infs[q])
+
+    th = [threading.Thread(target=worker, args=(q,)) for q in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for q in range(2):
+        assert out[q] is not None and np.array_equal(out[q], alone[q])
