@@ -49,3 +49,29 @@ def test_bf16_memory_variables(runs):
     print("bf16 storage: misfit vs fp32 %.3e, vs fp64 %.3e (fp32 vs fp64 %.3e)" % (m32, m64, base))
     assert m32 < 1e-2
     assert m64 < 1e-2 + base
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("store", ["fp16", "bf16"])
+def test_16bit_batch_equals_alone(tmp_path, store):
+    """The batched kernels with 16-bit memory variables give each member
+    exactly (bit for bit) the traces of the same simulation run alone."""
+    from openswpc_gb300 import gpu
+    infs = [configs.write_plain_small(str(tmp_path / n), nt=120, nx=n2, ny=n2, nz=48, xbeg=-n2 / 4, ybeg=-n2 / 4)
+            for n, n2 in (("a", 96), ("b", 128))]
+    orc = [pyoracle.Oracle(f, "fp32") for f in infs]
+    alone = []
+    for o in orc:
+        s = sim_from_oracle(o, store=store)
+        s.run(1, 120)
+        alone.append(s.waveforms())
+        s.close()
+    sims = [sim_from_oracle(o, store=store) for o in orc]
+    b = gpu.Batch(sims)
+    b.run(120)
+    b.sync()
+    for s, w in zip(sims, alone):
+        assert np.array_equal(s.waveforms(), w)
+    b.close()
+    for s in sims:
+        s.close()
