@@ -862,15 +862,30 @@ int Sim::allocate() {
     CK(cudaEventCreateWithFlags(&ev_fork2, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_join2, cudaEventDisableTiming));
     int rc;
-    if ((rc = dalloc((void**)&V, p.nV * 4))) return rc;
-    if ((rc = dalloc((void**)&S, p.nS * 4))) return rc;
-    if ((rc = dalloc((void**)&M, p.nM * 4))) return rc;
-    if ((rc = dalloc(&R, p.nR * p.rbytes))) return rc;
-    if ((rc = dalloc((void**)&band, 16 * (size_t)p.nxi * p.nyi))) return rc;
-    if (p.pml) {
-        if ((rc = dalloc((void**)&adeV, p.nade * 4))) return rc;
-        if ((rc = dalloc((void**)&adeS, p.nade * 4))) return rc;
+    // the large arrays are carved out of one allocation: freeing one 72 GB
+    // block took 26 ms on a GB300, freeing the same bytes in 4 to 16 blocks
+    // 45 to 53 ms (and one allocation maps faster too)
+    {
+        size_t off = 0;
+        auto carve = [&](size_t bytes) {
+            const size_t o = off;
+            off += (bytes + 4095) / 4096 * 4096;  // 4 KB aligned bases (tensor maps want 16 B)
+            return o;
+        };
+        const size_t oV = carve(p.nV * 4), oS = carve(p.nS * 4), oM = carve(p.nM * 4), oR = carve(p.nR * p.rbytes);
+        const size_t oAV = p.pml ? carve(p.nade * 4) : 0, oAS = p.pml ? carve(p.nade * 4) : 0;
+        char* arena = nullptr;
+        if ((rc = dalloc((void**)&arena, off))) return rc;
+        V = reinterpret_cast<float*>(arena + oV);
+        S = reinterpret_cast<float*>(arena + oS);
+        M = reinterpret_cast<float*>(arena + oM);
+        R = arena + oR;
+        if (p.pml) {
+            adeV = reinterpret_cast<float*>(arena + oAV);
+            adeS = reinterpret_cast<float*>(arena + oAS);
+        }
     }
+    if ((rc = dalloc((void**)&band, 16 * (size_t)p.nxi * p.nyi))) return rc;
     if ((rc = dalloc((void**)&d_it, 16))) return rc;
     if ((rc = dalloc((void**)&d_kob, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     if ((rc = dalloc((void**)&d_kfs, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
