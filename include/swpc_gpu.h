@@ -93,7 +93,10 @@ long long swpc_gpu_required_bytes(const swpc_dims* dims);
  * maps of surface_detection (m_medium.f90:339-394), and the nm relaxation
  * times ts (m_fdtool.f90:691-727).  The library derives the Zener
  * coefficients (m_kernel.f90:58-67) and the PML or Cerjan profiles
- * (m_absorb_p.f90:74-93, m_absorb_c.f90:27-111) in FP64 here. */
+ * (m_absorb_p.f90:74-93, m_absorb_c.f90:27-111) in FP64 here.  Arrays in
+ * pinned (page-locked) host memory are read by the device directly over the
+ * CPU-GPU link; other memory is staged through a device copy.  Either way
+ * the call returns after the arrays have been read. */
 int swpc_gpu_upload_medium(swpc_sim* sim, const float* rho, const float* lam, const float* mu,
                            const float* taup, const float* taus,
                            const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot,
