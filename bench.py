@@ -301,6 +301,44 @@ def run_reference(args, w):
     return 0
 
 
+def timed_window(w, steps, warmup):
+    """First step of the timed window: the window of `steps` steps holds a
+    snapshot frame (it = 1 + m * ntdec_s, m >= 1) near its middle and at
+    least `warmup` untimed steps come before it."""
+    nts = w["ntdec_s"]
+    m = 1
+    while 1 + m * nts - steps // 2 - 1 < warmup:
+        m += 1
+    return 1 + m * nts - steps // 2
+
+
+def pml_class_report(sim, peak):
+    """Per launch class of the PML kernels: time per launch and the
+    algorithmic bytes of its points.  Per shell point the stress update
+    reads V (12 B) and lam, mu (8 B) and rewrites S (48 B), the velocity
+    update reads S (24 B) and rho (4 B) and rewrites V (24 B); every damped
+    axis adds three auxiliaries read and written (24 B)."""
+    ms, n, pts, ax = sim.profile_read_pml()
+    names = ["x", "y", "z", "general"]
+    out = {}
+    for u, (kname, base) in enumerate((("stress_pml", 68), ("vel_pml", 52))):
+        tot_b, tot_ms = 0.0, 0.0
+        cls = {}
+        for q in range(4):
+            if n[u, q] == 0:
+                continue
+            b = base * float(pts[q]) + 24.0 * float(ax[q])
+            t = ms[u, q] / n[u, q]
+            cls[names[q]] = {"points": int(pts[q]), "bytes_per_point": b / max(pts[q], 1), "ms": t,
+                             "GBps": b / (t / 1e3) / 1e9, "frac": b / (t / 1e3) / 1e9 / peak}
+            tot_b += b
+            tot_ms += t
+        out[kname] = {"classes": cls, "bytes": tot_b, "ms": tot_ms,
+                      "GBps": tot_b / (tot_ms / 1e3) / 1e9 if tot_ms > 0 else None,
+                      "frac": tot_b / (tot_ms / 1e3) / 1e9 / peak if tot_ms > 0 else None}
+    return out
+
+
 def run_gpu(args, w):
     world, rank, local = dist_init()
     from openswpc_gb300 import gpu
@@ -316,12 +354,12 @@ def run_gpu(args, w):
     stream = torch.cuda.ExternalStream(sim.stream())
     t_setup = time.time() - t_setup
 
-    it = 1
-    sim.run(it, it + args.warmup - 1)
-    it += args.warmup
+    # untimed warm-up up to the timed window, which holds a snapshot frame
+    it = timed_window(w, args.steps, args.warmup)
+    sim.run(1, it - 1)
     sim.sync()
-    # timed region: per-kernel CUDA events on the simulation's stream
-    sim.profile(True)
+    # timed region: the production path (graph replay), CUDA events on the
+    # simulation's stream
     n0 = sim.launch_count()
     clk = Clocks(local)
     barrier(world)
@@ -333,13 +371,20 @@ def run_gpu(args, w):
     e0.record(stream)
     sim.run(it, it + args.steps - 1)
     e1.record(stream)
-    it += args.steps
     torch.cuda.synchronize()
     clocks = clk.stop()
     barrier(world)
     ms = e0.elapsed_time(e1)
     launches = sim.launch_count() - n0
+    frames = [f for f in range(it, it + args.steps) if (f - 1) % w["ntdec_s"] == 0]
+    it += args.steps
+    # per-kernel pass: the next K steps launched one by one with an event
+    # pair around every kernel (outside the headline region)
+    sim.profile(True)
+    sim.run(it, it + args.steps - 1)
+    it += args.steps
     kms, kn = sim.profile_read()
+    pml = pml_class_report(sim, peak)
     sim.profile(False)
     sim.sync()
     ms_max = reduce_max(ms, world)
@@ -348,11 +393,15 @@ def run_gpu(args, w):
     n_int, n_pml = counts(w)
     b_int, b_pml, kbytes = byte_model(args.store)
     step_bytes = b_int * n_int + b_pml * n_pml
-    names = ["stress_interior", "vel_interior", "stress_pml", "vel_pml"]
-    kavg = {nm: float(kms[q] / max(kn[q], 1)) for q, nm in enumerate(names)}
-    units = {"stress_interior": n_int, "vel_interior": n_int, "stress_pml": n_pml, "vel_pml": n_pml}
-    kern = {nm: {"ms": kavg[nm], "GBps": kbytes[nm] * units[nm] / (kavg[nm] / 1e3) / 1e9 if kavg[nm] > 0 else None,
-                 "share": float(kms[q] / max(kms[:4].sum(), 1e-12))} for q, nm in enumerate(names)}
+    kern = {}
+    for q, nm in enumerate(["stress_interior", "vel_interior"]):
+        t = float(kms[q] / max(kn[q], 1))
+        kern[nm] = {"ms": t, "bytes": kbytes[nm] * n_int, "GBps": kbytes[nm] * n_int / (t / 1e3) / 1e9 if t > 0 else None}
+        kern[nm]["frac"] = kern[nm]["GBps"] / peak if kern[nm]["GBps"] else None
+    kern.update(pml)
+    tot = sum(kern[k]["ms"] for k in kern)
+    for k in kern:
+        kern[k]["share"] = kern[k]["ms"] / tot if tot > 0 else None
     top = "stress_interior"
     achieved = kern[top]["GBps"]
     traffic = None
@@ -399,12 +448,18 @@ def run_gpu(args, w):
         cb = cpu_sample()
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
+    batch = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        batch = batch_block(args)
+
     if rank == 0:
         line = {
             "metric": "grid-pt updates/s", "value": value, "unit": "pt/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": arm_config(w, args, world),
+            "config": dict(arm_config(w, args, world),
+                           timed_steps="it=%d..%d (graph replay; snapshot frame at it=%s)"
+                                       % (it - 2 * args.steps, it - args.steps - 1, ",".join(map(str, frames)))),
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
                                   "peak": peak, "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak,
                                   "model": "%d B/interior pt + %d B/PML pt per step" % (b_int, b_pml)},
@@ -412,11 +467,14 @@ def run_gpu(args, w):
                          "frac": achieved / peak if achieved else None, "traffic": traffic,
                          "bytes_per_point": kbytes[top], "peak_source": peak_kind},
             "kernels": kern,
+            "kernel_timing": "per-launch CUDA events on the simulation's stream over the %d steps after the "
+                             "timed region (launched one by one)" % args.steps,
             "clocks": clocks,
             "gpu_launches": launches,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "parity": parity_statement(),
+            "batched": batch,
             "setup_s": t_setup,
         }
         print(json.dumps(line), flush=True)
@@ -440,33 +498,44 @@ def batch_inputs(n, seed, nt, root):
     return infs, sizes
 
 
-def run_batch(args):
-    """Batched form: solves/s of n simulations advanced together versus the
-    same simulations run one after another on the plain path.  Both are
-    timed over K steps (CUDA events) and scaled to the full nt = 1500
-    (steps cost the same throughout a run)."""
+def member_bytes(nx, ny, nz, na=20):
+    """Model bytes of one time step of a member (236 B per interior point,
+    228 B per PML point)."""
+    n_int = (nx - 2 * na) * (ny - 2 * na) * (nz - na)
+    return B_INT * n_int + B_PML * (nx * ny * nz - n_int)
+
+
+def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500):
+    """n simulations of the batched workload advanced together (swpc_batch)
+    versus the same simulations one after another on the plain path; both
+    timed with CUDA events over `steps` steps and scaled to nt_full steps
+    (every step of a run costs the same).  Returns ms per step of each arm,
+    solves/s, grid-point updates/s and the HBM fraction of the model bytes."""
     from openswpc_gb300 import autotune, gpu
     import torch
     gpu.lib()
-    n, nt_full = args.nsim, 1500
+    peak, _ = peaks()
     with tempfile.TemporaryDirectory() as root:
-        infs, sizes = batch_inputs(n, 20261203, nt_full, root)
+        infs, sizes = batch_inputs(nsim, seed, nt_full, root)
         sims = [gpu.Simulation.from_inf(f) for f in infs]
         pts = [int(np.prod(s)) for s in sizes]
-        t0 = time.time()
-        rec = autotune.tune(sims)
-        t_tune = time.time() - t0
+        step_bytes = float(sum(member_bytes(*map(int, s)) for s in sizes))
+        rec, t_tune = None, 0.0
+        if tune:
+            t0 = time.time()
+            rec = autotune.tune(sims)
+            t_tune = time.time() - t0
         b = gpu.Batch(sims)
         st = torch.cuda.ExternalStream(b.stream())
-        b.run(args.warmup)
+        b.run(warmup)
         b.sync()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         n0 = b.launch_count()
         e0.record(st)
-        b.run(args.steps)
+        b.run(steps)
         e1.record(st)
         e1.synchronize()
-        ms_batch = e0.elapsed_time(e1) / args.steps
+        ms_batch = e0.elapsed_time(e1) / steps
         launches = b.launch_count() - n0
         b.close()
         # the same members one after another, each on its own plain path
@@ -474,27 +543,54 @@ def run_batch(args):
         for s in sims:
             s.reset()
             s.set_zchunk(0)
-            s.run(1, args.warmup)
+            s.run(1, warmup)
             s.sync()
             stq = torch.cuda.ExternalStream(s.stream())
             a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a0.record(stq)
-            s.run(args.warmup + 1, args.warmup + args.steps)
+            s.run(warmup + 1, warmup + steps)
             a1.record(stq)
             a1.synchronize()
-            ms_seq += a0.elapsed_time(a1) / args.steps
+            ms_seq += a0.elapsed_time(a1) / steps
         for s in sims:
             s.close()
-    solves_batch = n / (nt_full * ms_batch / 1e3)
-    solves_seq = n / (nt_full * ms_seq / 1e3)
-    line = {"metric": "batched solves/s", "value": solves_batch, "unit": "solves/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True,
+    gbps_b = step_bytes / (ms_batch / 1e3) / 1e9
+    gbps_s = step_bytes / (ms_seq / 1e3) / 1e9
+    return {"members": nsim, "points_total": int(sum(pts)), "steps": steps, "warmup": warmup,
+            "ms_per_step": ms_batch, "sequential_ms_per_step": ms_seq,
+            "solves_per_s": nsim / (nt_full * ms_batch / 1e3), "sequential_solves_per_s": nsim / (nt_full * ms_seq / 1e3),
+            "speedup_vs_sequential": ms_seq / ms_batch,
+            "grid_pt_updates_per_s": sum(pts) / (ms_batch / 1e3),
+            "sequential_grid_pt_updates_per_s": sum(pts) / (ms_seq / 1e3),
+            "model_bytes_per_step": step_bytes,
+            "hbm_frac": gbps_b / peak, "sequential_hbm_frac": gbps_s / peak,
+            "gpu_launches": launches, "autotune": rec, "autotune_s": t_tune,
+            "nt_full": nt_full}
+
+
+def batch_block(args):
+    """Short batched block of the default run: 16 members of the batched
+    workload, 20 steps each arm."""
+    try:
+        r = batch_measure(16, 20, 3, tune=False)
+        r["workload"] = "batched many-instance: 16 simulations, axes in {96..256}, timed 20 steps, solves/s at nt=1500"
+        return r
+    except Exception as e:  # the headline line is still printed
+        return {"error": str(e)}
+
+
+def run_batch(args):
+    """Batched form: solves/s of n simulations advanced together versus the
+    same simulations run one after another on the plain path."""
+    r = batch_measure(args.nsim, args.steps, args.warmup)
+    line = {"metric": "batched solves/s", "value": r["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched many-instance: %d simulations, axes in {96..256}, nt=%d" % (n, nt_full),
-                       "points_total": int(sum(pts)), "zchunk": [rec["zchunk"], rec["zchunk_vel"]]},
-            "sequential_solves_per_s": solves_seq, "speedup_vs_sequential": solves_batch / solves_seq,
-            "grid_pt_updates_per_s": sum(pts) / (ms_batch / 1e3), "autotune": rec, "autotune_s": t_tune,
-            "gpu_launches": launches}
+            "config": {"workload": "batched many-instance: %d simulations, axes in {96..256}, nt=%d"
+                                   % (args.nsim, r["nt_full"]), "points_total": r["points_total"],
+                       "zchunk": [r["autotune"]["zchunk"], r["autotune"]["zchunk_vel"]] if r["autotune"] else None},
+            "gpu_launches": r["gpu_launches"]}
+    line.update({k: v for k, v in r.items() if k not in ("gpu_launches",)})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -647,6 +743,7 @@ def main():
     ap.add_argument("--quantum", type=int, default=50, help="serving: steps between scheduling points")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the short batched block of the default run")
     ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])
     ap.add_argument("--variant", type=int, default=0, help="0: TMA-fed interior kernels, 1: plain smem sweep")
     ap.add_argument("--pml-overlap", type=lambda v: {"auto": None, "on": True, "off": False}[v], default=None,

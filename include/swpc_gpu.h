@@ -190,15 +190,17 @@ int swpc_gpu_vmax(swpc_sim* sim, float out[3]);
  * uploaded medium rho lam mu taup taus. */
 int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out);
 
-/* The same read-back for callers that cannot allocate device memory (a host
- * whose device is fully committed under an HBM budget, or whose allocator
- * forbids side allocations).  No counterpart in the reference.  It calls no
+/* The read-back of swpc_gpu_fetch_field for the nine wavefields only
+ * (which = 0..8, Vx .. Sxy; the medium fields 9..13 are refused with
+ * SWPC_E_ARG), for callers that cannot allocate device memory (a host whose
+ * device is fully committed under an HBM budget, or whose allocator forbids
+ * side allocations).  No counterpart in the reference.  It calls no
  * cudaMalloc/cudaFree: the gather goes through a fixed 32 MiB scratch array
  * in the library image that every GPU loading the library holds until exit.
  * Grids above SWPC_STATIC_FIELD_MAX points are rejected with SWPC_E_ARG.  The
- * first call on a device looks the array up for that device; make it before
- * any stream capture.  All calls share the one array: calls that overlap on
- * the GPU (from different threads or streams) race. */
+ * first call for a device looks the array up on the simulation's device;
+ * make it before any stream capture.  All calls share the one array: calls
+ * that overlap on the GPU (from different threads or streams) race. */
 #define SWPC_STATIC_FIELD_MAX (4 * 1024 * 1024)
 int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out);
 
@@ -209,6 +211,16 @@ int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out);
  * sources; launches[0..5] the matching counts. */
 int swpc_gpu_profile(swpc_sim* sim, int enable);
 int swpc_gpu_profile_read(swpc_sim* sim, double* ms, long long* launches);
+/* The PML time of swpc_gpu_profile_read split by launch class (the shell
+ * parts damped along x only, y only, z only, and the rest): ms[0..3] and
+ * launches[0..3] for the stress update, ms[4..7] and launches[4..7] for the
+ * velocity update; points[0..3] the shell points of each class and
+ * axis_points[0..3] the sum over those points of the number of damped axes
+ * (each damped axis keeps three stress and three velocity auxiliaries per
+ * point, m_absorb_p.f90:99-116).  A small shell runs as one launch of the
+ * last class.  No counterpart in the reference. */
+int swpc_gpu_profile_read_pml(swpc_sim* sim, double* ms, long long* launches, long long* points,
+                              long long* axis_points);
 
 /* The cudaStream_t the simulation launches on (as void*). */
 void* swpc_gpu_stream(swpc_sim* sim);
@@ -300,6 +312,20 @@ int swpc_host_check(const char* inf_path, char* summary, size_t n);
 /* Number of time steps nt read from input.inf by swpc_host_prepare (0 if the
  * simulation was not made by it). */
 int swpc_host_nt(swpc_sim* sim);
+
+/* Progress-report interval ntdec_r read from input.inf (report__setup,
+ * src/swpc_3d/m_report.f90:47, default 10); 0 if the simulation was not
+ * made by swpc_host_prepare. */
+int swpc_host_ntdec_r(swpc_sim* sim);
+
+/* The run banner of report__setup (src/swpc_3d/m_report.f90:64-88): grid,
+ * MPI partitioning of input.inf, memory estimate (memory_size_3d,
+ * src/shared/m_fdtool.f90:137-187), stability number c and wavelength
+ * number r (m_fdtool.f90:81-134) from the velocity range of the processed
+ * medium (velocity_minmax, m_medium.f90:396-427) and the maximum
+ * frequency, formatted as the reference prints it.  Copies the text into
+ * buf and returns its length. */
+int swpc_host_banner(swpc_sim* sim, char* buf, size_t n);
 
 /* Medium post-processing of medium__setup (m_medium.f90:124-394) in FP64 for
  * hosts that bring their own velocity model.  On entry rho, lam, mu, qp_taup

@@ -259,3 +259,32 @@ def gradient_random_medium(nx, ny, nz, dx, zbeg, seed=DEFAULT_SEED, a=5.0, eps=0
     qpv = np.broadcast_to(qpa[None, None, :], shape)
     qsv = np.broadcast_to(qsa[None, None, :], shape)
     return rho, lam, mu, qpv, qsv
+
+
+def write_random_medium_case(d, nx=192, ny=192, nz=128, dx=0.25, dt=0.01, nt=600, seed=DEFAULT_SEED,
+                             src_depth=3.75, n_side=8):
+    """The large single-source workload's medium at a size the CPU oracle runs
+    in seconds: the gradient + von Karman medium of gradient_random_medium at
+    the workload's spacing (dx = 0.25 km, dt = 0.01 s), one double couple
+    (mechanism from the seed, Kupper 1 s) at src_depth km -- 15 km of a
+    128 km deep model scaled to 3.75 km of a 32 km deep one -- and
+    n_side x n_side receivers on the free surface.  Returns the input.inf
+    path and the raw medium (rho, lam, mu, qp, qs stacked over the halo
+    grid) that the oracle and the GPU path both take."""
+    zbeg = -3 * dx
+    inf = write_plain_small(d, seed=seed, nt=nt, nx=nx, ny=ny, nz=nz, dx=dx, dy=dx, dz=dx, dt=dt,
+                            xbeg=-nx * dx / 2, ybeg=-ny * dx / 2, zbeg=zbeg, ntdec_r=50)
+    rng = np.random.default_rng(seed + 1)
+    strike, dip, rake = double_couple(rng)
+    with open(os.path.join(d, "source.dat"), "w") as f:
+        f.write("# x y z tbeg trise mo strike dip rake\n")
+        f.write("  0.0 0.0 %.4f 0.0 1.0 1.0e16 %.4f %.4f %.4f\n" % (src_depth, strike, dip, rake))
+    half = 0.5 * min(nx, ny) * dx - (20 + 6) * dx
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        n = 0
+        for y in np.linspace(-half, half, n_side):
+            for x in np.linspace(-half, half, n_side):
+                n += 1
+                f.write("  %.3f %.3f 0.0 R%03d fsb\n" % (x, y, n))
+    med = np.stack(gradient_random_medium(nx, ny, nz, dx, zbeg, seed=seed))
+    return inf, med

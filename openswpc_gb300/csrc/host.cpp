@@ -253,6 +253,11 @@ struct Meta {  // what the SAC writer needs after set-up
     // Green's-function mode: the pseudo-source station and the output points
     struct GPoint { double x = 0, y = 0, z = 0, lon = 0, lat = 0; long long gid = 0; int i = 0, j = 0, k = 0; };
     struct Green { bool on = false; Station station; std::vector<GPoint> pts; } green;
+    // the numbers of report__setup's banner (src/swpc_3d/m_report.f90:71-85)
+    struct Banner {
+        int nproc_x = 1, nproc_y = 1;
+        float mem_all = 0, mem_node = 0, c = 0, r = 0, vmin = 0, vmax = 0, fmax = 0;
+    } banner;
 };
 std::mutex g_meta_mu;
 std::map<swpc_sim*, Meta> g_meta;
@@ -751,6 +756,74 @@ std::string tar_entry(const std::string& name, const std::string& data, long lon
 }
 
 
+// report__setup's banner numbers in the reference's single precision
+// (src/swpc_3d/m_report.f90:71-73): the memory estimate of memory_size_3d
+// (src/shared/m_fdtool.f90:137-187), the stability number c of
+// fdm_cond_stability (:81-113) and the wavelength number r of
+// fdm_cond_wavelength (:116-134), from the velocity range of the processed
+// medium below the free surface (velocity_minmax, m_medium.f90:396-427)
+// and fmax = 2 fcut (m_source.f90:184-188).  vel(f, k, i, j) reads the
+// processed rho (0), lam (1) or mu (2).
+template <class MedV>
+void banner_numbers(const Params& p, const Grid& G, const std::vector<int>& kfs, MedV vel, bool colmode, double fcut,
+                    int nproc_x, int nproc_y, Meta::Banner& b) {
+    b.nproc_x = nproc_x;
+    b.nproc_y = nproc_y;
+    float vmax = -1.f, vmin = 1e30f;
+    const float eps = 1.1920928955078125e-07f;
+    const int ie = colmode ? 1 : p.nx, je = colmode ? 1 : p.ny;  // one column stands for every column
+    for (int j = 1; j <= je; ++j)
+        for (int i = 1; i <= ie; ++i)
+            for (int k = kfs[G.idx2(i, j)] + 1; k <= p.nz; ++k) {
+                const float r = vel(0, k, i, j), l = vel(1, k, i, j), m = vel(2, k, i, j);
+                const float vp = std::sqrt((l + 2 * m) / r), vs = std::sqrt(m / r);
+                vmax = std::max(vmax, vp);
+                if (vs < eps) continue;
+                vmin = std::min(vmin, vs);
+            }
+    b.vmin = vmin;
+    b.vmax = vmax;
+    b.fmax = (float)(2 * fcut);
+    const float dx = (float)p.dx, dy = (float)p.dy, dz = (float)p.dz;
+    const float hh = 1.f / std::sqrt(1 / (dx * dx) + 1 / (dy * dy) + 1 / (dz * dz));
+    const float dt2 = 6.f / 7.f * hh / vmax;
+    b.c = (float)p.dt / dt2;
+    b.r = vmin / b.fmax / std::max(dx, std::max(dy, dz));
+    // memory_size_3d: 5 medium words (SP), 3 + 6 state words (DP) over the
+    // padded grid of every rank, 6 nm memory variables (SP) over the interior
+    // and 18 absorber words (SP) over the shell, as the reference counts them
+    const int nxp = (int)std::ceil(p.nx / (float)nproc_x), nyp = (int)std::ceil(p.ny / (float)nproc_y);
+    const float rn_com = (float)((nxp + 6) * nproc_x) * (float)((nyp + 6) * nproc_y) * (float)(p.nz + 6);
+    const float rn_int = (float)(p.nx - 2 * p.na) * (float)(p.ny - 2 * p.na) * (float)(p.nz - p.na);
+    const float rn_abc = (float)p.nx * (float)p.ny * (float)p.nz -
+                         (float)(p.nx - 2 * nxp) * (float)(p.ny - 2 * nyp) * (float)(p.nz - p.na);
+    const float ba = (5 * 4 + 3 * 8 + 6 * 8) * rn_com + (6 * 3 * 4) * rn_int + (18 * 4) * rn_abc;
+    b.mem_all = ba / (1024.f * 1024.f * 1024.f);
+    b.mem_node = b.mem_all / (float)(nproc_x * nproc_y);
+}
+
+// The banner as report__setup writes it (m_report.f90:64-88).
+std::string banner_text(const Meta& m) {
+    const Meta::Banner& b = m.banner;
+    const Params& p = m.p;
+    char buf[1600];
+    const char* rule = " ------------------------------------------------------------------------------";
+    std::snprintf(buf, sizeof buf,
+                  "\n%s\n  SWPC_3D GB300 (openswpc_gb300)\n%s\n\n"
+                  "  Grid Size               : %8d x %6d x %6d\n"
+                  "  MPI Partitioning        : %8d x %4d\n"
+                  "  Total Memory Size       : %15.3f  [GiB]\n"
+                  "  Node Memory Size        : %15.3f  [GiB]\n"
+                  "  Stability  Condition c  : %15.3f  (c<1)\n"
+                  "  Wavelength Condition r  : %15.3f  (r>5-10)\n"
+                  "  Minimum velocity        : %15.3f  [km/s]\n"
+                  "  Maximum velocity        : %15.3f  [km/s]\n"
+                  "  Maximum frequency       : %15.3f  [Hz]\n\n%s\n\n",
+                  rule, rule, p.nx, p.ny, p.nz, b.nproc_x, b.nproc_y, b.mem_all, b.mem_node, b.c, b.r, b.vmin, b.vmax,
+                  b.fmax, rule);
+    return buf;
+}
+
 // Everything the host set-up derives from one input.inf, held until the
 // simulation is put on a device: the medium, the source and receiver grid
 // indices and the device dimensions.
@@ -820,7 +893,7 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
     p.wav_format = inf.s("wav_format", "sac");
     p.sw_v = inf.b("sw_wav_v", false); p.sw_u = inf.b("sw_wav_u", false);
     p.sw_stress = inf.b("sw_wav_stress", false); p.sw_strain = inf.b("sw_wav_strain", false);
-    p.ntdec_r = inf.i("ntdec_r", 100);
+    p.ntdec_r = inf.i("ntdec_r", 10);  // m_report.f90:47
     // snapshot switches and planes (m_snap.f90:105-127)
     {
         const char* secs[5] = {"xy", "yz", "xz", "fs", "ob"};
@@ -1068,17 +1141,30 @@ int load(const char* inf_path, Prepared& P, std::string* dry = nullptr) {
         }
     }
 
+    banner_numbers(p, G, kfs, medv, colmode, fcut, std::max(1, inf.i("nproc_x", 1)), std::max(1, inf.i("nproc_y", 1)),
+                   meta.banner);
     if (dry) {  // set-up summary only, no device
-        char buf[512];
+        char buf[1024];
         std::string src_s, st_s;
         for (size_t q = 0; q < smo.size(); ++q)
             src_s += (q ? ";" : "") + std::to_string(sijk[3 * q]) + "," + std::to_string(sijk[3 * q + 1]) + "," + std::to_string(sijk[3 * q + 2]);
         for (size_t q = 0; q < meta.st.size(); ++q)
             st_s += (q ? ";" : "") + std::to_string(meta.st[q].i) + "," + std::to_string(meta.st[q].j) + "," + std::to_string(meta.st[q].k);
+        const Meta::Banner& bn = meta.banner;
+        auto jn = [](double v) {  // JSON number, null when not finite (e.g. r without a source frequency)
+            char t[40];
+            if (std::isfinite(v)) std::snprintf(t, sizeof t, "%.9g", v);
+            else std::snprintf(t, sizeof t, "null");
+            return std::string(t);
+        };
+        const std::string bj = "\"banner\": {\"mem_total_gib\": " + jn(bn.mem_all) + ", \"mem_node_gib\": " + jn(bn.mem_node) +
+                               ", \"c\": " + jn(bn.c) + ", \"r\": " + jn(bn.r) + ", \"vmin\": " + jn(bn.vmin) +
+                               ", \"vmax\": " + jn(bn.vmax) + ", \"fmax\": " + jn(bn.fmax) + ", \"nproc\": [" +
+                               std::to_string(bn.nproc_x) + ", " + std::to_string(bn.nproc_y) + "]}, ";
         std::snprintf(buf, sizeof buf, "{\"nx\": %d, \"ny\": %d, \"nz\": %d, \"nt\": %d, \"na\": %d, \"M0\": %.9g, \"UC\": %.9g, "
                       "\"fcut\": %.9g, \"nsrc\": %d, \"nst\": %d, \"ts\": [%.9g, %.9g, %.9g], ",
                       p.nx, p.ny, p.nz, p.nt, p.na, M0, UC, fcut, (int)smo.size(), (int)meta.st.size(), ts[0], ts[1], ts[2]);
-        *dry = std::string(buf) + "\"src\": \"" + src_s + "\", \"sta\": \"" + st_s + "\"}";
+        *dry = std::string(buf) + bj + "\"src\": \"" + src_s + "\", \"sta\": \"" + st_s + "\"}";
         return 0;
     }
 
@@ -1307,6 +1393,28 @@ int swpc_host_check(const char* inf_path, char* summary, size_t n) {
     } catch (const std::exception& e) {
         return swpc::set_err(SWPC_E_IO, e.what());
     }
+}
+
+int swpc_host_banner(swpc_sim* sim, char* buf, size_t n) {
+    std::string t;
+    {
+        std::lock_guard<std::mutex> lk(g_meta_mu);
+        auto it = g_meta.find(sim);
+        if (it == g_meta.end()) return swpc::set_err(SWPC_E_STATE, "simulation was not made by swpc_host_prepare");
+        t = banner_text(it->second);
+    }
+    if (buf && n) {
+        size_t m = std::min(n - 1, t.size());
+        std::memcpy(buf, t.data(), m);
+        buf[m] = 0;
+    }
+    return (int)t.size();
+}
+
+int swpc_host_ntdec_r(swpc_sim* sim) {
+    std::lock_guard<std::mutex> lk(g_meta_mu);
+    auto it = g_meta.find(sim);
+    return it == g_meta.end() ? 0 : it->second.p.ntdec_r;
 }
 
 int swpc_host_nt(swpc_sim* sim) {

@@ -26,6 +26,7 @@ struct Plan {
 struct Sim {
     swpc_dims dims;
     Plan p;
+    int device = 0;  // CUDA device the simulation was created on
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // PML shell kernels, joined back into `stream` every phase
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_fork2 = nullptr, ev_join2 = nullptr;
@@ -69,14 +70,21 @@ struct Sim {
     struct Pending { int cls; cudaEvent_t a, b; };
     std::vector<cudaEvent_t> ev_pool;
     std::vector<Pending> pending;
-    double prof_ms[6] = {0, 0, 0, 0, 0, 0};
-    long long prof_n[6] = {0, 0, 0, 0, 0, 0};
+    // timing classes: 0..5 as swpc_gpu_profile_read, then the PML launch
+    // classes (PML_CLASS_MASK order) of the stress (6..9) and velocity
+    // (10..13) updates
+    static constexpr int NPROF = 6 + 2 * PML_NCLASS;
+    double prof_ms[NPROF] = {};
+    long long prof_n[NPROF] = {};
+    // shell points of each PML launch class and the sum over them of the
+    // number of damped axes (the auxiliaries kept per point)
+    long long pml_pts[PML_NCLASS] = {}, pml_axpts[PML_NCLASS] = {};
 
     ~Sim();
     int dalloc(void** ptr, size_t bytes);
     int allocate();
     void plan_pml_parts(const std::vector<float>& prof);
-    void launch_pml(bool stress, cudaStream_t st);
+    void launch_pml(bool stress, cudaStream_t st, bool timed = false);
     int upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
                       const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
                       const int* kob_bot, const double* ts, bool column);

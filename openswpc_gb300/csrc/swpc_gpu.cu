@@ -138,12 +138,27 @@ void Sim::fill_zargs(ZArgs& z) const {
 }
 
 // the PML stress (or velocity) update: one launch per class that has parts
-void Sim::launch_pml(bool stress, cudaStream_t st) {
+// (timed: an event pair around each launch, timing class 6 + q for the
+// stress and 6 + PML_NCLASS + q for the velocity update of class q)
+void Sim::launch_pml(bool stress, cudaStream_t st, bool timed) {
+    const int base = 6 + (stress ? 0 : PML_NCLASS);
+    auto ev = [&](int c) {
+        cudaEvent_t a = get_event(), b = get_event();
+        cudaEventRecord(a, st);
+        return Pending{c, a, b};
+    };
+    auto done = [&](Pending pe) {
+        cudaEventRecord(pe.b, st);
+        pending.push_back(pe);
+    };
     if (!pml_split) {
         if (pml_all.nblocks == 0) return;
         const unsigned nb = (unsigned)pml_all.nblocks;
+        Pending pe{};
+        if (timed) pe = ev(base + PML_NCLASS - 1);
         if (stress) k_stress_pml<7><<<nb, PTPB, 0, st>>>(pml_all);
         else k_vel_pml<7><<<nb, PTPB, 0, st>>>(pml_all);
+        if (timed) done(pe);
         ++launches;
         return;
     }
@@ -151,12 +166,15 @@ void Sim::launch_pml(bool stress, cudaStream_t st) {
         const PArgs& a = pml_cls[q];
         if (a.nblocks == 0) continue;
         const unsigned nb = (unsigned)a.nblocks;
+        Pending pe{};
+        if (timed) pe = ev(base + q);
         switch (PML_CLASS_MASK[q]) {
         case 1: stress ? k_stress_pml<1><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<1><<<nb, PTPB, 0, st>>>(a); break;
         case 2: stress ? k_stress_pml<2><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<2><<<nb, PTPB, 0, st>>>(a); break;
         case 4: stress ? k_stress_pml<4><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<4><<<nb, PTPB, 0, st>>>(a); break;
         default: stress ? k_stress_pml<7><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<7><<<nb, PTPB, 0, st>>>(a); break;
         }
+        if (timed) done(pe);
         ++launches;
     }
 }
@@ -208,7 +226,7 @@ int Sim::launch_step(bool timed) {
     }
     if (p.pml) {
         ev0(2, sp);
-        launch_pml(true, sp);
+        launch_pml(true, sp, timed);
         ev1(2, sp);
         if (two) cudaEventRecord(ev_join, stream2);
     }
@@ -238,7 +256,7 @@ int Sim::launch_step(bool timed) {
     }
     if (p.pml) {
         ev0(3, sp);
-        launch_pml(false, sp);
+        launch_pml(false, sp, timed);
         ev1(3, sp);
         if (two) cudaEventRecord(ev_join2, stream2);
     }
@@ -694,18 +712,21 @@ int swpc_gpu_fetch_field(swpc_sim* sim, int which, double* out) {
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) double g_field_scratch[SWPC_STATIC_FIELD_MAX];
 
-// Device address of g_field_scratch, looked up once per device.  In host code
-// the symbol name is only a host-side stand-in, never a device address.
-static int static_scratch(double** out) {
+// Device address of g_field_scratch on device `dev` (the simulation's), looked
+// up once per device with that device current.  In host code the symbol name
+// is only a host-side stand-in, never a device address.
+static int static_scratch(int dev, double** out) {
     static std::mutex mu;
     static void* addr[128] = {};
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 128) return set_err(SWPC_E_ARG, "device ordinal out of range");
     std::lock_guard<std::mutex> lk(mu);
     if (!addr[dev]) {
+        int cur = 0;
+        CK(cudaGetDevice(&cur));
+        if (cur != dev) CK(cudaSetDevice(dev));
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_field_scratch);
+        if (cur != dev) cudaSetDevice(cur);
         if (e != cudaSuccess || !p)
             return set_err(SWPC_E_CUDA, std::string("cudaGetSymbolAddress(g_field_scratch): ") + cudaGetErrorString(e));
         addr[dev] = p;
@@ -716,14 +737,17 @@ static int static_scratch(double** out) {
 
 extern "C" int swpc_gpu_fetch_field_static(swpc_sim* sim, int which, double* out) {
     Sim* s = reinterpret_cast<Sim*>(sim);
-    if (!s || !out || which < 0 || which > 8) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_fetch_field_static");
+    if (!s || !out) return set_err(SWPC_E_ARG, "null argument to swpc_gpu_fetch_field_static");
+    if (which < 0 || which > 8)
+        return set_err(SWPC_E_ARG, "swpc_gpu_fetch_field_static reads the wavefields 0..8 (Vx .. Sxy) only; "
+                                   "use swpc_gpu_fetch_field for the medium fields");
     const Geo& g = s->p.g;
     const size_t n = (size_t)g.nx * g.ny * g.nz;
     if (n > (size_t)SWPC_STATIC_FIELD_MAX)
         return set_err(SWPC_E_ARG, "grid of " + std::to_string(n) + " points exceeds the static read-back limit of " +
                                        std::to_string((long long)SWPC_STATIC_FIELD_MAX) + " points; use swpc_gpu_fetch_field");
     double* d = nullptr;
-    int rc = static_scratch(&d);
+    int rc = static_scratch(s->device, &d);  // the scratch of the device the simulation lives on
     if (rc) return rc;
     // every one of the n elements copied back is written by the gather first,
     // so the array needs no clearing
@@ -810,7 +834,23 @@ int swpc_gpu_profile(swpc_sim* sim, int enable) {
     int rc = s->drain_events();
     if (rc) return rc;
     s->profiling = enable != 0;
-    for (int c = 0; c < 6; ++c) { s->prof_ms[c] = 0; s->prof_n[c] = 0; }
+    for (int c = 0; c < Sim::NPROF; ++c) { s->prof_ms[c] = 0; s->prof_n[c] = 0; }
+    return 0;
+}
+
+int swpc_gpu_profile_read_pml(swpc_sim* sim, double* ms, long long* n, long long* points, long long* axis_points) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    int rc = s->drain_events();
+    if (rc) return rc;
+    for (int c = 0; c < 2 * PML_NCLASS; ++c) {
+        if (ms) ms[c] = s->prof_ms[6 + c];
+        if (n) n[c] = s->prof_n[6 + c];
+    }
+    for (int q = 0; q < PML_NCLASS; ++q) {
+        if (points) points[q] = s->pml_pts[q];
+        if (axis_points) axis_points[q] = s->pml_axpts[q];
+    }
     return 0;
 }
 
@@ -899,6 +939,7 @@ int Sim::allocate() {
     // costs more: 4.67 ms at 492, 4.54 at 123, 4.95 at 16 planes)
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
+    device = dev;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     long long cols = (long long)((p.nxi + TBX - 1) / TBX) * ((p.nyi + TBY - 1) / TBY);
     long long want = 8LL * nsm;
@@ -962,6 +1003,7 @@ void Sim::plan_pml_parts(const std::vector<float>& prof) {
         if (i != n[ax]) ends_only = false;
     }
     std::vector<PmlPart> cls[PML_NCLASS];
+    long long cls_pts[PML_NCLASS] = {}, cls_ax[PML_NCLASS] = {};
     bool fits = ends_only;
     if (ends_only) {
         for (int b = 0; b < p.nbox; ++b) {
@@ -988,6 +1030,9 @@ void Sim::plan_pml_parts(const std::vector<float>& prof) {
                         for (int q = 0; q < PML_NCLASS - 1; ++q)
                             if (PML_CLASS_MASK[q] == mask) c = q;
                         cls[c].push_back(P);
+                        const long long np = (long long)P.nx * P.ny * P.nz;
+                        cls_pts[c] += np;
+                        cls_ax[c] += np * ((mask & 1) + (mask >> 1 & 1) + (mask >> 2 & 1));
                     }
         }
         for (int q = 0; q < PML_NCLASS; ++q)
@@ -1013,6 +1058,22 @@ void Sim::plan_pml_parts(const std::vector<float>& prof) {
         pml_all.nblocks += (int)(((long long)B.nx * B.ny * B.nz + PTPB - 1) / PTPB);
     }
     pml_split = p.npml >= 4000000LL;
+    // shell points and damped-axis points per launch class, for the byte
+    // count of each class (one general launch: everything in the last class)
+    for (int q = 0; q < PML_NCLASS; ++q) pml_pts[q] = pml_axpts[q] = 0;
+    if (pml_split && fits) {
+        for (int q = 0; q < PML_NCLASS; ++q) { pml_pts[q] = cls_pts[q]; pml_axpts[q] = cls_ax[q]; }
+    } else {
+        for (int b = 0; b < p.nbox; ++b) {
+            const PmlBox& B = p.box[b];
+            long long sx = 0, sy = 0, sz = 0;
+            for (int i = 0; i < B.nx; ++i) sx += damp[0][B.x0 + i];
+            for (int j = 0; j < B.ny; ++j) sy += damp[1][B.y0 + j];
+            for (int k = 0; k < B.nz; ++k) sz += damp[2][B.z0 + k];
+            pml_pts[PML_NCLASS - 1] += (long long)B.nx * B.ny * B.nz;
+            pml_axpts[PML_NCLASS - 1] += sx * B.ny * B.nz + sy * (long long)B.nx * B.nz + sz * (long long)B.nx * B.ny;
+        }
+    }
     for (int q = 0; q < PML_NCLASS; ++q) {
         PArgs& c = pml_cls[q];
         c = pml_args;

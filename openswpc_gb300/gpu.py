@@ -59,6 +59,7 @@ EXPORTS = [
     "swpc_host_request_dims", "swpc_host_materialize", "swpc_host_request_free", "swpc_serve_create",
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
+    "swpc_gpu_profile_read_pml", "swpc_host_banner", "swpc_host_ntdec_r",
 ]
 
 
@@ -101,6 +102,7 @@ def lib(build=True):
     L.swpc_gpu_fetch_field_static.argtypes = [vp, i, dp]
     L.swpc_gpu_profile.argtypes = [vp, i]
     L.swpc_gpu_profile_read.argtypes = [vp, dp, ip]
+    L.swpc_gpu_profile_read_pml.argtypes = [vp, dp, ip, ip, ip]
     L.swpc_gpu_stream.argtypes = [vp]
     L.swpc_gpu_stream.restype = vp
     L.swpc_gpu_launch_count.argtypes = [vp]
@@ -111,6 +113,8 @@ def lib(build=True):
     L.swpc_host_write_sac.argtypes = [vp, ctypes.c_char_p]
     L.swpc_host_write_snp.argtypes = [vp, ctypes.c_char_p]
     L.swpc_host_nt.argtypes = [vp]
+    L.swpc_host_ntdec_r.argtypes = [vp]
+    L.swpc_host_banner.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     L.swpc_host_check.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
     L.swpc_host_medium.argtypes = [i, i, i, i, d, d, d] + [fp] * 5 + [ip] * 6 + [dp]
     L.swpc_gpu_reset.argtypes = [vp]
@@ -339,6 +343,8 @@ class Simulation:
         d = self.dims
         if d is None:
             raise SwpcError(-1, "field_static() needs the dims the simulation was created with")
+        if name not in FIELDS:
+            raise SwpcError(-1, "field_static() reads the wavefields %s only, not %r" % (", ".join(FIELDS), name))
         out = np.zeros((d.ny, d.nx, d.nz), np.float64)
         _ck(lib().swpc_gpu_fetch_field_static(self._h, FIELDS.index(name), out.ctypes.data))
         return out
@@ -356,6 +362,17 @@ class Simulation:
         n = np.zeros(6, np.int64)
         _ck(lib().swpc_gpu_profile_read(self._h, ms.ctypes.data, n.ctypes.data))
         return ms, n
+
+    def profile_read_pml(self):
+        """PML time by launch class (x only, y only, z only, rest): ms and
+        launches as (2, 4) arrays (stress, velocity), the shell points of
+        each class and the sum of damped axes over those points."""
+        ms = np.zeros(8, np.float64)
+        n = np.zeros(8, np.int64)
+        pts = np.zeros(4, np.int64)
+        ax = np.zeros(4, np.int64)
+        _ck(lib().swpc_gpu_profile_read_pml(self._h, ms.ctypes.data, n.ctypes.data, pts.ctypes.data, ax.ctypes.data))
+        return ms.reshape(2, 4), n.reshape(2, 4), pts, ax
 
     def stream(self):
         return lib().swpc_gpu_stream(self._h)

@@ -657,6 +657,7 @@ struct Sim : SimBase {
         if (vm5) {
             // caller-provided rho, lam, mu, qp, qs over the halo grid (a stand-in for a model file)
             size_t n = rho.d.size();
+#pragma omp parallel for schedule(static)
             for (size_t q = 0; q < n; ++q) {
                 rho.d[q] = (SP)vm5[q]; lam.d[q] = (SP)vm5[n + q]; mu.d[q] = (SP)vm5[2 * n + q];
                 taup.d[q] = (SP)vm5[3 * n + q]; taus.d[q] = (SP)vm5[4 * n + q];
@@ -683,6 +684,10 @@ struct Sim : SimBase {
         SP fmin = (SP)p.fq_min, fmax = (SP)p.fq_max, fref = (SP)p.fq_ref;
         visco_set_relaxtime(fmin, fmax);
         SP zeta = visco_constq_zeta(fmin, fmax);
+        // (every point on its own: the set-up loops of this restatement run
+        // in parallel to keep large grids' set-up short; the values are the
+        // same as in serial order)
+#pragma omp parallel for schedule(static)
         for (size_t q = 0; q < taup.d.size(); ++q) { taup.d[q] = nm * zeta / taup.d[q]; taus.d[q] = nm * zeta / taus.d[q]; }
         // relaxed_medium :231-271
         {
@@ -695,6 +700,7 @@ struct Sim : SimBase {
                 cc += C((SP)v.real(), (SP)v.imag());
             }
             cc = cc / (SP)nm;
+#pragma omp parallel for schedule(static)
             for (size_t q = 0; q < mu.d.size(); ++q) {
                 SP rb2 = mu.d[q], ra2 = lam.d[q] + 2 * mu.d[q];
                 SP chi_mu = (SP)1.0 / (((SP)1.0) / std::sqrt(C(1, 0) - cc * taus.d[q])).real();

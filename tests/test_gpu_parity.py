@@ -55,6 +55,54 @@ def test_waveforms_match_oracle(small_inf, variant):
 
 
 @pytest.mark.gpu
+def test_full_length_small_configuration(tmp_path):
+    """The small plain configuration over its whole nt = 1000 steps: receiver
+    traces within 1e-5 of the fp32 oracle (the error against the fp64 oracle
+    is stated)."""
+    inf = configs.write_plain_small(str(tmp_path), nt=1000)
+    o = pyoracle.Oracle(inf, "fp32")
+    s = sim_from_oracle(o)
+    o.run(1000)
+    s.run(1, 1000)
+    w, w32 = s.waveforms(), o.waveforms()
+    s.close()
+    o.close()
+    o64 = pyoracle.Oracle(inf, "fp64")
+    o64.run(1000)
+    w64 = o64.waveforms()
+    o64.close()
+    m32, m64 = misfit(w, w32), misfit(w, w64)
+    print("small configuration, 1000 steps: misfit vs fp32 oracle %.3e, vs fp64 oracle %.3e" % (m32, m64))
+    assert m32 <= TOL, m32
+    assert m64 <= TOL, m64
+
+
+@pytest.mark.gpu
+def test_vmax_matches_oracle(small_inf):
+    """max |V| at the ocean bottom every ntdec_r steps (kernel__vmax,
+    m_kernel.f90:350-374, as report__progress prints it, m_report.f90:157)
+    equals the oracle's."""
+    o = pyoracle.Oracle(small_inf, "fp32")
+    assert o.ntdec_r > 0
+    s = sim_from_oracle(o, ntdec_r=o.ntdec_r)
+    nrep = 240 // o.ntdec_r
+    got = []
+    for q in range(nrep):
+        s.run(q * o.ntdec_r + 1, (q + 1) * o.ntdec_r)
+        got.append(s.vmax())
+    o.run(nrep * o.ntdec_r)
+    ref = o.vmax_log()
+    s.close()
+    assert ref.shape[0] == len(got) == nrep
+    assert np.array_equal(ref[:, 0], np.arange(1, len(got) + 1) * o.ntdec_r)
+    ref_v = ref[:, 1:].astype(np.float64) * o.UC * o.M0
+    got = np.array(got, np.float64)
+    assert np.all(ref_v > 0)
+    assert misfit(got, ref_v) <= TOL, misfit(got, ref_v)
+    assert np.allclose(got, ref_v, rtol=1e-4, atol=0)
+
+
+@pytest.mark.gpu
 def test_step_by_step_equals_graph_replay(small_inf):
     o = pyoracle.Oracle(small_inf, "fp32")
     a = sim_from_oracle(o)

@@ -18,6 +18,32 @@ from oracle import pyoracle
 from tests.helpers import misfit, sim_from_oracle
 
 TOL = 1e-5  # the relative L2 tolerance used by the parity tests
+CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8  # cuda.h CUmemPool_attribute
+
+
+def _pool_high(dev=0, reset=False):
+    """High-water mark of used bytes of the device's default memory pool (the
+    pool cudaMallocAsync draws on), through the driver API; with reset the
+    mark is set back to zero first."""
+    import ctypes
+    cu = ctypes.CDLL("libcuda.so.1")
+    d = ctypes.c_int()
+    assert cu.cuDeviceGet(ctypes.byref(d), dev) == 0
+    pool = ctypes.c_void_p()
+    assert cu.cuDeviceGetDefaultMemPool(ctypes.byref(pool), d) == 0
+    v = ctypes.c_uint64(0)
+    if reset:
+        assert cu.cuMemPoolSetAttribute(pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH, ctypes.byref(v)) == 0
+    assert cu.cuMemPoolGetAttribute(pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH, ctypes.byref(v)) == 0
+    return int(v.value)
+
+
+def _free_bytes():
+    import ctypes
+    cu = ctypes.CDLL("libcuda.so.1")
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert cu.cuMemGetInfo_v2(ctypes.byref(free), ctypes.byref(total)) == 0
+    return int(free.value)
 
 
 @pytest.mark.gpu
@@ -38,6 +64,37 @@ def test_static_read_back_matches_allocating_read_back(tmp_path):
     # next must not see them
     vx = s.field_static("Vx")
     assert np.array_equal(vx, s.field("Vx"))
+    # no device allocation: the default pool's high-water mark (reset to the
+    # bytes in use) does not move across two static read-backs, while the
+    # allocating read-back, which gathers through a pool allocation, raises
+    # it; the free device memory is the same before and after
+    s.sync()
+    free0 = _free_bytes()
+    h0 = _pool_high(reset=True)
+    s.field_static("Sxx")
+    s.field_static("Vy")
+    assert _pool_high() == h0
+    assert _free_bytes() == free0
+    s.field("Sxx")
+    assert _pool_high() > h0
+    s.close()
+
+
+@pytest.mark.gpu
+def test_static_read_back_refuses_medium_fields(tmp_path):
+    """Only the nine wavefields are served; the medium fields (9..13 of the
+    allocating read-back) are refused with SWPC_E_ARG."""
+    import ctypes
+    inf = configs.write_plain_small(str(tmp_path), nt=10, nx=64, ny=64, nz=48, xbeg=-16.0, ybeg=-16.0, na=10)
+    s = gpu.Simulation.from_inf(inf)
+    out = np.zeros(64 * 64 * 48, np.float64)
+    for which in (9, 13, -1, 14):
+        rc = gpu.lib().swpc_gpu_fetch_field_static(s.handle, which, out.ctypes.data_as(ctypes.c_void_p))
+        assert rc == -1, which
+    assert "0..8" in gpu.last_error()
+    with pytest.raises(gpu.SwpcError) as e:
+        s.field_static("rho")
+    assert e.value.code == -1
     s.close()
 
 
