@@ -44,6 +44,11 @@ WORKLOADS = {
     "large": dict(nx=1024, ny=1024, nz=512, dx=0.25, dt=0.01, nt=4000, nst=1024, ntdec_s=100),
     "mid": dict(nx=512, ny=512, nz=256, dx=0.5, dt=0.02, nt=3000, nst=256, ntdec_s=100),
     "small": dict(nx=128, ny=128, nz=64, dx=0.5, dt=0.02, nt=1000, nst=16, ntdec_s=100),
+    # the profiling case: the large workload's medium model on a grid of about
+    # 3.7 GB on the device (its PML shell large enough to run the per-axis
+    # launch classes), far larger than L2, so that DRAM counters of one
+    # launch mean something
+    "profile": dict(nx=384, ny=384, nz=192, dx=0.25, dt=0.01, nt=1000, nst=64, ntdec_s=100),
 }
 
 # Algorithmic bytes per grid point and step (FP32 storage, nm = 3): every
@@ -137,23 +142,36 @@ class Clocks:
         return out
 
 
-def make_medium(w, seed):
-    """Raw model over the halo grid, then the reference's medium
-    post-processing (FP64, swpc_host_medium)."""
+def make_medium(w, seed, where="device"):
+    """The workload's medium.  where = "device": the background column and
+    the periodic perturbation field, from which the library builds and
+    post-processes every cell on the GPU (swpc_gpu_build_medium_rmed);
+    where = "host": every cell built in numpy and post-processed on the host
+    in FP64 (swpc_host_medium), then uploaded as five full arrays.  Both give
+    the same medium bit for bit."""
     from openswpc_gb300 import configs, gpu
     nx, ny, nz, dx = w["nx"], w["ny"], w["nz"], w["dx"]
     zbeg = -3 * dx
-    rho, lam, mu, qp, qs = configs.gradient_random_medium(nx, ny, nz, dx, zbeg, seed=seed)
+    bg, xi, kxi0 = configs.gradient_random_fields(nx, ny, nz, dx, zbeg, seed=seed)
+    if where == "device":
+        return dict(bg=bg, xi=xi, kxi0=kxi0, zbeg=zbeg, where=where)
+    rho, lam, mu, qp, qs = configs.rmed_apply(bg, xi, nx, ny, nz, kxi0)
     qp = np.ascontiguousarray(qp)
     qs = np.ascontiguousarray(qs)
     taup, taus, maps, ts = gpu.host_medium(nx, ny, nz, 20, 0.05, 5.0, 1.0, rho, lam, mu, qp, qs)
-    return dict(rho=rho, lam=lam, mu=mu, taup=taup, taus=taus, maps=maps, ts=ts, zbeg=zbeg)
+    return dict(rho=rho, lam=lam, mu=mu, taup=taup, taus=taus, maps=maps, ts=ts, zbeg=zbeg, where=where)
 
 
-def source_and_stations(w, med, seed):
+def medium_bytes(med):
+    """Host bytes the medium upload reads."""
+    if med["where"] == "device":
+        return int(med["bg"].nbytes + med["xi"].nbytes)
+    return sum(int(med[k].nbytes) for k in ("rho", "lam", "mu", "taup", "taus")) + sum(int(m.nbytes) for m in med["maps"])
+
+
+def source_and_stations(w, kfs, zbeg, seed):
     rng = np.random.default_rng(seed + 1)
     nx, ny, nz, dx = w["nx"], w["ny"], w["nz"], w["dx"]
-    zbeg = med["zbeg"]
     ks = int(np.ceil((min(15.0, 0.6 * nz * dx) - zbeg) / dx))
     src = np.array([[nx // 2, ny // 2, ks]], np.int32)
     s, d, r = [np.deg2rad(v) for v in (rng.uniform(0, 360), rng.uniform(0, 90), rng.uniform(-180, 180))]
@@ -163,7 +181,6 @@ def source_and_stations(w, med, seed):
                      -(np.cos(d) * np.cos(r) * np.sin(s) - np.cos(2 * d) * np.sin(r) * np.cos(s)),
                      -(np.cos(d) * np.cos(r) * np.cos(s) + np.cos(2 * d) * np.sin(r) * np.sin(s)),
                      np.sin(d) * np.cos(r) * np.cos(2 * s) + 0.5 * np.sin(2 * d) * np.sin(r) * np.sin(2 * s)]])
-    kfs = med["maps"][0]
     ii = rng.integers(26, nx - 25, w["nst"])
     jj = rng.integers(26, ny - 25, w["nst"])
     kk = kfs[jj + 2, ii + 2] + 1
@@ -171,18 +188,24 @@ def source_and_stations(w, med, seed):
     return src, mij, sta
 
 
-def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None):
+def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None, seed=20261203):
+    """A simulation of the workload: medium (built on the device or uploaded,
+    see make_medium), the moment-tensor source, the receivers and the xy
+    velocity snapshot."""
     from openswpc_gb300 import gpu
     dims = gpu.make_dims(w["nx"], w["ny"], w["nz"], nt, w["dx"], w["dx"], w["dx"], w["dt"], na=20, store=store,
                          xbeg=-w["nx"] * w["dx"] / 2, ybeg=-w["ny"] * w["dx"] / 2, zbeg=med["zbeg"], fcut=1.0,
                          M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant, concurrent=concurrent)
     sim = gpu.Simulation(dims)
-    m = med["maps"]
-    sim.upload_medium(med["rho"], med["lam"], med["mu"], med["taup"], med["taus"], m[0], m[1], m[2], m[3], m[4], m[5],
-                      med["ts"])
-    src, mij, sta = med["src"], med["mij"], med["sta"]
-    sim.set_sources(src, np.array([[0.0, 1.0]]), mo=np.array([1.0]), mij=mij, stftype="kupper")
-    sim.set_receivers(sta, ntdec_w=1, flags=gpu.SWPC_WAV_V)
+    if med["where"] == "device":
+        maps, _ = sim.build_medium_rmed(med["bg"], med["xi"], med["kxi0"], fq_min=0.05, fq_max=5.0, fq_ref=1.0)
+    else:
+        maps = med["maps"]
+        sim.upload_medium(med["rho"], med["lam"], med["mu"], med["taup"], med["taus"], *maps, med["ts"])
+    if "sta" not in med:
+        med["src"], med["mij"], med["sta"] = source_and_stations(w, maps[0], med["zbeg"], seed)
+    sim.set_sources(med["src"], np.array([[0.0, 1.0]]), mo=np.array([1.0]), mij=med["mij"], stftype="kupper")
+    sim.set_receivers(med["sta"], ntdec_w=1, flags=gpu.SWPC_WAV_V)
     z0 = int(np.ceil((0.25 - med["zbeg"]) / w["dx"]))
     sim.set_snapshot(gpu.SWPC_SNAP_XY_V, z0, 1, 1, w["ntdec_s"])
     return sim
@@ -221,32 +244,92 @@ def barrier(world):
         dist.barrier()
 
 
-def cpu_sample(steps=8, warmup=2, n=(512, 512, 256), dx=0.5, dt=0.02, mode="mixed", seed=20261203):
+def mem_available():
+    """Host memory available now (bytes), from /proc/meminfo."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def oracle_bytes(nx, ny, nz, na=20, mode="mixed"):
+    """Host bytes the oracle holds for a grid (mixed precision: V and S in
+    FP64, the medium, the 18 shell auxiliaries over the whole grid as the
+    reference allocates them, the 18 memory variables over the interior),
+    plus the raw medium handed to it."""
+    halo = (nx + 6) * (ny + 6) * (nz + 6)
+    vs = 9 * (8 if mode != "fp32" else 4)
+    n_int = (nx - 2 * na) * (ny - 2 * na) * (nz - na)
+    return halo * (vs + 20 + 72 + 20) + 72 * n_int
+
+
+def write_workload_inputs(d, w, nt, seed):
+    """input.inf, source and stations of the large single-source workload for
+    the CPU oracle: the grid, spacing and time step of `w`, the bench's
+    moment tensor (same draws as source_and_stations) at 15 km, 1024 random
+    surface receivers and the xy velocity snapshot every ntdec_s steps."""
+    from openswpc_gb300 import configs
+    nx, ny, nz, dx = w["nx"], w["ny"], w["nz"], w["dx"]
+    inf = configs.write_plain_small(d, nt=nt, nx=nx, ny=ny, nz=nz, dx=dx, dy=dx, dz=dx, dt=w["dt"],
+                                    xbeg=-nx * dx / 2, ybeg=-ny * dx / 2, zbeg=-3 * dx, ntdec_r=100,
+                                    xy_v_sw=True, z0_xy=0.25, ntdec_s=w["ntdec_s"])
+    rng = np.random.default_rng(seed + 1)
+    s, dp, r = rng.uniform(0, 360), rng.uniform(0, 90), rng.uniform(-180, 180)
+    with open(os.path.join(d, "source.dat"), "w") as f:
+        f.write("  0.0 0.0 %.4f 0.0 1.0 1.0e16 %.6f %.6f %.6f\n" % (min(15.0, 0.6 * nz * dx), s, dp, r))
+    ii = rng.integers(26, nx - 25, w["nst"])
+    jj = rng.integers(26, ny - 25, w["nst"])
+    with open(os.path.join(d, "stations.xy"), "w") as f:
+        for q, (i, j) in enumerate(zip(ii, jj)):
+            f.write("  %.4f %.4f 0.0 R%04d fsb\n" % (-nx * dx / 2 + (i - 0.5) * dx, -ny * dx / 2 + (j - 0.5) * dx, q))
+    return inf
+
+
+def cpu_sample(steps=8, warmup=2, n=(512, 512, 256), dx=0.5, dt=0.02, mode="mixed", seed=20261203, w=None):
     """The reference's CPU path (oracle restatement, -O2 -ffast-math -fopenmp,
-    all host threads) on a bounded sample of the workload: the same medium
-    construction on a smaller grid."""
+    all host threads).  With `w` the workload itself (its grid, spacing,
+    source, receivers and snapshot); otherwise a bounded sample: the same
+    medium construction on a smaller grid."""
     from openswpc_gb300 import configs
     from oracle import pyoracle
     pyoracle.use_fast_build()
-    nx, ny, nz = n
+    if w is not None:
+        nx, ny, nz, dx = w["nx"], w["ny"], w["nz"], w["dx"]
+    else:
+        nx, ny, nz = n
+    cores = os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as d:
-        inf = configs.write_plain_small(d, nt=steps + warmup, nx=nx, ny=ny, nz=nz, dx=dx, dy=dx, dz=dx, dt=dt,
-                                        xbeg=-nx * dx / 2, ybeg=-ny * dx / 2, zbeg=-3 * dx, sw_wav_v=False)
+        if w is not None:
+            inf = write_workload_inputs(d, w, steps + warmup, seed)
+        else:
+            inf = configs.write_plain_small(d, nt=steps + warmup, nx=nx, ny=ny, nz=nz, dx=dx, dy=dx, dz=dx, dt=dt,
+                                            xbeg=-nx * dx / 2, ybeg=-ny * dx / 2, zbeg=-3 * dx, sw_wav_v=False)
+        t0 = time.perf_counter()
         rho, lam, mu, qp, qs = configs.gradient_random_medium(nx, ny, nz, dx, -3 * dx, seed=seed)
-        vm = np.stack([rho, lam, mu, np.ascontiguousarray(qp), np.ascontiguousarray(qs)])
+        vm = np.empty((5,) + rho.shape, np.float32)
+        for q, a in enumerate((rho, lam, mu, qp, qs)):
+            vm[q] = a
         del rho, lam, mu, qp, qs
-        cores = os.cpu_count() or 1
         o = pyoracle.Oracle(inf, mode, cores, medium=vm)
         del vm
+        t_setup = time.perf_counter() - t0
         o.run(warmup)
         t = time.perf_counter()
         o.run(steps)
         el = time.perf_counter() - t
         o.close()
-    return dict(value=nx * ny * nz * steps / el, unit="pt/s", cores=cores, kind="port",
-                sample="%dx%dx%d grid of the same medium model, %d timed steps after %d warm-up, %s precision"
-                       % (nx, ny, nz, steps, warmup, mode),
-                seconds=el)
+    if w is not None:
+        sample = "the workload itself (%dx%dx%d, its source, %d receivers and xy snapshot), %d timed steps after %d " \
+                 "warm-up, %s precision" % (nx, ny, nz, w["nst"], steps, warmup, mode)
+    else:
+        sample = "%dx%dx%d grid of the same medium model, %d timed steps after %d warm-up, %s precision" \
+                 % (nx, ny, nz, steps, warmup, mode)
+    return dict(value=nx * ny * nz * steps / el, unit="pt/s", cores=cores, kind="port", sample=sample,
+                seconds=el, setup_s=t_setup, same_config=w is not None)
 
 
 def parity_statement():
@@ -286,13 +369,26 @@ def run_reference(args, w):
     world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
         return 0
-    cb = cpu_sample(steps=args.steps, warmup=args.warmup)
+    # the stated grid when the host can hold the oracle's arrays; otherwise a
+    # bounded sample of the same medium (and the line says so)
+    full = mem_available() > 1.2 * oracle_bytes(w["nx"], w["ny"], w["nz"])
+    if full:
+        cb = cpu_sample(steps=args.steps, warmup=2, w=w)
+    else:
+        cb = cpu_sample(steps=args.steps, warmup=args.warmup)
     line = {
         "metric": "grid-pt updates/s", "value": cb["value"], "unit": "pt/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * cb["seconds"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64/f32 (mixed, reference default)", "data": "synthetic",
-        "config": dict(arm_config(w, args, 1), sample=cb["sample"]),
+        # the workload's own config when the oracle ran the stated grid; the
+        # sample's description otherwise
+        "config": arm_config(w, args, 1) if cb["same_config"] else dict(arm_config(w, args, 1), sample=cb["sample"]),
+        "reference_run": {"sample": cb["sample"], "same_grid": cb["same_config"], "oracle_setup_s": cb["setup_s"],
+                          "timed_s": cb["seconds"],
+                          "what": "C++ restatement of the reference's CPU time loop (oracle/swpc_oracle.cpp), "
+                                  "-O2 -ffast-math -fopenmp as the reference's gfortran build, all host threads; "
+                                  "the Fortran reference itself needs gfortran, MPI and netcdf-fortran, absent here"},
         "cpu_baseline": {"value": cb["value"], "unit": "pt/s", "cores": cb["cores"], "kind": "port",
                          "sample": cb["sample"]},
         "e2e": {"value": cb["value"], "unit": "pt/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -348,9 +444,8 @@ def run_gpu(args, w):
     peak, peak_kind = peaks()
     seed = 20261203 + 7 * rank
     t_setup = time.time()
-    med = make_medium(w, seed)
-    med["src"], med["mij"], med["sta"] = source_and_stations(w, med, seed)
-    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant, concurrent=args.pml_overlap)
+    med = make_medium(w, seed, args.medium)
+    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant, concurrent=args.pml_overlap, seed=seed)
     stream = torch.cuda.ExternalStream(sim.stream())
     t_setup = time.time() - t_setup
 
@@ -419,8 +514,9 @@ def run_gpu(args, w):
     # K steps + waveform read-back + destroy
     e2e = None
     if not args.no_e2e:
+        keys = ("bg", "xi") if med["where"] == "device" else ("rho", "lam", "mu", "taup", "taus")
         pin = {}
-        for k in ("rho", "lam", "mu", "taup", "taus"):
+        for k in keys:
             t = torch.empty(med[k].shape, dtype=torch.float32, pin_memory=True)
             t.numpy()[...] = med[k]
             pin[k] = t
@@ -430,16 +526,20 @@ def run_gpu(args, w):
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant, concurrent=args.pml_overlap)
+        sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant, concurrent=args.pml_overlap,
+                         seed=seed)
         sim2.run(1, args.steps)
         wav = sim2.waveforms()
         sim2.close()
         t1 = time.perf_counter()
         e_s = reduce_max(t1 - t0, world)
-        h2d = sum(int(med[k].nbytes) for k in ("rho", "lam", "mu", "taup", "taus")) + sum(int(m.nbytes) for m in med["maps"])
+        h2d = medium_bytes(med)
+        what = ("build_medium_rmed (background column + perturbation field from pinned host memory)"
+                if med["where"] == "device" else "upload_medium (five halo arrays from pinned host memory)")
         e2e = {"value": world * npt * args.steps / e_s, "unit": "pt/s",
                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": int(wav.nbytes) // args.steps,
-               "job": "create + upload_medium (pinned host) + %d steps + fetch_waveforms + destroy" % args.steps,
+               "job": "create + %s + sources/receivers/snapshot + %d steps + fetch_waveforms + destroy"
+                      % (what, args.steps),
                "seconds": e_s}
         del pin, med_p
 
@@ -457,9 +557,9 @@ def run_gpu(args, w):
             "metric": "grid-pt updates/s", "value": value, "unit": "pt/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(arm_config(w, args, world),
-                           timed_steps="it=%d..%d (graph replay; snapshot frame at it=%s)"
-                                       % (it - 2 * args.steps, it - args.steps - 1, ",".join(map(str, frames)))),
+            "config": arm_config(w, args, world),
+            "timed_window": "it=%d..%d (graph replay; snapshot frame at it=%s)"
+                            % (it - 2 * args.steps, it - args.steps - 1, ",".join(map(str, frames))),
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
                                   "peak": peak, "frac": step_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak,
                                   "model": "%d B/interior pt + %d B/PML pt per step" % (b_int, b_pml)},
@@ -476,6 +576,7 @@ def run_gpu(args, w):
             "parity": parity_statement(),
             "batched": batch,
             "setup_s": t_setup,
+            "medium_setup": med["where"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -537,11 +638,26 @@ def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500):
         e1.synchronize()
         ms_batch = e0.elapsed_time(e1) / steps
         launches = b.launch_count() - n0
+        items = b.item_count()
+        # the same batch as one persistent fused launch per step (8-row tiles)
+        ms_persist = None
+        for s in sims:
+            tiles = s.tiles()
+        if tiles == (8, 8):
+            b.set_persistent(True)
+            b.run(warmup)
+            b.sync()
+            e0.record(st)
+            b.run(steps)
+            e1.record(st)
+            e1.synchronize()
+            ms_persist = e0.elapsed_time(e1) / steps
         b.close()
         # the same members one after another, each on its own plain path
         ms_seq = 0.0
         for s in sims:
             s.reset()
+            s.set_tiles(0, 0)
             s.set_zchunk(0)
             s.run(1, warmup)
             s.sync()
@@ -557,7 +673,9 @@ def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500):
     gbps_b = step_bytes / (ms_batch / 1e3) / 1e9
     gbps_s = step_bytes / (ms_seq / 1e3) / 1e9
     return {"members": nsim, "points_total": int(sum(pts)), "steps": steps, "warmup": warmup,
+            "form": "one launch per phase of the time step over all members, graph-replayed",
             "ms_per_step": ms_batch, "sequential_ms_per_step": ms_seq,
+            "persistent_ms_per_step": ms_persist, "persistent_items_per_step": items,
             "solves_per_s": nsim / (nt_full * ms_batch / 1e3), "sequential_solves_per_s": nsim / (nt_full * ms_seq / 1e3),
             "speedup_vs_sequential": ms_seq / ms_batch,
             "grid_pt_updates_per_s": sum(pts) / (ms_batch / 1e3),
@@ -588,7 +706,8 @@ def run_batch(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batched many-instance: %d simulations, axes in {96..256}, nt=%d"
                                    % (args.nsim, r["nt_full"]), "points_total": r["points_total"],
-                       "zchunk": [r["autotune"]["zchunk"], r["autotune"]["zchunk_vel"]] if r["autotune"] else None},
+                       "zchunk": [r["autotune"]["zchunk"], r["autotune"]["zchunk_vel"]] if r["autotune"] else None,
+                       "tiles": r["autotune"]["tiles"] if r["autotune"] else None},
             "gpu_launches": r["gpu_launches"]}
     line.update({k: v for k, v in r.items() if k not in ("gpu_launches",)})
     print(json.dumps(line), flush=True)
@@ -692,8 +811,7 @@ def run_precision(args):
     gpu.lib()
     w = WORKLOADS["mid"]
     seed = 20261203
-    med = make_medium(w, seed)
-    med["src"], med["mij"], med["sta"] = source_and_stations(w, med, seed)
+    med = make_medium(w, seed, args.medium)
     n_int, n_pml = counts(w)
     npt = w["nx"] * w["ny"] * w["nz"]
     res = {}
@@ -724,8 +842,45 @@ def run_precision(args):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "forms": forms,
            "config": {"workload": "precision form 512x512x256, large-workload medium and source, nt=%d" % args.nt,
                       "timing": "CUDA events over the whole run from it=1 (graph replay)"}}
+    if not args.no_cpu:
+        out["vs_fp64_oracle"] = precision_vs_fp64(args.nt, seed)
     print(json.dumps(out), flush=True)
     return 0
+
+
+def precision_vs_fp64(nt, seed):
+    """Receiver misfit of the three storage forms against the oracle built in
+    FP64, on a downscaled copy of the precision workload (256 x 256 x 128 at
+    the same spacing, the same medium model, source and receiver rule): the
+    FP64 oracle over the full 512 x 512 x 256 grid and nt steps would keep
+    the host busy for a quarter of an hour."""
+    from oracle import pyoracle
+    from openswpc_gb300 import configs
+    wq = dict(WORKLOADS["mid"], nx=256, ny=256, nz=128, nst=64)
+    med = make_medium(wq, seed, "device")
+    wavs = {}
+    for store in ("fp32", "fp16", "bf16"):
+        sim = build_sim(wq, med, nt, store=store, seed=seed)
+        sim.run(1, nt)
+        wavs[store] = sim.waveforms()
+        sim.close()
+    with tempfile.TemporaryDirectory() as d:
+        inf = write_workload_inputs(d, wq, nt, seed)
+        bg, xi, kxi0 = configs.gradient_random_fields(wq["nx"], wq["ny"], wq["nz"], wq["dx"], -3 * wq["dx"], seed=seed)
+        vm = np.stack(configs.rmed_apply(bg, xi, wq["nx"], wq["ny"], wq["nz"], kxi0))
+        t0 = time.perf_counter()
+        o = pyoracle.Oracle(inf, "fp64", os.cpu_count() or 1, medium=vm)
+        o.run(nt)
+        ref = o.waveforms()
+        sta = o.stations()
+        o.close()
+        t_or = time.perf_counter() - t0
+    assert np.array_equal(sta[:, :2], med["sta"][:, :2]), "oracle and GPU receivers differ"
+    den = float(np.linalg.norm(ref))
+    return {"grid": "256x256x128, dx=0.5 km, nt=%d" % nt, "oracle": "fp64 build of the oracle", "oracle_s": t_or,
+            "misfit": {k: float(np.linalg.norm(w.astype(np.float64) - ref)) / den for k, w in wavs.items()},
+            "fp16_vs_fp32": float(np.linalg.norm(wavs["fp16"] - wavs["fp32"]) / np.linalg.norm(wavs["fp32"])),
+            "bf16_vs_fp32": float(np.linalg.norm(wavs["bf16"] - wavs["fp32"]) / np.linalg.norm(wavs["fp32"]))}
 
 
 def main():
@@ -744,6 +899,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the short batched block of the default run")
+    ap.add_argument("--medium", default="device", choices=["device", "host"],
+                    help="build the random medium on the GPU (default) or on the host and upload it")
     ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])
     ap.add_argument("--variant", type=int, default=0, help="0: TMA-fed interior kernels, 1: plain smem sweep")
     ap.add_argument("--pml-overlap", type=lambda v: {"auto": None, "on": True, "off": False}[v], default=None,

@@ -112,6 +112,32 @@ int swpc_gpu_upload_medium_column(swpc_sim* sim, const float* rho, const float* 
                                   const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot,
                                   const int* kob_top, const int* kob_bot, const double* ts);
 
+/* The medium of a layered model with a random perturbation built on the
+ * device (vmodel_lhm_rmed / vmodel_lgm_rmed, src/swpc_3d/m_vmodel_lhm_rmed.f90:
+ * 21-229, followed by medium__setup, m_medium.f90:124-394), in place of
+ * building the halo arrays on the host and uploading them.
+ *   bg:  5 x (nz+6) floats, the background column at k = -2 .. nz+3:
+ *        rho0, vp0, vs0, Qp, Qs (layers or gradients as the host reads them).
+ *   xi:  the perturbation, nzc planes of nyc rows of nxc values (x fastest),
+ *        repeated periodically over the grid as src/shared/m_rdrmed.f90:73-134
+ *        wraps a field smaller than the grid.
+ *   kxi0: first 1-based k of the solid; cells above keep the column (air,
+ *        water).  Below: rho = rho0 (1 + 0.8 xi), vp = vp0 (1 + xi),
+ *        vs = vs0 (1 + xi), kept inside [vmin, vmax] and above rhomin by
+ *        vcheck (src/shared/m_fdtool.f90:15-48).
+ * The device then homogenises the absorber band, applies the tau-method,
+ * relaxes the moduli to fq_ref in FP64, finds the free surface and ocean
+ * bottom of every column and sets the coefficients as swpc_gpu_upload_medium
+ * does; the result equals host set-up (swpc_host_medium) of the same cells
+ * bit for bit.  maps6 (optional) receives the six surface maps kfs, kob,
+ * kfs_top, kfs_bot, kob_top, kob_bot, each (nx+6) x (ny+6) ints as in
+ * swpc_gpu_upload_medium, for placing stations and sources on the host; ts
+ * receives the nm relaxation times.  Host traffic: the column and the field
+ * instead of five full halo arrays. */
+int swpc_gpu_build_medium_rmed(swpc_sim* sim, const float* bg, const float* xi, int nxc, int nyc, int nzc, int kxi0,
+                               double vmin, double vmax, double rhomin, double fq_min, double fq_max, double fq_ref,
+                               int* maps6, double* ts);
+
 /* Sources (replaces source__stressglut / source__bodyforce state,
  * m_source.f90:26-36).  ijk: 3n grid indices.  mo: n normalised moments
  * (mo/M0).  mij: 6n components xx yy zz yz xz xy.  fxyz: 3n normalised body
@@ -253,6 +279,14 @@ int swpc_gpu_reset(swpc_sim* sim);
  * velocity kernel, fewer when the grid is too small to fill the GPU).  The autotuner (openswpc_gb300/autotune.py) sets them.
  * set_zchunk sets both to one depth; get_zchunk returns the stress depth. */
 int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel);
+/* Tile shape of the interior stress and velocity kernels: 32 columns by 8
+ * (default) or 16 rows each, with 8-row tiles two stress blocks or three
+ * velocity blocks share an SM, with 16-row tiles one (fewer halo rows per
+ * point, fewer blocks); 0 restores 8.  The autotuner sets them together with
+ * the z-sweep depths.  Batched members must share their tile shapes, and the
+ * persistent batch form runs 8-row tiles.  No counterpart in the reference. */
+int swpc_gpu_set_tiles(swpc_sim* sim, int rows_stress, int rows_vel);
+int swpc_gpu_get_tiles(swpc_sim* sim, int* rows_stress, int* rows_vel);
 int swpc_gpu_get_zchunks(swpc_sim* sim, int* kstress, int* kvel);
 int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk);
 int swpc_gpu_get_zchunk(swpc_sim* sim);
@@ -270,6 +304,16 @@ typedef struct swpc_batch swpc_batch;
 int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out);
 int swpc_batch_run(swpc_batch* batch, int nsteps);
 int swpc_batch_sync(swpc_batch* batch);
+/* How the batch advances a time step.  on = 1: one persistent fused launch
+ * per time step; resident blocks take every member's stress tiles, PML
+ * blocks, sources, velocity tiles, taps and snapshots from a device work
+ * queue in phase order, each item waiting (bounded) until the items of its
+ * member it depends on are done (8-row tiles only).  on = 0 (the default):
+ * one launch per phase of the step over a block table spanning all members.
+ * Both give the same results bit for bit.  No counterpart in the reference. */
+int swpc_batch_set_persistent(swpc_batch* batch, int on);
+/* Items in the persistent form's work queue for one time step. */
+int swpc_batch_item_count(swpc_batch* batch);
 void* swpc_batch_stream(swpc_batch* batch);
 long long swpc_batch_launch_count(swpc_batch* batch);
 int swpc_batch_destroy(swpc_batch* batch);

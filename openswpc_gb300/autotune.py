@@ -1,6 +1,8 @@
-"""Autotuner of the z-sweep depths of the interior kernels.
+"""Autotuner of the tile shapes and z-sweep depths of the interior kernels.
 
-Each interior block sweeps a chunk of z planes.  Long chunks amortise the
+Each interior block sweeps a chunk of z planes of a tile of 32 columns by 8
+or 16 rows.  Taller tiles read fewer halo rows per point but run fewer
+blocks per SM.  Long chunks amortise the
 pipeline prologue (the first planes of every ring are loaded before any
 compute); short chunks create more blocks, which small grids need to fill the
 GPU, and keep neighbouring blocks on the same planes so that they share halo
@@ -21,6 +23,7 @@ import numpy as np
 from . import gpu
 
 CANDIDATES = (8, 16, 32, 64, 128, 0)  # 0 = the library's automatic choice
+TILE_ROWS = (8, 16)  # rows of the 32-column tiles
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 
@@ -59,29 +62,35 @@ def _time(runner, stream, steps):
     return e0.elapsed_time(e1) / steps
 
 
-def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=CANDIDATES, batch=None):
-    """Pick the z-sweep depths of the stress and velocity kernels for `sims`
-    (one simulation, or the members of a batch when len(sims) > 1), apply
-    them to every member and return {"zchunk": stress depth, "zchunk_vel":
-    velocity depth, "ms_per_step": {depth: ms}, "ms_per_step_vel": {depth:
-    ms}} (0 = the library's automatic choice).
+def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=CANDIDATES, batch=None,
+         rows=TILE_ROWS):
+    """Pick the tile shapes and z-sweep depths of the stress and velocity
+    kernels for `sims` (one simulation, or the members of a batch when
+    len(sims) > 1), apply them to every member and return {"tiles": [stress
+    rows, velocity rows], "zchunk": stress depth, "zchunk_vel": velocity
+    depth, "ms_per_step": {"rows/depth": ms}, "ms_per_step_vel": {...}}
+    (depth 0 = the library's automatic choice).
 
-    The stress depth is swept first with the velocity kernel at its automatic
-    depth, then the velocity depth with the stress depth fixed at its best.
-    The warm-up builds the CUDA graph of the step (8 steps), so the timed
-    steps replay it as a production run does.
-    The members are stepped while timing and reset afterwards, so call this
-    after set-up and before the production run.
+    The stress kernel's (rows, depth) pairs are swept first with the
+    velocity kernel at 8 rows and its automatic depth, then the velocity
+    kernel's pairs with the stress kernel fixed at its best.  The warm-up
+    builds the CUDA graph of the step (8 steps), so the timed steps replay it
+    as a production run does.  The members are stepped while timing and
+    reset afterwards, so call this after set-up and before the production
+    run.
     """
-    key = _shape_key(sims, store)
+    key = _shape_key(sims, store) + "-tiles"
     db = _load(cache) if cache else {}
-    if key in db and "zchunk_vel" in db[key]:
+    if key in db and "tiles" in db[key]:
+        r = db[key]
         for s in sims:
-            s.set_zchunks(db[key]["zchunk"], db[key]["zchunk_vel"])
-        return db[key]
+            s.set_tiles(*r["tiles"])
+            s.set_zchunks(r["zchunk"], r["zchunk_vel"])
+        return r
 
-    def measure(ks, kv):
+    def measure(rs, ks, rv, kv):
         for s in sims:
+            s.set_tiles(rs, rv)
             s.set_zchunks(ks, kv)
         if len(sims) == 1:
             s = sims[0]
@@ -104,14 +113,16 @@ def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=
             s.reset()
         return ms
 
-    t_s = {z: measure(z, 0) for z in candidates}
+    t_s = {(r, z): measure(r, z, 8, 0) for r in rows for z in candidates}
     best_s = min(t_s, key=t_s.get)
-    t_v = {z: measure(best_s, z) for z in candidates}
+    t_v = {(r, z): measure(best_s[0], best_s[1], r, z) for r in rows for z in candidates}
     best_v = min(t_v, key=t_v.get)
     for s in sims:
-        s.set_zchunks(best_s, best_v)
-    rec = {"zchunk": best_s, "zchunk_vel": best_v, "ms_per_step": {str(k): float(v) for k, v in t_s.items()},
-           "ms_per_step_vel": {str(k): float(v) for k, v in t_v.items()}}
+        s.set_tiles(best_s[0], best_v[0])
+        s.set_zchunks(best_s[1], best_v[1])
+    rec = {"tiles": [best_s[0], best_v[0]], "zchunk": best_s[1], "zchunk_vel": best_v[1],
+           "ms_per_step": {"%d/%d" % k: float(v) for k, v in t_s.items()},
+           "ms_per_step_vel": {"%d/%d" % k: float(v) for k, v in t_v.items()}}
     if cache:
         db = _load(cache)
         db[key] = rec

@@ -205,60 +205,112 @@ def write_uniform(d, nx=64, ny=64, nz=64, nt=100, dx=0.5, dt=0.02, vp=6.0, vs=3.
     return os.path.join(d, "input.inf")
 
 
-def gradient_random_medium(nx, ny, nz, dx, zbeg, seed=DEFAULT_SEED, a=5.0, eps=0.05, na=20, qp=600.0, qs=300.0):
-    """Large single-source workload medium over the halo grid, Fortran (k,i,j)
-    order flattened as (ny+6, nx+6, nz+6): a 1-D gradient Vp = 5 -> 7 km/s
-    over depth, Vs = Vp/1.73, rho = 1.74 Vp^0.25, times (1 + xi) with xi an
-    exponential von Karman field (correlation length ``a`` km, rms ``eps``)
-    made by the spectral method (white noise -> FFT -> sqrt(PSDF) -> IFFT ->
-    de-mean -> rescale), applied per point with rho x (1 + 0.8 xi)
-    (src/swpc_3d/m_vmodel_lhm_rmed.f90:187-206).  Air above z = 0.
-
-    Returns float32 arrays rho, lam, mu, qp, qs of shape (ny+6, nx+6, nz+6).
-    The field is generated on a coarse lattice and replicated periodically
-    (src/shared/m_rdrmed.f90:73-134 wraps its field the same way), which
-    keeps set-up memory bounded for very large grids.
-    """
+def von_karman_field(nxc, nyc, nzc, dx, seed=DEFAULT_SEED, a=5.0, eps=0.05):
+    """Exponential von Karman perturbation (correlation length ``a`` km, rms
+    ``eps``) on an nxc x nyc x nzc lattice of spacing dx, by the spectral
+    method (white noise -> FFT -> sqrt(PSDF) -> IFFT -> de-mean -> rescale).
+    Returns float32 (nzc, nyc, nxc), x fastest -- the layout of one k plane
+    after another, as src/shared/m_rdrmed.f90:73-134 reads a field."""
     rng = np.random.default_rng(seed)
-    nc = [min(n, 256) for n in (nx, ny, nz)]
+    nc = (nxc, nyc, nzc)
     kx = np.fft.fftfreq(nc[0], d=dx) * 2 * np.pi
     ky = np.fft.fftfreq(nc[1], d=dx) * 2 * np.pi
     kz = np.fft.rfftfreq(nc[2], d=dx) * 2 * np.pi
     K2 = kx[:, None, None] ** 2 + ky[None, :, None] ** 2 + kz[None, None, :] ** 2
     psdf = 8 * np.pi * eps ** 2 * a ** 3 / (1 + K2 * a * a) ** 2  # exponential ACF
     w = rng.standard_normal(nc)
-    f = np.fft.irfftn(np.fft.rfftn(w) * np.sqrt(psdf), s=nc)
+    f = np.fft.irfftn(np.fft.rfftn(w) * np.sqrt(psdf), s=nc, axes=(0, 1, 2))
     f -= f.mean()
     f *= eps / f.std()
-    f = f.astype(np.float32)  # (x, y, z)
-    ii = (np.arange(-2, nx + 4) - 1) % nc[0]
-    jj = (np.arange(-2, ny + 4) - 1) % nc[1]
-    kk = (np.arange(-2, nz + 4) - 1) % nc[2]
-    z = (zbeg + (np.arange(-2, nz + 4) - 0.5) * dx).astype(np.float32)
+    return np.ascontiguousarray(f.astype(np.float32).transpose(2, 1, 0))
+
+
+def gradient_random_fields(nx, ny, nz, dx, zbeg, seed=DEFAULT_SEED, a=5.0, eps=0.05, qp=600.0, qs=300.0):
+    """The large single-source workload's medium as a background column and a
+    perturbation field: a 1-D gradient Vp = 5 -> 7 km/s over depth,
+    Vs = Vp/1.73, rho = 1.74 Vp^0.25 (air above z = 0) and a periodic
+    exponential von Karman field on a lattice of at most 256 cells per axis
+    (src/shared/m_rdrmed.f90 wraps its field the same way), which keeps
+    set-up memory bounded for very large grids.
+
+    Returns bg (5, nz+6) float32 -- rho0, vp0, vs0, qp, qs at k = -2 .. nz+3 --
+    the field xi (nzc, nyc, nxc) and kxi0, the first 1-based k of the solid
+    (the perturbation applies from there down)."""
+    nc = [min(n, 256) for n in (nx, ny, nz)]
+    xi = von_karman_field(nc[0], nc[1], nc[2], dx, seed=seed, a=a, eps=eps)
+    k = np.arange(-2, nz + 4)
+    z = (zbeg + (k - 0.5) * dx).astype(np.float32)
     zmax = zbeg + nz * dx
     vp0 = (5.0 + 2.0 * np.clip(z, 0, None) / zmax).astype(np.float32)
+    vs0 = vp0 / np.float32(1.73)
+    rho0 = np.float32(1.74) * vp0 ** np.float32(0.25)
+    air = z < 0
+    bg = np.stack([np.where(air, np.float32(0.001), rho0), np.where(air, np.float32(0), vp0),
+                   np.where(air, np.float32(0), vs0), np.where(air, np.float32(10), np.float32(qp)),
+                   np.where(air, np.float32(10), np.float32(qs))]).astype(np.float32)
+    kxi0 = int(k[np.argmax(~air)])
+    return bg, xi, kxi0
+
+
+def rmed_apply(bg, xi, nx, ny, nz, kxi0, vmin=0.0, vmax=np.inf, rhomin=1.0):
+    """Every cell of the halo grid from the background column and the
+    periodic perturbation, as vmodel_lhm_rmed builds it
+    (src/swpc_3d/m_vmodel_lhm_rmed.f90:161-212): below the topography
+    rho = rho0 (1 + 0.8 xi), vp = vp0 (1 + xi), vs = vs0 (1 + xi), held inside
+    [vmin, vmax] and above rhomin by vcheck (src/shared/m_fdtool.f90:15-48);
+    air and water keep the column.  Single precision in the reference's
+    order.  Returns rho, lam, mu, qp, qs as float32 (ny+6, nx+6, nz+6) (the
+    Fortran (k, i, j) halo layout)."""
+    f32 = np.float32
+    nzc, nyc, nxc = xi.shape
+    r0, vp0, vs0, qp0, qs0 = [np.asarray(c, np.float32) for c in bg]
+    ii = (np.arange(-2, nx + 4) - 1) % nxc
+    jj = (np.arange(-2, ny + 4) - 1) % nyc
+    kk = (np.arange(-2, nz + 4) - 1) % nzc
+    solid = (np.arange(-2, nz + 4) >= kxi0)[None, :]
+    check = solid & ((vp0 > 0) & (vs0 > 0))[None, :]
+    vmin, vmax, rhomin = f32(vmin), f32(vmax), f32(rhomin)
     shape = (ny + 6, nx + 6, nz + 6)
     rho = np.empty(shape, np.float32)
     lam = np.empty(shape, np.float32)
     mu = np.empty(shape, np.float32)
-    fx = f[ii]  # (nx+6, nyc, nzc)
-    for jo, j in enumerate(jj):
-        xi = fx[:, j, :][:, kk]  # (nx+6, nz+6)
-        vp = vp0[None, :] * (1 + xi)
-        vs = vp / 1.73
-        r = (1.74 * vp0[None, :] ** 0.25) * (1 + 0.8 * xi)
-        air = (z < 0)[None, :]
-        vp = np.where(air, 0.0, vp)
-        vs = np.where(air, 0.0, vs)
-        r = np.where(air, 0.001, r)
-        rho[jo] = r
-        mu[jo] = r * vs * vs
-        lam[jo] = r * (vp * vp - 2 * vs * vs)
-    qpa = np.where(z < 0, 10.0, qp).astype(np.float32)
-    qsa = np.where(z < 0, 10.0, qs).astype(np.float32)
-    qpv = np.broadcast_to(qpa[None, None, :], shape)
-    qsv = np.broadcast_to(qsa[None, None, :], shape)
+    xk = xi[kk]  # (nz+6, nyc, nxc)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for jo, j in enumerate(jj):
+            x = xk[:, j, :][:, ii].T  # (nx+6, nz+6)
+            one = f32(1) + x
+            r = np.where(solid, r0[None, :] * (f32(1) + f32(0.8) * x), r0[None, :])
+            vp = np.where(solid, vp0[None, :] * one, vp0[None, :])
+            vs = np.where(solid, vs0[None, :] * one, vs0[None, :])
+            gamma = vp / vs
+            gamma = np.where(gamma < f32(1.1920928955078125e-07), f32(np.sqrt(3.0)), gamma)
+            over = check & ((vp > vmax) | (vs > vmax))
+            if over.any():
+                xi2 = (one * vmax) / vp - f32(1)
+                r = np.where(over, r * (f32(1) + f32(0.8) * xi2) / (f32(1) + f32(0.8) * x), r)
+                vp = np.where(over, vmax, vp)
+                vs = np.where(over, vmax / gamma, vs)
+            under = check & ((vp < vmin) | (vs < vmin))
+            if under.any():
+                vs = np.where(under, vmin, vs)
+                vp = np.where(under, vmin * gamma, vp)
+            r = np.where(check & (r < rhomin), rhomin, r)
+            rho[jo] = r
+            mu[jo] = r * vs * vs
+            lam[jo] = r * (vp * vp - f32(2) * vs * vs)
+    qpv = np.broadcast_to(qp0[None, None, :], shape)
+    qsv = np.broadcast_to(qs0[None, None, :], shape)
     return rho, lam, mu, qpv, qsv
+
+
+def gradient_random_medium(nx, ny, nz, dx, zbeg, seed=DEFAULT_SEED, a=5.0, eps=0.05, na=20, qp=600.0, qs=300.0):
+    """Large single-source workload medium over the halo grid, Fortran (k,i,j)
+    order flattened as (ny+6, nx+6, nz+6): the background column and the
+    perturbation of gradient_random_fields applied per point by rmed_apply.
+
+    Returns float32 arrays rho, lam, mu, qp, qs of shape (ny+6, nx+6, nz+6)."""
+    bg, xi, kxi0 = gradient_random_fields(nx, ny, nz, dx, zbeg, seed=seed, a=a, eps=eps, qp=qp, qs=qs)
+    return rmed_apply(bg, xi, nx, ny, nz, kxi0)
 
 
 def write_random_medium_case(d, nx=192, ny=192, nz=128, dx=0.25, dt=0.01, nt=600, seed=DEFAULT_SEED,

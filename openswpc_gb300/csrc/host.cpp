@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/swpc_gpu.h"
+#include "visco.hpp"
 
 namespace swpc {
 int set_err(int code, const std::string& msg);
@@ -358,27 +359,9 @@ void vmodel(const Inf& inf, const Params& p, const Grid& G, std::vector<float>& 
     spread();
 }
 
-// src/shared/m_fdtool.f90:691-812 in FP64
-void relaxation_times(int nm, double fmin, double fmax, double* ts) {
-    double oa = 2 * PI * fmin, ob = 2 * PI * fmax;
-    if (nm == 1) { ts[0] = 1.0 / std::sqrt(oa * ob); return; }
-    for (int m = 0; m < nm; ++m) ts[m] = 1.0 / (oa * std::pow(ob / oa, (double)m / (nm - 1)));
-}
-double constq_zeta(int nm, double fmin, double fmax, const double* ts) {
-    double oa = 2 * PI * fmin, ob = 2 * PI * fmax, i0 = 0, i1 = 0, i2 = 0;
-    for (int m = 0; m < nm; ++m) {
-        double t = ts[m];
-        i0 += (std::log(1 + ob * ob * t * t) - std::log(1 + oa * oa * t * t)) / (2 * t);
-        i1 += ((std::atan(ob * t) - ob * t / (1 + ob * ob * t * t)) - (std::atan(oa * t) - oa * t / (1 + oa * oa * t * t))) / (2 * t);
-    }
-    for (int a = 0; a < nm - 1; ++a)
-        for (int b = a + 1; b < nm; ++b) {
-            double w1 = std::atan(ob * ts[a]) / ts[a] - std::atan(ob * ts[b]) / ts[b];
-            double w2 = std::atan(oa * ts[a]) / ts[a] - std::atan(oa * ts[b]) / ts[b];
-            i2 += ts[a] * ts[b] / (ts[b] * ts[b] - ts[a] * ts[a]) * (w1 - w2);
-        }
-    return i0 / (i1 + 2 * i2);
-}
+namespace visco = swpc::visco;
+using visco::constq_zeta;
+using visco::relaxation_times;
 
 // src/swpc_3d/m_medium.f90:124-394 in FP64: absorber homogenisation,
 // tau-method, relaxation of the moduli to fq_ref, surface detection.
@@ -403,29 +386,23 @@ void medium_post(int nx, int ny, int nz, int na, double fq_min, double fq_max, d
     const int nm = 3;
     relaxation_times(nm, fq_min, fq_max, ts);
     const double zeta = constq_zeta(nm, fq_min, fq_max, ts);
-    std::complex<double> cc(0, 0);
-    const double om = 2 * PI * fq_ref;
-    for (int m = 0; m < nm; ++m) {
-        std::complex<double> iw(0, om * ts[m]);
-        cc += iw / (1.0 - iw);
-    }
-    cc /= (double)nm;
+    double cr, ci;
+    visco::zener_c(nm, fq_ref, ts, cr, ci);
     const size_t n3 = G.n3();
-    // chi depends on Q only; media hold few distinct Q values, so remember the last ones
+    // the relaxation factor depends on Q only; media hold few distinct Q
+    // values, so remember the last ones
     float lq[2] = {-1.f, -1.f};
-    double lchi[2] = {0, 0};
-    auto chi = [&](int w, float q, double tau) {
-        if (q != lq[w]) { lq[w] = q; lchi[w] = 1.0 / (1.0 / std::sqrt(1.0 - cc * tau)).real(); }
-        return lchi[w];
+    double lrc[2] = {0, 0};
+    auto relax = [&](int w, float q, double tau) {
+        if (q != lq[w]) { lq[w] = q; lrc[w] = visco::relax_factor(cr, ci, tau); }
+        return lrc[w];
     };
     for (size_t q = 0; q < n3; ++q) {
         double tp = nm * zeta / (double)qp[q], tsv = nm * zeta / (double)qs[q];
         double rb2 = mu[q], ra2 = (double)lam[q] + 2.0 * mu[q];
-        double chi_mu = chi(0, qs[q], tsv);
-        double chi_lam = chi(1, qp[q], tp);
-        double m2 = rb2 / (chi_mu * chi_mu);
+        double m2 = rb2 * relax(0, qs[q], tsv);
         mu[q] = (float)m2;
-        lam[q] = (float)(ra2 / (chi_lam * chi_lam) - 2 * m2);
+        lam[q] = (float)(ra2 * relax(1, qp[q], tp) - 2 * m2);
         qp[q] = (float)tp;
         qs[q] = (float)tsv;
     }

@@ -1151,10 +1151,12 @@ __global__ void k_spread_col(const float* __restrict__ col, float* __restrict__ 
 // extrapolated linearly from the two outermost cells before the PML update
 // reads them (src/swpc_3d/m_absorb_p.f90:137-244 for S, 332-427 for V):
 // x sides for j = 1..ny, y sides for i = 1..nx, k = 1..nz; corners untouched.
-__global__ void k_pw_ghost(float* F, Geo g, int nf) {
+__host__ __device__ __forceinline__ long long pw_ghost_units(const Geo& g, int nf) {
+    return (2LL * g.ny * g.nz + 2LL * g.nx * g.nz) * nf;
+}
+__device__ __forceinline__ void pw_ghost_unit(float* F, const Geo& g, int nf, long long p) {
     const long long nxs = (long long)g.ny * g.nz, nys = (long long)g.nx * g.nz;
-    const long long n = (2 * nxs + 2 * nys) * nf;
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    {
         const int f = (int)(p % nf);
         long long q = p / nf;
         int side;
@@ -1171,6 +1173,11 @@ __global__ void k_pw_ghost(float* F, Geo g, int nf) {
         }
         F[goff(g, nf, f, gi, gj, k)] = 2 * F[goff(g, nf, f, i1, j1, k)] - F[goff(g, nf, f, i2, j2, k)];
     }
+}
+__global__ void k_pw_ghost(float* F, Geo g, int nf) {
+    const long long n = pw_ghost_units(g, nf);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+        pw_ghost_unit(F, g, nf, p);
 }
 
 // one field of a device group -> Fortran (nz, nx, ny) physical-grid double

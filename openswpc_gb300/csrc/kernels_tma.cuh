@@ -15,7 +15,7 @@
 
 namespace swpc {
 
-constexpr int TTY = 8;            // tile rows of the TMA kernels
+constexpr int TTY = 8;            // default tile rows of the TMA kernels (8 or 16 per kernel)
 constexpr int WAIT_LIMIT = 1 << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -43,6 +43,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
@@ -56,13 +59,15 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 // Tensor maps and scalars of the TMA kernels.  The maps must stay 64-byte
 // aligned and are read from the kernel parameter space (__grid_constant__).
 struct TArgs {
-    CUtensorMap tmV;    // V group, box (40, 3, TTY+4, 1)
-    CUtensorMap tmS;    // S group, box (32, 6, TTY, 1)
-    CUtensorMap tmM;    // M group fields lam..taus, box (36, 4, TTY+1, 1)
-    CUtensorMap tmR;    // memory variables, box (32, 18, TTY, 1)
-    CUtensorMap tmSh;   // S group with halo, box (40, 6, TTY+4, 1)
-    CUtensorMap tmRho;  // M group field rho, box (36, 1, TTY+1, 1)
-    CUtensorMap tmVc;   // V group centre, box (32, 3, TTY, 1)
+    // boxes for tile rows TY (the stress kernel's for the first four, the
+    // velocity kernel's for the last three)
+    CUtensorMap tmV;    // V group, box (40, 3, TY+4, 1)
+    CUtensorMap tmS;    // S group, box (32, 6, TY, 1)
+    CUtensorMap tmM;    // M group fields lam..taus, box (36, 4, TY+1, 1)
+    CUtensorMap tmR;    // memory variables, box (32, 18, TY, 1)
+    CUtensorMap tmSh;   // S group with halo, box (40, 6, TY+4, 1)
+    CUtensorMap tmRho;  // M group field rho, box (36, 1, TY+1, 1)
+    CUtensorMap tmVc;   // V group centre, box (32, 3, TY, 1)
     ZArgs z;
     int* err;           // error word (bounded wait ran out)
 };
@@ -75,12 +80,12 @@ struct alignas(128) Slot3 { T d[A][B][C]; };
 template <class T, int A, int B>
 struct alignas(128) Slot2 { T d[A][B]; };
 
-template <class RT>
+template <class RT, int TY = TTY>
 struct StressSmem {
-    Slot3<RT, TTY, 18, 32> R[2];
-    Slot3<float, TTY, 6, 32> S[2];
-    Slot3<float, TTY + 1, 4, 36> M[3];
-    Slot3<float, TTY + 4, 3, 40> V[6];
+    Slot3<RT, TY, 18, 32> R[2];
+    Slot3<float, TY, 6, 32> S[2];
+    Slot3<float, TY + 1, 4, 36> M[3];
+    Slot3<float, TY + 4, 3, 40> V[6];
     alignas(8) uint64_t barRS[2], barM[3], barV[6];
     int bad;
 };
@@ -98,17 +103,24 @@ struct StressSmem {
 constexpr int VRING = VEL_RING;
 constexpr int VMINB = VEL_MINB;
 static_assert(VRING >= 5, "the velocity S ring needs planes k-2 .. k+2 at start-up");
+template <int TY = TTY>
 struct VelSmem {
-    Slot3<float, TTY + 4, 6, 40> S[VRING];
-    Slot2<float, TTY + 1, 36> M[3];
-    Slot3<float, TTY, 3, 32> V[4];
+    Slot3<float, TY + 4, 6, 40> S[VRING];
+    Slot2<float, TY + 1, 36> M[3];
+    Slot3<float, TY, 3, 32> V[4];
     alignas(8) uint64_t barS[VRING], barM[3], barV[4];
     int bad;
 };
+// blocks per SM the tile kernels are built for: 8-row tiles two (stress) and
+// VMINB (velocity), 16-row tiles one (their rings take 181 and 125 KB)
+template <int TY> struct TileOcc { static constexpr int stress = 2, vel = VMINB; };
+template <> struct TileOcc<16> { static constexpr int stress = 1, vel = 1; };
 static_assert(sizeof(Slot3<float, TTY + 1, 4, 36>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot2<float, TTY + 1, 36>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot3<__half, TTY, 18, 32>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot3<float, TTY + 4, 6, 40>) % 128 == 0, "slot size");
+static_assert(sizeof(Slot3<float, 17, 4, 36>) % 128 == 0 && sizeof(Slot2<float, 17, 36>) % 128 == 0, "slot size");
+static_assert(sizeof(StressSmem<float, 16>) <= 227 * 1024 && sizeof(VelSmem<16>) <= 227 * 1024, "16-row rings fit");
 
 // Start-up check of a TMA destination (128-byte boundary) and of the
 // innermost box coordinate (a multiple of 16 bytes); a block that fails it
@@ -151,24 +163,26 @@ struct FillLog {
 // One 32 x TTY column tile and z chunk (bx, by, bz) of one simulation; `ta`
 // lives in kernel parameter space (single simulation) or in global memory
 // (batched launch).
-template <class RT>
-__device__ __forceinline__ void stress_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
+// Returns whether the block initialised its mbarriers (a caller that reuses
+// the shared memory for other work invalidates them first).
+template <class RT, int TY = TTY>
+__device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    StressSmem<RT>& sm = *reinterpret_cast<StressSmem<RT>*>(smraw);
+    StressSmem<RT, TY>& sm = *reinterpret_cast<StressSmem<RT, TY>*>(smraw);
     int& bad = sm.bad;
     const ZArgs& a = ta.z;
     const Coef cf = a.c;
     const Geo& g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TTY;
+    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TY;
     const int ix = xt + tx, jy = yt + ty;
     const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
     const int kz0 = bz * a.kchunk;
     const int kz1 = min(kz0 + a.kchunk, a.kz_end);
-    if (kz0 >= kz1) return;
+    if (kz0 >= kz1) return false;
 
-    constexpr uint32_t BR = sizeof(RT) * TTY * 18 * 32, BS = 4 * TTY * 6 * 32;
-    constexpr uint32_t BM = 4 * (TTY + 1) * 4 * 36, BV = 4 * (TTY + 4) * 3 * 40;
+    constexpr uint32_t BR = sizeof(RT) * TY * 18 * 32, BS = 4 * TY * 6 * 32;
+    constexpr uint32_t BM = 4 * (TY + 1) * 4 * 36, BV = 4 * (TY + 4) * 3 * 40;
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) mbar_init(&sm.barRS[s], 1);
         for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
@@ -185,7 +199,7 @@ __device__ __forceinline__ void stress_tma_tile(const TArgs& ta, const int bx, c
         if (!ok) { bad = 1; atomicExch(ta.err, 2); }
     }
     __syncthreads();
-    if (bad) return;
+    if (bad) return true;
 
     // producer (thread 0): next plane and ring position of every stream
     int nRS = kz0, nM = kz0, nV = kz0 - 2;
@@ -368,6 +382,7 @@ __device__ __forceinline__ void stress_tma_tile(const TArgs& ta, const int bx, c
         lM.drain(sm.barM, 3);
         lV.drain(sm.barV, 6);
     }
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -377,22 +392,23 @@ __device__ __forceinline__ void stress_tma_tile(const TArgs& ta, const int bx, c
 //   rho ring: 3 planes (k, k+1, k+2 in flight)
 //   V ring:   4 planes (k, k+1 .. k+3 in flight)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
+template <int TY = TTY>
+__device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    VelSmem& sm = *reinterpret_cast<VelSmem*>(smraw);
+    VelSmem<TY>& sm = *reinterpret_cast<VelSmem<TY>*>(smraw);
     int& bad = sm.bad;
     const ZArgs& a = ta.z;
     const Coef cf = a.c;
     const Geo& g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TTY;
+    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TY;
     const int ix = xt + tx, jy = yt + ty;
     const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
     const int kz0 = bz * a.kchunk_v;
     const int kz1 = min(kz0 + a.kchunk_v, a.kz_end);
-    if (kz0 >= kz1) return;
+    if (kz0 >= kz1) return false;
 
-    constexpr uint32_t BSH = 4 * (TTY + 4) * 6 * 40, BRHO = 4 * (TTY + 1) * 36, BVC = 4 * TTY * 3 * 32;
+    constexpr uint32_t BSH = 4 * (TY + 4) * 6 * 40, BRHO = 4 * (TY + 1) * 36, BVC = 4 * TY * 3 * 32;
     if (tid == 0) {
         for (int s = 0; s < VRING; ++s) mbar_init(&sm.barS[s], 1);
         for (int s = 0; s < 3; ++s) mbar_init(&sm.barM[s], 1);
@@ -409,7 +425,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
         if (!ok) { bad = 1; atomicExch(ta.err, 2); }
     }
     __syncthreads();
-    if (bad) return;
+    if (bad) return true;
 
     int nS = kz0 - 2, nM = kz0, nV = kz0;
     RingPos<VRING> pS{0, 0u};
@@ -562,6 +578,7 @@ __device__ __forceinline__ void vel_tma_tile(const TArgs& ta, const int bx, cons
         lM.drain(sm.barM, 3);
         lV.drain(sm.barV, 4);
     }
+    return true;
 }
 
 // Block order of the single-simulation stress launch (a 1-D grid): groups of
@@ -586,15 +603,16 @@ __device__ __forceinline__ void grouped_tile(int L, int tx, int ty, int nzc, int
     by = g * STRESS_YGROUP + r2 / tx;
     bx = r2 - (r2 / tx) * tx;
 }
-template <class RT>
-__global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma(const __grid_constant__ TArgs ta) {
+template <class RT, int TY = TTY>
+__global__ void __launch_bounds__(32 * TY, TileOcc<TY>::stress) k_stress_tma(const __grid_constant__ TArgs ta) {
     const ZArgs& a = ta.z;
     int bx, by, bz;
-    grouped_tile(blockIdx.x, (a.nxi + 31) / 32, (a.nyi + TTY - 1) / TTY, (a.kz_end + a.kchunk - 1) / a.kchunk, bx, by, bz);
-    stress_tma_tile<RT>(ta, bx, by, bz);
+    grouped_tile(blockIdx.x, (a.nxi + 31) / 32, (a.nyi + TY - 1) / TY, (a.kz_end + a.kchunk - 1) / a.kchunk, bx, by, bz);
+    stress_tma_tile<RT, TY>(ta, bx, by, bz);
 }
-__global__ void __launch_bounds__(32 * TTY, VMINB) k_vel_tma(const __grid_constant__ TArgs ta) {
-    vel_tma_tile(ta, blockIdx.x, blockIdx.y, blockIdx.z);
+template <int TY = TTY>
+__global__ void __launch_bounds__(32 * TY, TileOcc<TY>::vel) k_vel_tma(const __grid_constant__ TArgs ta) {
+    vel_tma_tile<TY>(ta, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // Self-test of the bounded wait: an mbarrier that expects one arrival which
@@ -631,16 +649,19 @@ __device__ __forceinline__ void tmaps_acquire(const TArgs& t) {
         tmap_acquire(&t.tmVc);
     }
 }
-template <class RT>
-__global__ void __launch_bounds__(32 * TTY, 2) k_stress_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
+template <class RT, int TY = TTY>
+__global__ void __launch_bounds__(32 * TY, TileOcc<TY>::stress) k_stress_tma_batch(const TArgs* __restrict__ all,
+                                                                                  const int4* __restrict__ blocks) {
     const int4 e = blocks[blockIdx.x];
     tmaps_acquire(all[e.x]);
-    stress_tma_tile<RT>(all[e.x], e.y, e.z, e.w);
+    stress_tma_tile<RT, TY>(all[e.x], e.y, e.z, e.w);
 }
-__global__ void __launch_bounds__(32 * TTY, VMINB) k_vel_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
+template <int TY = TTY>
+__global__ void __launch_bounds__(32 * TY, TileOcc<TY>::vel) k_vel_tma_batch(const TArgs* __restrict__ all,
+                                                                            const int4* __restrict__ blocks) {
     const int4 e = blocks[blockIdx.x];
     tmaps_acquire(all[e.x]);
-    vel_tma_tile(all[e.x], e.y, e.z, e.w);
+    vel_tma_tile<TY>(all[e.x], e.y, e.z, e.w);
 }
 
 }  // namespace swpc

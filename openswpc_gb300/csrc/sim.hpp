@@ -50,6 +50,7 @@ struct Sim {
     int kchunk = 1, kchunk_auto = 1;      // z-sweep depth of the stress kernels
     int kchunk_v = 1, kchunk_v_auto = 1;  // and of the velocity kernels
     int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
+    int ty_s = TTY, ty_v = TTY;  // tile rows of the stress and velocity TMA kernels (8 or 16)
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
     size_t smem_stress = 0, smem_vel = 0;
 
@@ -88,6 +89,10 @@ struct Sim {
     int upload_medium(const float* rho, const float* lam, const float* mu, const float* taup, const float* taus,
                       const int* kfs, const int* kob, const int* kfs_top, const int* kfs_bot, const int* kob_top,
                       const int* kob_bot, const double* ts, bool column);
+    int finish_medium(const double* ts);
+    int build_medium_rmed(const float* bg, const float* xi, int nxc, int nyc, int nzc, int kxi0, double vmin,
+                          double vmax, double rhomin, double fq_min, double fq_max, double fq_ref, int* maps6,
+                          double* ts);
     int set_sources(int n, const int* ijk, const double* mo, const double* mij, const double* fxyz, const double* prm,
                     int stftype, bool bf);
     int set_receivers(int n, const int* ijk, int ntdec_w, int flags);

@@ -11,7 +11,10 @@
 
 #include "../../include/swpc_gpu.h"
 #include "kernels.cuh"
+#include "medium.cuh"
+#include "persist.cuh"
 #include "sim.hpp"
+#include "visco.hpp"
 
 using namespace swpc;
 
@@ -216,9 +219,9 @@ int Sim::launch_step(bool timed) {
     ZArgs z;
     fill_zargs(z);
     targs.z = z;
-    const dim3 tblk(32, TTY);
-    const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + TTY - 1) / TTY, (p.nzi + kchunk - 1) / kchunk);
-    const dim3 tgrd_v(tgrd.x, tgrd.y, (p.nzi + kchunk_v - 1) / kchunk_v);
+    const dim3 tblk(32, ty_s), tblk_v(32, ty_v);
+    const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + ty_s - 1) / ty_s, (p.nzi + kchunk - 1) / kchunk);
+    const dim3 tgrd_v((p.nxi + 31) / 32, (p.nyi + ty_v - 1) / ty_v, (p.nzi + kchunk_v - 1) / kchunk_v);
     if (pw && p.pml) { k_pw_ghost<<<256, 256, 0, stream>>>(V, p.g, 3); ++launches; }
     if (two) {
         cudaEventRecord(ev_fork, stream);
@@ -233,9 +236,15 @@ int Sim::launch_step(bool timed) {
     ev0(0, stream);
     if (variant == 0) {
         const unsigned nlin = tgrd.x * tgrd.y * tgrd.z;  // 1-D grid, grouped block order
-        if (p.rbytes == 4) k_stress_tma<float><<<nlin, tblk, smem_stress, stream>>>(targs);
-        else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half><<<nlin, tblk, smem_stress, stream>>>(targs);
-        else k_stress_tma<__nv_bfloat16><<<nlin, tblk, smem_stress, stream>>>(targs);
+        if (ty_s == 16) {
+            if (p.rbytes == 4) k_stress_tma<float, 16><<<nlin, tblk, smem_stress, stream>>>(targs);
+            else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half, 16><<<nlin, tblk, smem_stress, stream>>>(targs);
+            else k_stress_tma<__nv_bfloat16, 16><<<nlin, tblk, smem_stress, stream>>>(targs);
+        } else {
+            if (p.rbytes == 4) k_stress_tma<float><<<nlin, tblk, smem_stress, stream>>>(targs);
+            else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half><<<nlin, tblk, smem_stress, stream>>>(targs);
+            else k_stress_tma<__nv_bfloat16><<<nlin, tblk, smem_stress, stream>>>(targs);
+        }
     } else {
         if (p.rbytes == 4) k_stress_interior<float><<<grd, blk, 0, stream>>>(z);
         else if (dims.store == SWPC_STORE_FP16) k_stress_interior<__half><<<grd, blk, 0, stream>>>(z);
@@ -261,8 +270,12 @@ int Sim::launch_step(bool timed) {
         if (two) cudaEventRecord(ev_join2, stream2);
     }
     ev0(1, stream);
-    if (variant == 0) k_vel_tma<<<tgrd_v, tblk, smem_vel, stream>>>(targs);
-    else k_vel_interior<<<grd_v, blk, 0, stream>>>(z);
+    if (variant == 0) {
+        if (ty_v == 16) k_vel_tma<16><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
+        else k_vel_tma<><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
+    } else {
+        k_vel_interior<<<grd_v, blk, 0, stream>>>(z);
+    }
     ++launches;
     ev1(1, stream);
     if (two) cudaStreamWaitEvent(stream, ev_join2, 0);
@@ -340,6 +353,8 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
+int tile_kernel_attributes();
+
 // 4-D map (x, field, y, z) over a row-interleaved group
 static int make_map(CUtensorMap* m, void* base, CUtensorMapDataType dt, int es, long long nx, int nf, long long ny,
                     long long nz, int bx, int bf, int by) {
@@ -363,35 +378,63 @@ int Sim::build_tensor_maps() {
     const Geo& g = p.g;
     const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     int rc;
-    if ((rc = make_map(&targs.tmV, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 40, 3, TTY + 4))) return rc;
-    if ((rc = make_map(&targs.tmS, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 32, 6, TTY))) return rc;
-    if ((rc = make_map(&targs.tmM, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 4, TTY + 1))) return rc;
-    if ((rc = make_map(&targs.tmSh, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 40, 6, TTY + 4))) return rc;
-    if ((rc = make_map(&targs.tmRho, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 1, TTY + 1))) return rc;
-    if ((rc = make_map(&targs.tmVc, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 32, 3, TTY))) return rc;
+    const int ts_ = ty_s, tv_ = ty_v;
+    if ((rc = make_map(&targs.tmV, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 40, 3, ts_ + 4))) return rc;
+    if ((rc = make_map(&targs.tmS, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 32, 6, ts_))) return rc;
+    if ((rc = make_map(&targs.tmM, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 4, ts_ + 1))) return rc;
+    if ((rc = make_map(&targs.tmSh, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 40, 6, tv_ + 4))) return rc;
+    if ((rc = make_map(&targs.tmRho, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 1, tv_ + 1))) return rc;
+    if ((rc = make_map(&targs.tmVc, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 32, 3, tv_))) return rc;
     const CUtensorMapDataType RTy = dims.store == SWPC_STORE_FP32 ? F
                                     : dims.store == SWPC_STORE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                                     : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-    if ((rc = make_map(&targs.tmR, R, RTy, p.rbytes, p.rpitch, 18, p.nyi, p.nzi, 32, 18, TTY))) return rc;
+    if ((rc = make_map(&targs.tmR, R, RTy, p.rbytes, p.rpitch, 18, p.nyi, p.nzi, 32, 18, ts_))) return rc;
     targs.err = d_err;
-    smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>);
-    smem_vel = sizeof(VelSmem);
-    CK(cudaFuncSetAttribute(k_stress_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(StressSmem<float>)));
-    CK(cudaFuncSetAttribute(k_stress_tma<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(StressSmem<__half>)));
-    CK(cudaFuncSetAttribute(k_stress_tma<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)sizeof(StressSmem<__nv_bfloat16>)));
-    CK(cudaFuncSetAttribute(k_vel_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(VelSmem)));
-    CK(cudaFuncSetAttribute(k_stress_tma_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)sizeof(StressSmem<float>)));
-    CK(cudaFuncSetAttribute(k_stress_tma_batch<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)sizeof(StressSmem<__half>)));
-    CK(cudaFuncSetAttribute(k_stress_tma_batch<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)sizeof(StressSmem<__nv_bfloat16>)));
-    CK(cudaFuncSetAttribute(k_vel_tma_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(VelSmem)));
-    // the velocity kernel is sized for VMINB blocks per SM: ask for the
-    // largest shared-memory carve-out
-    CK(cudaFuncSetAttribute(k_vel_tma, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared));
-    CK(cudaFuncSetAttribute(k_vel_tma_batch, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared));
+    if (ts_ == 16) smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float, 16>) : sizeof(StressSmem<__half, 16>);
+    else smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>);
+    smem_vel = tv_ == 16 ? sizeof(VelSmem<16>) : sizeof(VelSmem<>);
+    return tile_kernel_attributes();
+}
+
+// Dynamic shared memory of every instantiation of the TMA tile kernels (set
+// once per process: the attribute belongs to the kernel)
+int tile_kernel_attributes() {
+    static std::mutex mu;
+    static bool set_on[128] = {};
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return set_err(SWPC_E_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (set_on[dev]) return 0;
+    cudaError_t err = cudaSuccess;
+    {
+        auto set = [&err](const void* f, size_t bytes, bool carve) {
+            cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            // the velocity kernel is sized for several blocks per SM: ask for
+            // the largest shared-memory carve-out
+            if (e == cudaSuccess && carve)
+                e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+            if (e != cudaSuccess && err == cudaSuccess) err = e;
+        };
+        set((const void*)k_stress_tma<float>, sizeof(StressSmem<float>), false);
+        set((const void*)k_stress_tma<__half>, sizeof(StressSmem<__half>), false);
+        set((const void*)k_stress_tma<__nv_bfloat16>, sizeof(StressSmem<__nv_bfloat16>), false);
+        set((const void*)k_stress_tma<float, 16>, sizeof(StressSmem<float, 16>), false);
+        set((const void*)k_stress_tma<__half, 16>, sizeof(StressSmem<__half, 16>), false);
+        set((const void*)k_stress_tma<__nv_bfloat16, 16>, sizeof(StressSmem<__nv_bfloat16, 16>), false);
+        set((const void*)k_vel_tma<>, sizeof(VelSmem<>), true);
+        set((const void*)k_vel_tma<16>, sizeof(VelSmem<16>), true);
+        set((const void*)k_stress_tma_batch<float>, sizeof(StressSmem<float>), false);
+        set((const void*)k_stress_tma_batch<__half>, sizeof(StressSmem<__half>), false);
+        set((const void*)k_stress_tma_batch<__nv_bfloat16>, sizeof(StressSmem<__nv_bfloat16>), false);
+        set((const void*)k_stress_tma_batch<float, 16>, sizeof(StressSmem<float, 16>), false);
+        set((const void*)k_stress_tma_batch<__half, 16>, sizeof(StressSmem<__half, 16>), false);
+        set((const void*)k_stress_tma_batch<__nv_bfloat16, 16>, sizeof(StressSmem<__nv_bfloat16, 16>), false);
+        set((const void*)k_vel_tma_batch<>, sizeof(VelSmem<>), true);
+        set((const void*)k_vel_tma_batch<16>, sizeof(VelSmem<16>), true);
+    }
+    if (err != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(err));
+    set_on[dev] = true;
     return 0;
 }
 
@@ -478,6 +521,16 @@ int swpc_gpu_upload_medium_column(swpc_sim* sim, const float* rho, const float* 
     if (!s || !rho || !lam || !mu || !taup || !taus || !kfs || !kob || !kfs_top || !kfs_bot || !kob_top || !kob_bot || !ts)
         return set_err(SWPC_E_ARG, "null argument to swpc_gpu_upload_medium_column");
     return s->upload_medium(rho, lam, mu, taup, taus, kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, ts, true);
+}
+
+int swpc_gpu_build_medium_rmed(swpc_sim* sim, const float* bg, const float* xi, int nxc, int nyc, int nzc, int kxi0,
+                               double vmin, double vmax, double rhomin, double fq_min, double fq_max, double fq_ref,
+                               int* maps6, double* ts) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !bg || !xi || !ts || nxc <= 0 || nyc <= 0 || nzc <= 0)
+        return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_build_medium_rmed");
+    if (!(fq_min > 0 && fq_max > fq_min && fq_ref > 0)) return set_err(SWPC_E_ARG, "need 0 < fq_min < fq_max, fq_ref > 0");
+    return s->build_medium_rmed(bg, xi, nxc, nyc, nzc, kxi0, vmin, vmax, rhomin, fq_min, fq_max, fq_ref, maps6, ts);
 }
 
 int swpc_gpu_set_sources(swpc_sim* sim, int n, const int* ijk, const double* mo, const double* mij, const double* fxyz,
@@ -958,7 +1011,7 @@ int Sim::allocate() {
     // cannot fill the GPU by itself (measured: 128x128x64 0.134 vs 0.16 ms per
     // step; 1024x1024x512 27.9 serial vs 28.3 ms concurrent)
     {
-        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + TTY - 1) / TTY) * ((p.nzi + kfill - 1) / kfill);
+        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + ty_s - 1) / ty_s) * ((p.nzi + kfill - 1) / kfill);
         concurrent = dims.reserved[1] == 2 || (dims.reserved[1] == 0 && tiles < 4LL * nsm);
     }
     if ((rc = build_tensor_maps())) return rc;
@@ -1139,7 +1192,77 @@ int Sim::upload_medium(const float* rho, const float* lam, const float* mu, cons
     CK(cudaMemcpyAsync(band, bnd.data(), bnd.size() * 4, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_kob, kb.data(), kb.size() * 4, cudaMemcpyHostToDevice, stream));
     CK(cudaMemcpyAsync(d_kfs, kf.data(), kf.size() * 4, cudaMemcpyHostToDevice, stream));
+    // the host arrays must stay readable until the copies are done
+    CK(cudaStreamSynchronize(stream));
+    return finish_medium(ts);
+}
 
+// The medium of a layered model with a random perturbation, built on the
+// device from the background column and the periodic field (medium.cuh):
+// cells, absorber band, tau-method and relaxation in FP64, surface maps and
+// the interior band table.  maps6 (optional) receives the six surface maps
+// of the halo plane (kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot, each
+// (nx+6) x (ny+6), i fastest); ts the relaxation times.
+int Sim::build_medium_rmed(const float* bg, const float* xi, int nxc, int nyc, int nzc, int kxi0, double vmin,
+                           double vmax, double rhomin, double fq_min, double fq_max, double fq_ref, int* maps6,
+                           double* ts) {
+    const Geo& g = p.g;
+    visco::relaxation_times(NM, fq_min, fq_max, ts);
+    const double zeta = visco::constq_zeta(NM, fq_min, fq_max, ts);
+    RmedArgs a{};
+    a.g = g; a.M = M;
+    a.nxc = nxc; a.nyc = nyc; a.nzc = nzc; a.kxi0 = kxi0; a.na = dims.na;
+    a.vmin = (float)vmin; a.vmax = (float)vmax; a.rhomin = (float)rhomin;
+    // Q depends on depth only: the tau-method ratios and the relaxation
+    // factors of every k, in the FP64 sequence of the host set-up
+    double cr, ci;
+    visco::zener_c(NM, fq_ref, ts, cr, ci);
+    const int nk = g.nz + 6;
+    std::vector<double> kq(4 * (size_t)nk);
+    for (int k = 0; k < nk; ++k) {
+        const double tp = NM * zeta / (double)bg[3 * nk + k], tsv = NM * zeta / (double)bg[4 * nk + k];
+        kq[k] = tp;
+        kq[nk + k] = tsv;
+        kq[2 * nk + k] = visco::relax_factor(cr, ci, tsv);
+        kq[3 * nk + k] = visco::relax_factor(cr, ci, tp);
+    }
+    const size_t nbg = 5 * (size_t)nk, nfield = (size_t)nxc * nyc * nzc;
+    const size_t n2 = (size_t)(g.nx + 6) * (g.ny + 6);
+    const size_t bytes = kq.size() * 8 + (nbg + nfield) * 4 + 6 * n2 * 4;
+    char* stage = nullptr;
+    CK(cudaMallocAsync((void**)&stage, bytes, stream));
+    double* dkq = reinterpret_cast<double*>(stage);
+    float* dbg = reinterpret_cast<float*>(dkq + kq.size());
+    float* dxi = dbg + nbg;
+    int* dm = reinterpret_cast<int*>(dxi + nfield);
+    CK(cudaMemcpyAsync(dkq, kq.data(), kq.size() * 8, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(dbg, bg, nbg * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(dxi, xi, nfield * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(dm, 0, 6 * n2 * 4, stream));
+    a.bg = dbg;
+    a.xi = dxi;
+    a.kq = dkq;
+    k_rmed_medium<<<4096, 256, 0, stream>>>(a);
+    int* kfs = dm; int* kob = dm + n2; int* kft = dm + 2 * n2; int* kfb = dm + 3 * n2; int* kot = dm + 4 * n2;
+    int* kobb = dm + 5 * n2;
+    const int ncol = (g.nx + 3) * (g.ny + 3);
+    k_rmed_surface<<<(ncol + 255) / 256, 256, 0, stream>>>(M, g, kfs, kob);
+    k_rmed_ranges<<<(g.nx * g.ny + 255) / 256, 256, 0, stream>>>(kfs, kob, g, kft, kfb, kot, kobb);
+    const int nt = std::max(p.nxi * p.nyi, g.nx * g.ny);
+    k_rmed_tables<<<(nt + 255) / 256, 256, 0, stream>>>(kfs, kob, kft, kfb, kot, kobb, g, p.x0, p.y0, p.nxi, p.nyi,
+                                                      band, d_kob, d_kfs);
+    launches += 4;
+    CK(cudaGetLastError());
+    if (maps6) CK(cudaMemcpyAsync(maps6, dm, 6 * n2 * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaFreeAsync(stage, stream));
+    CK(cudaStreamSynchronize(stream));
+    return finish_medium(ts);
+}
+
+// Coefficients, absorber profiles and the divergence check once the medium
+// and the surface maps are on the device.
+int Sim::finish_medium(const double* ts) {
+    const Geo& g = p.g;
     // FD and Zener coefficients in FP64 (m_kernel.f90:43-67)
     const double dt = dims.dt, dx = dims.dx, dy = dims.dy, dz = dims.dz;
     coef.e4x0 = (float)(18.0 / 16.0 / dx); coef.e4x1 = (float)(2.0 / 48.0 / dx);
@@ -1430,6 +1553,14 @@ struct Batch {
     bool any_vmax = false, any_snap = false, any_bf = false, any_mt = false;
     size_t smem_stress = 0, smem_vel = 0;
     long long launches = 0, launches_per_graph = 0;
+    // persistent fused form: the work queue of one time step of every
+    // member, the per-member finished counters and the launch shape
+    bool persistent = false;
+    int ty_s = TTY, ty_v = TTY;  // tile rows shared by every member
+    PersistArgs pargs{};
+    int n_items = 0, persist_grid = 0;
+    size_t smem_persist = 0;
+    int* d_ctr = nullptr;  // [0] head, [1] error word, [2..] per-member finished counters
     ~Batch() {
         if (stream) cudaStreamSynchronize(stream);
         if (graph) cudaGraphExecDestroy(graph);
@@ -1446,6 +1577,95 @@ struct Batch {
         allocs.push_back(q);
         if (!v.empty()) CK(cudaMemcpy(q, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
         *dst = (T*)q;
+        return 0;
+    }
+    // The work queue of the persistent form (persist.cuh): phase by phase,
+    // every member's items of that phase, each with the number of the
+    // member's items in earlier phases that must be finished first.
+    int build_queue(const std::vector<int4>& tb, const std::vector<int4>& tbv, const std::vector<PArgs>* pa) {
+        const int n = (int)sims.size();
+        const int T = PERSIST_THREADS;
+        auto chunks = [T](long long units) { return (int)((units + T - 1) / T); };
+        std::vector<int4> items;
+        std::vector<int> need;
+        std::vector<int> cnt(n, 0);
+        // tiles of each member, in the order of the phase launches' tables
+        std::vector<std::vector<int4>> st(n), vt(n);
+        for (const int4& e : tb) st[e.x].push_back(e);
+        for (const int4& e : tbv) vt[e.x].push_back(e);
+        auto item = [](int type, int m, int y, int z, int w) { return make_int4(type | (m << 4), y, z, w); };
+        for (int phase = 0; phase < 8; ++phase) {
+            for (int m = 0; m < n; ++m) {
+                Sim* s = sims[m];
+                const size_t first = items.size();
+                const bool pw = s->pw && s->p.pml;
+                switch (phase) {
+                case 0: {  // taps, Green's-function taps, snapshot pixels
+                    long long u = s->tap_args.n + s->green_args.n;
+                    for (int q = 0; q < s->snap_args.n; ++q) u += (long long)s->snap_args.pl[q].n1 * s->snap_args.pl[q].n2;
+                    for (int c = 0; c < chunks(u); ++c) items.push_back(item(IT_PRE, m, c, 0, 0));
+                    break;
+                }
+                case 1:
+                    if (pw) for (int c = 0; c < chunks(pw_ghost_units(s->p.g, 3)); ++c) items.push_back(item(IT_PW_V, m, c, 0, 0));
+                    break;
+                case 2:
+                    if (s->p.pml)
+                        for (int c = 0; c < PML_NCLASS; ++c)
+                            for (int k = 0; k < (pa[c][m].nblocks + PML_ITEM_BLOCKS - 1) / PML_ITEM_BLOCKS; ++k)
+                                items.push_back(item(IT_PML_S, m, c, k, 0));
+                    for (const int4& e : st[m]) items.push_back(item(IT_STRESS, m, e.y, e.z, e.w));
+                    break;
+                case 3:
+                    if (s->src_args.n > 0 && !s->bf_mode)
+                        for (int c = 0; c < chunks(s->src_args.n); ++c) items.push_back(item(IT_SRC_S, m, c, 0, 0));
+                    break;
+                case 4:
+                    if (pw) for (int c = 0; c < chunks(pw_ghost_units(s->p.g, 6)); ++c) items.push_back(item(IT_PW_S, m, c, 0, 0));
+                    break;
+                case 5:
+                    if (s->p.pml)
+                        for (int c = 0; c < PML_NCLASS; ++c)
+                            for (int k = 0; k < (pa[c][m].nblocks + PML_ITEM_BLOCKS - 1) / PML_ITEM_BLOCKS; ++k)
+                                items.push_back(item(IT_PML_V, m, c, k, 0));
+                    for (const int4& e : vt[m]) items.push_back(item(IT_VEL, m, e.y, e.z, e.w));
+                    break;
+                case 6:
+                    if (s->src_args.n > 0 && s->bf_mode)
+                        for (int c = 0; c < chunks(s->src_args.n); ++c) items.push_back(item(IT_SRC_V, m, c, 0, 0));
+                    break;
+                default:
+                    items.push_back(item(IT_ADV, m, 0, 0, 0));
+                    break;
+                }
+                need.insert(need.end(), items.size() - first, cnt[m]);
+                cnt[m] += (int)(items.size() - first);
+            }
+        }
+        int rc;
+        int4* d_items = nullptr;
+        int* d_need = nullptr;
+        if ((rc = upload(&d_items, items)) || (rc = upload(&d_need, need))) return rc;
+        std::vector<int> zero(2 + n, 0);
+        if ((rc = upload(&d_ctr, zero))) return rc;
+        n_items = (int)items.size();
+        PersistArgs& P = pargs;
+        P.items = d_items; P.need = d_need; P.n_items = n_items;
+        P.head = d_ctr; P.err = d_ctr + 1; P.done = d_ctr + 2;
+        P.targs = d_targs;
+        for (int c = 0; c < PML_NCLASS; ++c) P.pargs[c] = d_pargs[c];
+        P.src = d_src; P.tap = d_tap; P.snap = d_snap; P.green = d_green; P.its = d_its;
+        // one block of the 8-row tile kernels' shape holds either tile's rings
+        smem_persist = std::max(rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>), sizeof(VelSmem<>));
+        int dev = 0, nsm = 0, occ = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        const void* fn = rbytes == 4 ? (const void*)k_batch_persistent<float>
+                         : store == SWPC_STORE_FP16 ? (const void*)k_batch_persistent<__half>
+                                                    : (const void*)k_batch_persistent<__nv_bfloat16>;
+        CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_persist));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, PERSIST_THREADS, smem_persist));
+        persist_grid = std::max(1, std::min(n_items, nsm * std::max(1, occ)));
         return 0;
     }
     bool any_pml() const {
@@ -1468,13 +1688,29 @@ struct Batch {
             ++launches;
         }
     }
+    int launch_persistent() {
+        const int n = (int)sims.size();
+        if (any_vmax) { k_vmax_batch<<<dim3(64, n), 256, 0, stream>>>(d_vmax); ++launches; }
+        // head and finished counters back to zero, the error word kept
+        CK(cudaMemsetAsync(d_ctr, 0, sizeof(int), stream));
+        CK(cudaMemsetAsync(d_ctr + 2, 0, sizeof(int) * (size_t)n, stream));
+        const dim3 tblk(32, TTY);  // the persistent form runs 8-row tiles only
+        if (rbytes == 4) k_batch_persistent<float><<<persist_grid, tblk, smem_persist, stream>>>(pargs);
+        else if (store == SWPC_STORE_FP16) k_batch_persistent<__half><<<persist_grid, tblk, smem_persist, stream>>>(pargs);
+        else k_batch_persistent<__nv_bfloat16><<<persist_grid, tblk, smem_persist, stream>>>(pargs);
+        ++launches;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+        return 0;
+    }
     int launch_step() {
+        if (persistent) return launch_persistent();
         const int n = (int)sims.size();
         if (any_vmax) { k_vmax_batch<<<dim3(64, n), 256, 0, stream>>>(d_vmax); ++launches; }
         if (max_nst) { k_taps_batch<<<dim3((max_nst + 127) / 128, n), 128, 0, stream>>>(d_tap); ++launches; }
         if (max_green) { k_green_batch<<<dim3((max_green + 127) / 128, n), 128, 0, stream>>>(d_green); ++launches; }
         if (any_snap) { k_snap_batch<<<dim3((max_pix + 127) / 128, max_planes, n), 128, 0, stream>>>(d_snap); ++launches; }
-        const dim3 tblk(32, TTY);
+        const dim3 tblk(32, ty_s), tblk_v(32, ty_v);
         for (Sim* m : pw_members) { k_pw_ghost<<<256, 256, 0, stream>>>(m->V, m->p.g, 3); ++launches; }
         const bool pml = any_pml();
         if (pml) {
@@ -1483,9 +1719,16 @@ struct Batch {
             launch_pml(true);
             cudaEventRecord(ev[1], stream2);
         }
-        if (rbytes == 4) k_stress_tma_batch<float><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
-        else if (store == SWPC_STORE_FP16) k_stress_tma_batch<__half><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
-        else k_stress_tma_batch<__nv_bfloat16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+        if (ty_s == 16) {
+            if (rbytes == 4) k_stress_tma_batch<float, 16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+            else if (store == SWPC_STORE_FP16)
+                k_stress_tma_batch<__half, 16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+            else k_stress_tma_batch<__nv_bfloat16, 16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+        } else {
+            if (rbytes == 4) k_stress_tma_batch<float><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+            else if (store == SWPC_STORE_FP16) k_stress_tma_batch<__half><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+            else k_stress_tma_batch<__nv_bfloat16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
+        }
         ++launches;
         if (pml) cudaStreamWaitEvent(stream, ev[1], 0);
         if (any_mt) { k_stressglut_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
@@ -1496,7 +1739,9 @@ struct Batch {
             launch_pml(false);
             cudaEventRecord(ev[3], stream2);
         }
-        k_vel_tma_batch<<<n_tblocks_v, tblk, smem_vel, stream>>>(d_targs, d_tblocks_v); ++launches;
+        if (ty_v == 16) k_vel_tma_batch<16><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
+        else k_vel_tma_batch<><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
+        ++launches;
         if (pml) cudaStreamWaitEvent(stream, ev[3], 0);
         if (any_bf) { k_bodyforce_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
         k_advance_batch<<<(n + 127) / 128, 128, 0, stream>>>(d_its, n); ++launches;
@@ -1521,6 +1766,30 @@ int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel) {
 
 int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk) { return swpc_gpu_set_zchunks(sim, kchunk, kchunk); }
 
+int swpc_gpu_set_tiles(swpc_sim* sim, int rows_stress, int rows_vel) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    if (rows_stress == 0) rows_stress = TTY;
+    if (rows_vel == 0) rows_vel = TTY;
+    if ((rows_stress != 8 && rows_stress != 16) || (rows_vel != 8 && rows_vel != 16))
+        return set_err(SWPC_E_ARG, "tile rows must be 8 or 16 (0: the default 8)");
+    CK(cudaStreamSynchronize(s->stream));
+    s->ty_s = rows_stress;
+    s->ty_v = rows_vel;
+    int rc = s->build_tensor_maps();
+    if (rc) return rc;
+    if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+    return 0;
+}
+
+int swpc_gpu_get_tiles(swpc_sim* sim, int* rows_stress, int* rows_vel) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s || !rows_stress || !rows_vel) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_get_tiles");
+    *rows_stress = s->ty_s;
+    *rows_vel = s->ty_v;
+    return 0;
+}
+
 int swpc_gpu_get_zchunks(swpc_sim* sim, int* kstress, int* kvel) {
     Sim* s = reinterpret_cast<Sim*>(sim);
     if (!s || !kstress || !kvel) return set_err(SWPC_E_ARG, "bad arguments to swpc_gpu_get_zchunks");
@@ -1544,6 +1813,10 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         if (!s || !s->medium_ready) return fail(set_err(SWPC_E_STATE, "every member must have its medium uploaded"));
         if (s->variant != 0) return fail(set_err(SWPC_E_ARG, "batched members must use the TMA interior kernels"));
         if (q && s->dims.store != b->store) return fail(set_err(SWPC_E_ARG, "batched members must share one storage precision"));
+        if (q && (s->ty_s != b->ty_s || s->ty_v != b->ty_v))
+            return fail(set_err(SWPC_E_ARG, "batched members must share their tile shapes"));
+        b->ty_s = s->ty_s;
+        b->ty_v = s->ty_v;
         for (int r = 0; r < q; ++r)
             if (b->sims[r] == s) return fail(set_err(SWPC_E_ARG, "a simulation appears twice in the batch"));
         b->store = s->dims.store;
@@ -1585,15 +1858,15 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         if (s->pw && s->p.pml) b->pw_members.push_back(s);
         vm[q] = s->vmax_args;
         its[q] = s->d_it;
-        const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + TTY - 1) / TTY, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
-        const int gzv = (s->p.nzi + s->kchunk_v - 1) / s->kchunk_v;
+        const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + s->ty_s - 1) / s->ty_s, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
+        const int gyv = (s->p.nyi + s->ty_v - 1) / s->ty_v, gzv = (s->p.nzi + s->kchunk_v - 1) / s->kchunk_v;
         // stress tiles in the grouped order of the single-simulation launch
         for (int y0 = 0; y0 < gy; y0 += STRESS_YGROUP)
             for (int bz = 0; bz < gz; ++bz)
                 for (int by = y0; by < std::min(gy, y0 + STRESS_YGROUP); ++by)
                     for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
         for (int bz = 0; bz < gzv; ++bz)
-            for (int by = 0; by < gy; ++by)
+            for (int by = 0; by < gyv; ++by)
                 for (int bx = 0; bx < gx; ++bx) tbv.push_back(make_int4(q, bx, by, bz));
         b->max_nst = std::max(b->max_nst, s->tap_args.n);
         b->max_src = std::max(b->max_src, s->src_args.n);
@@ -1618,6 +1891,7 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     for (int c = 0; c < PML_NCLASS; ++c) b->n_pblocks[c] = (int)pb[c].size();
     b->smem_stress = b->sims[0]->smem_stress;
     b->smem_vel = b->sims[0]->smem_vel;
+    if ((rc = b->build_queue(tb, tbv, pa))) return fail(rc);
     *out = reinterpret_cast<swpc_batch*>(b);
     return 0;
 }
@@ -1662,11 +1936,35 @@ int swpc_batch_sync(swpc_batch* batch) {
     Batch* b = reinterpret_cast<Batch*>(batch);
     if (!b) return set_err(SWPC_E_ARG, "null batch");
     CK(cudaStreamSynchronize(b->stream));
+    if (b->d_ctr) {
+        int e = 0;
+        CK(cudaMemcpy(&e, b->d_ctr + 1, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) return set_err(SWPC_E_TIMEOUT, "a bounded wait of the persistent batch launch ran out");
+    }
     for (Sim* s : b->sims) {
         int rc = s->check_divergence();
         if (rc) return rc;
     }
     return 0;
+}
+
+int swpc_batch_set_persistent(swpc_batch* batch, int on) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    if (!b) return set_err(SWPC_E_ARG, "null batch");
+    if (on && (b->ty_s != TTY || b->ty_v != TTY))
+        return set_err(SWPC_E_ARG, "the persistent batch form runs 8-row tiles; the members use other tile shapes");
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->persistent != (on != 0) && b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->persistent = on != 0;
+    return 0;
+}
+
+int swpc_batch_item_count(swpc_batch* batch) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    return b ? b->n_items : set_err(SWPC_E_ARG, "null batch");
 }
 
 void* swpc_batch_stream(swpc_batch* batch) { return batch ? (void*)reinterpret_cast<Batch*>(batch)->stream : nullptr; }

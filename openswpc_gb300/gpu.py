@@ -60,6 +60,8 @@ EXPORTS = [
     "swpc_serve_submit", "swpc_serve_state", "swpc_serve_wait", "swpc_serve_result", "swpc_serve_error",
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
     "swpc_gpu_profile_read_pml", "swpc_host_banner", "swpc_host_ntdec_r",
+    "swpc_batch_set_persistent", "swpc_batch_item_count", "swpc_gpu_build_medium_rmed",
+    "swpc_gpu_set_tiles", "swpc_gpu_get_tiles",
 ]
 
 
@@ -122,10 +124,14 @@ def lib(build=True):
     L.swpc_gpu_set_zchunk.argtypes = [vp, i]
     L.swpc_gpu_get_zchunk.argtypes = [vp]
     L.swpc_gpu_set_zchunks.argtypes = [vp, i, i]
+    L.swpc_gpu_set_tiles.argtypes = [vp, i, i]
+    L.swpc_gpu_get_tiles.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.swpc_gpu_get_zchunks.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.swpc_batch_create.argtypes = [ctypes.c_void_p, i, ctypes.POINTER(vp)]
     L.swpc_batch_run.argtypes = [vp, i]
     L.swpc_batch_sync.argtypes = [vp]
+    L.swpc_batch_set_persistent.argtypes = [vp, i]
+    L.swpc_batch_item_count.argtypes = [vp]
     L.swpc_batch_stream.argtypes = [vp]
     L.swpc_batch_stream.restype = vp
     L.swpc_batch_launch_count.argtypes = [vp]
@@ -141,6 +147,7 @@ def lib(build=True):
     L.swpc_gpu_set_field.argtypes = [vp, i, fp]
     L.swpc_gpu_set_plane_wave.argtypes = [vp, i]
     L.swpc_gpu_upload_medium_column.argtypes = [vp] + [fp] * 5 + [ip] * 6 + [dp]
+    L.swpc_gpu_build_medium_rmed.argtypes = [vp, fp, fp, i, i, i, i, d, d, d, d, d, d, ip, dp]
     L.swpc_host_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
     L.swpc_host_request_bytes.argtypes = [vp]
     L.swpc_host_request_bytes.restype = ctypes.c_longlong
@@ -254,6 +261,26 @@ class Simulation:
         m = [np.ascontiguousarray(a, np.int32) for a in (kfs, kob, kfs_top, kfs_bot, kob_top, kob_bot)]
         t = np.ascontiguousarray(ts, np.float64)
         _ck(lib().swpc_gpu_upload_medium(self._h, *[_ptr(a) for a in f], *[_ptr(a) for a in m], _ptr(t)))
+
+    def build_medium_rmed(self, bg, xi, kxi0, vmin=0.0, vmax=float("inf"), rhomin=1.0, fq_min=0.05, fq_max=5.0,
+                          fq_ref=1.0):
+        """Medium of a layered model with a periodic random perturbation,
+        built on the device (swpc_gpu_build_medium_rmed): bg (5, nz+6)
+        background column, xi (nzc, nyc, nxc) field.  Returns the six
+        surface maps ((ny+6, nx+6) int32 each: kfs, kob, kfs_top, kfs_bot,
+        kob_top, kob_bot) and the relaxation times."""
+        d = self.dims
+        bg = np.ascontiguousarray(bg, np.float32)
+        xi = np.ascontiguousarray(xi, np.float32)
+        if d is None or bg.shape != (5, d.nz + 6) or xi.ndim != 3:
+            raise SwpcError(-1, "build_medium_rmed(): bg must be (5, nz+6) and xi 3-D")
+        maps = np.zeros((6, d.ny + 6, d.nx + 6), np.int32)
+        ts = np.zeros(3, np.float64)
+        nzc, nyc, nxc = xi.shape
+        _ck(lib().swpc_gpu_build_medium_rmed(self._h, bg.ctypes.data, xi.ctypes.data, nxc, nyc, nzc, int(kxi0),
+                                             float(vmin), float(vmax), float(rhomin), float(fq_min), float(fq_max),
+                                             float(fq_ref), maps.ctypes.data, ts.ctypes.data))
+        return list(maps), ts
 
     def set_sources(self, ijk, prm, mo=None, mij=None, fxyz=None, stftype="kupper", bf_mode=False):
         ijk = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
@@ -396,6 +423,15 @@ class Simulation:
         """z-sweep depths of the stress and velocity kernels (0: automatic)."""
         _ck(lib().swpc_gpu_set_zchunks(self._h, int(kstress), int(kvel)))
 
+    def set_tiles(self, rows_stress, rows_vel):
+        """Tile rows (8 or 16; 0 = 8) of the interior stress and velocity kernels."""
+        _ck(lib().swpc_gpu_set_tiles(self._h, int(rows_stress), int(rows_vel)))
+
+    def tiles(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _ck(lib().swpc_gpu_get_tiles(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def zchunks(self):
         ks, kv = ctypes.c_int(), ctypes.c_int()
         _ck(lib().swpc_gpu_get_zchunks(self._h, ctypes.byref(ks), ctypes.byref(kv)))
@@ -444,11 +480,21 @@ class Batch:
     """Several simulations advanced together by fused launches
     (swpc_batch_*).  The members stay owned by the caller."""
 
-    def __init__(self, sims):
+    def __init__(self, sims, persistent=None):
         self.sims = list(sims)
         arr = (ctypes.c_void_p * len(self.sims))(*[s.handle.value for s in self.sims])
         self._h = ctypes.c_void_p()
         _ck(lib().swpc_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(self.sims), ctypes.byref(self._h)))
+        if persistent is not None:
+            self.set_persistent(persistent)
+
+    def set_persistent(self, on=True):
+        """One persistent fused launch per step (True) or one launch per
+        phase of the step (False); the results are the same."""
+        _ck(lib().swpc_batch_set_persistent(self._h, int(bool(on))))
+
+    def item_count(self):
+        return int(lib().swpc_batch_item_count(self._h))
 
     def run(self, nsteps):
         _ck(lib().swpc_batch_run(self._h, int(nsteps)))

@@ -33,10 +33,16 @@ def _alone(inf):
 
 
 @pytest.mark.gpu
-def test_batch_equals_members_alone(infs):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_batch_equals_members_alone(infs, persistent):
+    """Both forms of the batch -- one persistent fused launch per step over a
+    work queue, and one launch per phase -- give each member's traces bit
+    for bit as the member run alone."""
     alone = [_alone(f) for f in infs]
     sims = [gpu.Simulation.from_inf(f) for f in infs]
-    b = gpu.Batch(sims)
+    b = gpu.Batch(sims, persistent=persistent)
+    if persistent:
+        assert b.item_count() > 3 * len(sims)
     b.run(NT)
     b.sync()
     for s, w in zip(sims, alone):
@@ -68,6 +74,8 @@ def test_reset_and_autotune_leave_results_unchanged(infs, tmp_path):
     sims = [gpu.Simulation.from_inf(f) for f in infs]
     rec = autotune.tune(sims, cache=str(tmp_path / "tune.json"), steps=3, candidates=(8, 0))
     assert rec["zchunk"] in (8, 0) and rec["zchunk_vel"] in (8, 0)
+    assert all(r in (8, 16) for r in rec["tiles"]) and len(rec["ms_per_step"]) == 4
+    assert sims[0].tiles() == tuple(rec["tiles"])
     b = gpu.Batch(sims)
     b.run(NT)
     b.sync()
@@ -79,3 +87,46 @@ def test_reset_and_autotune_leave_results_unchanged(infs, tmp_path):
     if rec["zchunk"] and rec["zchunk_vel"]:
         assert sims[0].zchunks() == (rec["zchunk"], rec["zchunk_vel"])
     b.close()
+
+
+@pytest.mark.gpu
+def test_persistent_batch_in_pieces_and_graph(infs):
+    """The persistent form replayed through its graph (8 steps per replay)
+    and stepped in odd pieces, members continuing from their own steps, gives
+    the traces of the members alone."""
+    alone = [_alone(f) for f in infs]
+    sims = [gpu.Simulation.from_inf(f) for f in infs]
+    sims[0].run(1, 5)  # the first member starts ahead
+    b = gpu.Batch(sims, persistent=True)
+    b.run(3)
+    b.run(NT - 13)  # members at steps NT - 5 and NT - 10
+    b.sync()
+    b.close()
+    sims[0].run(NT - 4, NT)
+    sims[1].run(NT - 9, NT)
+    sims[2].run(NT - 9, NT)
+    for s, w in zip(sims, alone):
+        s.sync()
+        assert np.array_equal(s.waveforms(), w)
+        s.close()
+
+
+@pytest.mark.gpu
+def test_batch_with_16_row_tiles_equals_alone(infs):
+    """Members with 16-row stress and velocity tiles, advanced by the phase
+    launches, give the traces of the members alone (8-row tiles); the
+    persistent form refuses other than 8-row tiles."""
+    alone = [_alone(f) for f in infs]
+    sims = [gpu.Simulation.from_inf(f) for f in infs]
+    for s in sims:
+        s.set_tiles(16, 16)
+    b = gpu.Batch(sims)
+    with pytest.raises(gpu.SwpcError):
+        b.set_persistent(True)
+    b.run(NT)
+    b.sync()
+    for s, w in zip(sims, alone):
+        assert np.array_equal(s.waveforms(), w)
+    b.close()
+    for s in sims:
+        s.close()
