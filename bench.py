@@ -188,14 +188,15 @@ def source_and_stations(w, kfs, zbeg, seed):
     return src, mij, sta
 
 
-def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None, seed=20261203):
+def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None, seed=20261203, pml_points=0):
     """A simulation of the workload: medium (built on the device or uploaded,
     see make_medium), the moment-tensor source, the receivers and the xy
     velocity snapshot."""
     from openswpc_gb300 import gpu
     dims = gpu.make_dims(w["nx"], w["ny"], w["nz"], nt, w["dx"], w["dx"], w["dx"], w["dt"], na=20, store=store,
                          xbeg=-w["nx"] * w["dx"] / 2, ybeg=-w["ny"] * w["dx"] / 2, zbeg=med["zbeg"], fcut=1.0,
-                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant, concurrent=concurrent)
+                         M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant, concurrent=concurrent,
+                         pml_points=pml_points)
     sim = gpu.Simulation(dims)
     if med["where"] == "device":
         maps, _ = sim.build_medium_rmed(med["bg"], med["xi"], med["kxi0"], fq_min=0.05, fq_max=5.0, fq_ref=1.0)
@@ -445,7 +446,12 @@ def run_gpu(args, w):
     seed = 20261203 + 7 * rank
     t_setup = time.time()
     med = make_medium(w, seed, args.medium)
-    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant, concurrent=args.pml_overlap, seed=seed)
+    sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant, concurrent=args.pml_overlap, seed=seed,
+                    pml_points=args.pml_points)
+    if args.tiles:
+        sim.set_tiles(*[int(v) for v in args.tiles.split(",")])
+    if args.zchunks:
+        sim.set_zchunks(*[int(v) for v in args.zchunks.split(",")])
     stream = torch.cuda.ExternalStream(sim.stream())
     t_setup = time.time() - t_setup
 
@@ -480,6 +486,7 @@ def run_gpu(args, w):
     it += args.steps
     kms, kn = sim.profile_read()
     pml = pml_class_report(sim, peak)
+    sim_tiles, sim_z = sim.tiles(), sim.zchunks()
     sim.profile(False)
     sim.sync()
     ms_max = reduce_max(ms, world)
@@ -527,7 +534,11 @@ def run_gpu(args, w):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant, concurrent=args.pml_overlap,
-                         seed=seed)
+                         seed=seed, pml_points=args.pml_points)
+        if args.tiles:
+            sim2.set_tiles(*[int(v) for v in args.tiles.split(",")])
+        if args.zchunks:
+            sim2.set_zchunks(*[int(v) for v in args.zchunks.split(",")])
         sim2.run(1, args.steps)
         wav = sim2.waveforms()
         sim2.close()
@@ -558,6 +569,7 @@ def run_gpu(args, w):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": arm_config(w, args, world),
+            "kernel_shape": {"tiles": list(sim_tiles), "zchunks": list(sim_z), "pml_points": args.pml_points or 1},
             "timed_window": "it=%d..%d (graph replay; snapshot frame at it=%s)"
                             % (it - 2 * args.steps, it - args.steps - 1, ",".join(map(str, frames))),
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
@@ -899,6 +911,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the short batched block of the default run")
+    ap.add_argument("--tiles", default="", help="rows of the stress and velocity tiles, e.g. 16,8 (default: 8,8)")
+    ap.add_argument("--zchunks", default="", help="z-sweep depths of the stress and velocity kernels, e.g. 8,128")
+    ap.add_argument("--pml-points", type=int, default=0, choices=[0, 1, 2],
+                    help="shell points per thread of the PML kernels (0: library default)")
     ap.add_argument("--medium", default="device", choices=["device", "host"],
                     help="build the random medium on the GPU (default) or on the host and upload it")
     ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])

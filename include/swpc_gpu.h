@@ -77,7 +77,9 @@ typedef struct swpc_dims {
     double M0;           /* total moment (m_source.f90:190-198) */
     double UC;           /* unit conversion (m_global.f90:29; x1e3 in body-force mode) */
     int ntdec_r;         /* divergence-check interval (m_report.f90:134); 0 = off */
-    int reserved[7];
+    int reserved[7];     /* 0 (all zero: library defaults); [0] 1 = interior kernels without TMA,
+                            [1] 1/2 = PML kernels in series/beside the interior ones,
+                            [2] 1/2 = PML shell points per thread */
 } swpc_dims;
 
 /* Create a simulation and allocate its device state on the current CUDA

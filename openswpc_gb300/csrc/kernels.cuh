@@ -484,14 +484,24 @@ __device__ __forceinline__ float4 pml_prof(const PArgs& a, int off, int i) {
     return make_float4(1.f, -1.f, 1.f, 0.f);
 }
 
-// PML stress update (m_absorb_p.f90:429-531) at shell point c.  Every load
-// is issued before any arithmetic or store, so a thread has all of its ~40
-// independent loads in flight at once (the kernel is bound by load latency).
+// PML stress update (m_absorb_p.f90:429-531) at shell point c, in two stages:
+// stress_pml_load issues every load of the point (about 40 independent
+// words; the kernel is bound by load latency, so all of them go out before
+// any arithmetic or store), stress_pml_store does the arithmetic and the
+// stores.  A thread may load two points before storing either.
+struct PmlSIn {
+    float* S;
+    float* A;
+    int P, AP;
+    float4 gxc, gxe, gyc, gye, gzc, gze;
+    float vx, vy, vz, vxw, vys, vzu, vye, vze, vxn, vzn, vxd, vyd;
+    float lamv, m000, m100, m010, m110, m001, m011, m101;
+    float ad[9], sv[6];
+};
 template <int MASK>
-__device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
+__device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, PmlSIn& L) {
     const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
-    const float eps = 1.1920928955078125e-07f;
     const int P = g.pitch;
     const long long rowV = 3LL * P, planeV = rowV * g.nyp;
     const long long rowM = 5LL * P, planeM = rowM * g.nyp;
@@ -502,43 +512,55 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
     const float* __restrict__ V = a.V + oV;
     const float* __restrict__ M = a.M + oM;
-    float* __restrict__ S = a.S + oS;
-    float* __restrict__ A = a.adeV + oA;
-    const int AP = B.pitch;
-    // loads
-    const float4 gxc = pml_prof<MASK, 0>(a, a.pxc, ix), gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
-    const float4 gyc = pml_prof<MASK, 1>(a, a.pyc, jy), gye = pml_prof<MASK, 1>(a, a.pye, jy);
-    const float4 gzc = pml_prof<MASK, 2>(a, a.pzc, kz), gze = pml_prof<MASK, 2>(a, a.pze, kz);
-    const float vx = V[0], vy = V[P], vz = V[2 * P];
-    const float vxw = V[-1], vys = V[P - rowV], vzu = V[2 * P - planeV];
-    const float vye = V[P + 1], vze = V[2 * P + 1], vxn = V[rowV], vzn = V[2 * P + rowV];
-    const float vxd = V[planeV], vyd = V[P + planeV];
-    const float lamv = M[P], m000 = M[2 * P], m100 = M[2 * P + planeM], m010 = M[2 * P + 1];
-    const float m110 = M[2 * P + planeM + 1], m001 = M[2 * P + rowM], m011 = M[2 * P + rowM + 1];
-    const float m101 = M[2 * P + planeM + rowM];
+    L.S = a.S + oS;
+    L.A = a.adeV + oA;
+    L.P = P;
+    L.AP = B.pitch;
+    L.gxc = pml_prof<MASK, 0>(a, a.pxc, ix); L.gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
+    L.gyc = pml_prof<MASK, 1>(a, a.pyc, jy); L.gye = pml_prof<MASK, 1>(a, a.pye, jy);
+    L.gzc = pml_prof<MASK, 2>(a, a.pzc, kz); L.gze = pml_prof<MASK, 2>(a, a.pze, kz);
+    L.vx = V[0]; L.vy = V[P]; L.vz = V[2 * P];
+    L.vxw = V[-1]; L.vys = V[P - rowV]; L.vzu = V[2 * P - planeV];
+    L.vye = V[P + 1]; L.vze = V[2 * P + 1]; L.vxn = V[rowV]; L.vzn = V[2 * P + rowV];
+    L.vxd = V[planeV]; L.vyd = V[P + planeV];
+    L.lamv = M[P]; L.m000 = M[2 * P]; L.m100 = M[2 * P + planeM]; L.m010 = M[2 * P + 1];
+    L.m110 = M[2 * P + planeM + 1]; L.m001 = M[2 * P + rowM]; L.m011 = M[2 * P + rowM + 1];
+    L.m101 = M[2 * P + planeM + rowM];
     // an auxiliary variable whose axis has no damping here (g4 = 0, the
     // point lies outside that axis's layer) starts at zero and its update
     // g3 * 0 + 0 keeps it zero: it is neither loaded nor stored.  Order:
     // axVx ayVy azVz ayVx azVx axVy azVy axVz ayVz
+    const bool live[9] = {L.gxc.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gye.w != 0.f, L.gze.w != 0.f,
+                          L.gxe.w != 0.f, L.gze.w != 0.f, L.gxe.w != 0.f, L.gye.w != 0.f};
+    const float* __restrict__ A = L.A;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) L.ad[q] = live[q] ? A[q * L.AP] : 0.f;
+    const float* __restrict__ S = L.S;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) L.sv[q] = S[q * P];
+}
+__device__ __forceinline__ void stress_pml_store(const PArgs& a, const PmlSIn& L) {
+    const float eps = 1.1920928955078125e-07f;
+    const int P = L.P, AP = L.AP;
+    float* __restrict__ S = L.S;
+    float* __restrict__ A = L.A;
+    const float4 gxc = L.gxc, gxe = L.gxe, gyc = L.gyc, gye = L.gye, gzc = L.gzc, gze = L.gze;
     const bool live[9] = {gxc.w != 0.f, gyc.w != 0.f, gzc.w != 0.f, gye.w != 0.f, gze.w != 0.f,
                           gxe.w != 0.f, gze.w != 0.f, gxe.w != 0.f, gye.w != 0.f};
-    float ad[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) ad[q] = live[q] ? A[q * AP] : 0.f;
-    float sv[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) sv[q] = S[q * P];
+    const float* ad = L.ad;
+    const float* sv = L.sv;
+    const float vx = L.vx, vy = L.vy, vz = L.vz;
     // every operation below is an explicitly rounded intrinsic, so that the
     // kernels specialised to one damped axis (profile constants 1, -1, 1, 0)
     // and the general kernel produce the same bits: the compiler may not
     // contract or reorder them differently around the constants
     const float dt = a.dt;
     // normal part (m_absorb_p.f90:453-474)
-    const float dxVx = __fmul_rn(__fsub_rn(vx, vxw), a.r20x);
-    const float dyVy = __fmul_rn(__fsub_rn(vy, vys), a.r20y);
-    const float dzVz = __fmul_rn(__fsub_rn(vz, vzu), a.r20z);
-    const float lam2mu = __fmaf_rn(2.f, m000, lamv);
-    const float lamR = __fmaf_rn(-2.f, m000, lam2mu);
+    const float dxVx = __fmul_rn(__fsub_rn(vx, L.vxw), a.r20x);
+    const float dyVy = __fmul_rn(__fsub_rn(vy, L.vys), a.r20y);
+    const float dzVz = __fmul_rn(__fsub_rn(vz, L.vzu), a.r20z);
+    const float lam2mu = __fmaf_rn(2.f, L.m000, L.lamv);
+    const float lamR = __fmaf_rn(-2.f, L.m000, lam2mu);
     const float dxa = __fmaf_rn(gxc.y, ad[0], __fmul_rn(gxc.x, dxVx));
     const float dya = __fmaf_rn(gyc.y, ad[1], __fmul_rn(gyc.x, dyVy));
     const float dza = __fmaf_rn(gzc.y, ad[2], __fmul_rn(gzc.x, dzVz));
@@ -550,12 +572,12 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     if (live[1]) A[AP] = ade(gyc, ad[1], dyVy);
     if (live[2]) A[2 * AP] = ade(gzc, ad[2], dzVz);
     // shear part (m_absorb_p.f90:477-518)
-    const float dxVy = __fmul_rn(__fsub_rn(vye, vy), a.r20x);
-    const float dxVz = __fmul_rn(__fsub_rn(vze, vz), a.r20x);
-    const float dyVx = __fmul_rn(__fsub_rn(vxn, vx), a.r20y);
-    const float dyVz = __fmul_rn(__fsub_rn(vzn, vz), a.r20y);
-    const float dzVx = __fmul_rn(__fsub_rn(vxd, vx), a.r20z);
-    const float dzVy = __fmul_rn(__fsub_rn(vyd, vy), a.r20z);
+    const float dxVy = __fmul_rn(__fsub_rn(L.vye, vy), a.r20x);
+    const float dxVz = __fmul_rn(__fsub_rn(L.vze, vz), a.r20x);
+    const float dyVx = __fmul_rn(__fsub_rn(L.vxn, vx), a.r20y);
+    const float dyVz = __fmul_rn(__fsub_rn(L.vzn, vz), a.r20y);
+    const float dzVx = __fmul_rn(__fsub_rn(L.vxd, vx), a.r20z);
+    const float dzVy = __fmul_rn(__fsub_rn(L.vyd, vy), a.r20z);
     // harmonic mean of four moduli: 4 m1 m2 m3 m4 / (sum of the triple products + eps)
     auto hmean = [eps](float m1, float m2, float m3, float m4) {
         const float num = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(4.f, m1), m2), m3), m4);
@@ -566,9 +588,9 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
         den = __fadd_rn(den, __fmul_rn(__fmul_rn(m2, m3), m4));
         return __fdiv_rn(num, __fadd_rn(den, eps));
     };
-    const float muxz = hmean(m000, m100, m010, m110);
-    const float muxy = hmean(m000, m010, m001, m011);
-    const float muyz = hmean(m000, m100, m001, m101);
+    const float muxz = hmean(L.m000, L.m100, L.m010, L.m110);
+    const float muxy = hmean(L.m000, L.m010, L.m001, L.m011);
+    const float muyz = hmean(L.m000, L.m100, L.m001, L.m101);
     const float ayVx = ad[3], azVx = ad[4], axVy = ad[5], azVy = ad[6], axVz = ad[7], ayVz = ad[8];
     // (g1 d1 + g1' d2 + g2 a1 + g2' a2) in a fixed order
     auto sum4 = [](float4 p, float d1, float4 q, float d2, float a1, float a2) {
@@ -587,10 +609,26 @@ __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
     if (live[7]) A[7 * AP] = ade(gxe, axVz, dxVz);
     if (live[8]) A[8 * AP] = ade(gye, ayVz, dyVz);
 }
-
-// PML velocity update (m_absorb_p.f90:246-317) at shell point c, loads first.
 template <int MASK>
-__device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
+__device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
+    PmlSIn L;
+    stress_pml_load<MASK>(a, c, L);
+    stress_pml_store(a, L);
+}
+
+// PML velocity update (m_absorb_p.f90:246-317) at shell point c, in the same
+// two stages.
+struct PmlVIn {
+    float* V;
+    float* A;
+    int P, AP;
+    float4 gxc, gxe, gyc, gye, gzc, gze;
+    float sxx, syy, szz, syz, sxz, sxy, sxxe, syyn, szzd, syzs, syzu, sxzw, sxzu, sxyw, sxys;
+    float r0, rx, ry, rz;
+    float ad[9], v0, v1, v2;
+};
+template <int MASK>
+__device__ __forceinline__ void vel_pml_load(const PArgs& a, const PmlPt c, PmlVIn& L) {
     const PmlBox& B = a.box[c.b];
     const Geo& g = a.g;
     const int P = g.pitch;
@@ -603,42 +641,52 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
     const float* __restrict__ S = a.S + oS;
     const float* __restrict__ M = a.M + oM;
-    float* __restrict__ V = a.V + oV;
-    float* __restrict__ A = a.adeS + oA;
-    const int AP = B.pitch;
-    // loads
-    const float4 gxc = pml_prof<MASK, 0>(a, a.pxc, ix), gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
-    const float4 gyc = pml_prof<MASK, 1>(a, a.pyc, jy), gye = pml_prof<MASK, 1>(a, a.pye, jy);
-    const float4 gzc = pml_prof<MASK, 2>(a, a.pzc, kz), gze = pml_prof<MASK, 2>(a, a.pze, kz);
-    const float sxx = S[0], syy = S[P], szz = S[2 * P], syz = S[3 * P], sxz = S[4 * P], sxy = S[5 * P];
-    const float sxxe = S[1], syyn = S[P + rowS], szzd = S[2 * P + planeS];
-    const float syzs = S[3 * P - rowS], syzu = S[3 * P - planeS];
-    const float sxzw = S[4 * P - 1], sxzu = S[4 * P - planeS];
-    const float sxyw = S[5 * P - 1], sxys = S[5 * P - rowS];
-    const float r0 = M[0], rx = M[1], ry = M[rowM], rz = M[planeM];
+    L.V = a.V + oV;
+    L.A = a.adeS + oA;
+    L.P = P;
+    L.AP = B.pitch;
+    L.gxc = pml_prof<MASK, 0>(a, a.pxc, ix); L.gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
+    L.gyc = pml_prof<MASK, 1>(a, a.pyc, jy); L.gye = pml_prof<MASK, 1>(a, a.pye, jy);
+    L.gzc = pml_prof<MASK, 2>(a, a.pzc, kz); L.gze = pml_prof<MASK, 2>(a, a.pze, kz);
+    L.sxx = S[0]; L.syy = S[P]; L.szz = S[2 * P]; L.syz = S[3 * P]; L.sxz = S[4 * P]; L.sxy = S[5 * P];
+    L.sxxe = S[1]; L.syyn = S[P + rowS]; L.szzd = S[2 * P + planeS];
+    L.syzs = S[3 * P - rowS]; L.syzu = S[3 * P - planeS];
+    L.sxzw = S[4 * P - 1]; L.sxzu = S[4 * P - planeS];
+    L.sxyw = S[5 * P - 1]; L.sxys = S[5 * P - rowS];
+    L.r0 = M[0]; L.rx = M[1]; L.ry = M[rowM]; L.rz = M[planeM];
     // auxiliaries of undamped axes stay zero (as in the stress update).
     // Order: axSxx aySxy azSxz axSxy aySyy azSyz axSxz aySyz azSzz
+    const bool live[9] = {L.gxe.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gxc.w != 0.f, L.gye.w != 0.f,
+                          L.gzc.w != 0.f, L.gxc.w != 0.f, L.gyc.w != 0.f, L.gze.w != 0.f};
+    const float* __restrict__ A = L.A;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) L.ad[q] = live[q] ? A[q * L.AP] : 0.f;
+    const float* __restrict__ V = L.V;
+    L.v0 = V[0]; L.v1 = V[P]; L.v2 = V[2 * P];
+}
+__device__ __forceinline__ void vel_pml_store(const PArgs& a, const PmlVIn& L) {
+    const int P = L.P, AP = L.AP;
+    float* __restrict__ V = L.V;
+    float* __restrict__ A = L.A;
+    const float4 gxc = L.gxc, gxe = L.gxe, gyc = L.gyc, gye = L.gye, gzc = L.gzc, gze = L.gze;
     const bool live[9] = {gxe.w != 0.f, gyc.w != 0.f, gzc.w != 0.f, gxc.w != 0.f, gye.w != 0.f,
                           gzc.w != 0.f, gxc.w != 0.f, gyc.w != 0.f, gze.w != 0.f};
-    float ad[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) ad[q] = live[q] ? A[q * AP] : 0.f;
-    const float v0 = V[0], v1 = V[P], v2 = V[2 * P];
     // explicitly rounded operations, as in the stress update
     const float dt = a.dt;
     // m_absorb_p.f90:265-305
-    const float dxSxx = __fmul_rn(__fsub_rn(sxxe, sxx), a.r20x);
-    const float dySyy = __fmul_rn(__fsub_rn(syyn, syy), a.r20y);
-    const float dzSzz = __fmul_rn(__fsub_rn(szzd, szz), a.r20z);
-    const float dySyz = __fmul_rn(__fsub_rn(syz, syzs), a.r20y);
-    const float dzSyz = __fmul_rn(__fsub_rn(syz, syzu), a.r20z);
-    const float dxSxz = __fmul_rn(__fsub_rn(sxz, sxzw), a.r20x);
-    const float dzSxz = __fmul_rn(__fsub_rn(sxz, sxzu), a.r20z);
-    const float dxSxy = __fmul_rn(__fsub_rn(sxy, sxyw), a.r20x);
-    const float dySxy = __fmul_rn(__fsub_rn(sxy, sxys), a.r20y);
-    const float bx = __fdiv_rn(2.f, __fadd_rn(r0, rx));
-    const float by = __fdiv_rn(2.f, __fadd_rn(r0, ry));
-    const float bz = __fdiv_rn(2.f, __fadd_rn(r0, rz));
+    const float dxSxx = __fmul_rn(__fsub_rn(L.sxxe, L.sxx), a.r20x);
+    const float dySyy = __fmul_rn(__fsub_rn(L.syyn, L.syy), a.r20y);
+    const float dzSzz = __fmul_rn(__fsub_rn(L.szzd, L.szz), a.r20z);
+    const float dySyz = __fmul_rn(__fsub_rn(L.syz, L.syzs), a.r20y);
+    const float dzSyz = __fmul_rn(__fsub_rn(L.syz, L.syzu), a.r20z);
+    const float dxSxz = __fmul_rn(__fsub_rn(L.sxz, L.sxzw), a.r20x);
+    const float dzSxz = __fmul_rn(__fsub_rn(L.sxz, L.sxzu), a.r20z);
+    const float dxSxy = __fmul_rn(__fsub_rn(L.sxy, L.sxyw), a.r20x);
+    const float dySxy = __fmul_rn(__fsub_rn(L.sxy, L.sxys), a.r20y);
+    const float bx = __fdiv_rn(2.f, __fadd_rn(L.r0, L.rx));
+    const float by = __fdiv_rn(2.f, __fadd_rn(L.r0, L.ry));
+    const float bz = __fdiv_rn(2.f, __fadd_rn(L.r0, L.rz));
+    const float* ad = L.ad;
     const float axSxx = ad[0], aySxy = ad[1], azSxz = ad[2], axSxy = ad[3], aySyy = ad[4];
     const float azSyz = ad[5], axSxz = ad[6], aySyz = ad[7], azSzz = ad[8];
     // (g1 d1 + g1' d2 + g1'' d3 + g2 a1 + g2' a2 + g2'' a3) in a fixed order
@@ -650,9 +698,9 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
         t = __fmaf_rn(q.y, a2, t);
         return __fmaf_rn(r.y, a3, t);
     };
-    V[0] = __fmaf_rn(__fmul_rn(bx, sum6(gxe, dxSxx, gyc, dySxy, gzc, dzSxz, axSxx, aySxy, azSxz)), dt, v0);
-    V[P] = __fmaf_rn(__fmul_rn(by, sum6(gxc, dxSxy, gye, dySyy, gzc, dzSyz, axSxy, aySyy, azSyz)), dt, v1);
-    V[2 * P] = __fmaf_rn(__fmul_rn(bz, sum6(gxc, dxSxz, gyc, dySyz, gze, dzSzz, axSxz, aySyz, azSzz)), dt, v2);
+    V[0] = __fmaf_rn(__fmul_rn(bx, sum6(gxe, dxSxx, gyc, dySxy, gzc, dzSxz, axSxx, aySxy, azSxz)), dt, L.v0);
+    V[P] = __fmaf_rn(__fmul_rn(by, sum6(gxc, dxSxy, gye, dySyy, gzc, dzSyz, axSxy, aySyy, azSyz)), dt, L.v1);
+    V[2 * P] = __fmaf_rn(__fmul_rn(bz, sum6(gxc, dxSxz, gyc, dySyz, gze, dzSzz, axSxz, aySyz, azSzz)), dt, L.v2);
     auto ade = [dt](float4 gp, float aux, float d) { return __fmaf_rn(gp.z, aux, __fmul_rn(__fmul_rn(gp.w, d), dt)); };
     if (live[0]) A[0] = ade(gxe, axSxx, dxSxx);
     if (live[1]) A[AP] = ade(gyc, aySxy, dySxy);
@@ -663,6 +711,37 @@ __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     if (live[6]) A[6 * AP] = ade(gxc, axSxz, dxSxz);
     if (live[7]) A[7 * AP] = ade(gyc, aySyz, dySyz);
     if (live[8]) A[8 * AP] = ade(gze, azSzz, dzSzz);
+}
+template <int MASK>
+__device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
+    PmlVIn L;
+    vel_pml_load<MASK>(a, c, L);
+    vel_pml_store(a, L);
+}
+
+// Two points per thread: both points' loads go out before either point's
+// arithmetic and stores (points of blocks 2b and 2b + 1 of the launch).
+template <int MASK>
+__device__ __forceinline__ void stress_pml_two(const PArgs& a, int b2, int t) {
+    PmlPt c0, c1;
+    const bool o0 = pml_point(a, 2 * b2, t, c0);
+    const bool o1 = 2 * b2 + 1 < a.nblocks && pml_point(a, 2 * b2 + 1, t, c1);
+    PmlSIn L0, L1;
+    if (o0) stress_pml_load<MASK>(a, c0, L0);
+    if (o1) stress_pml_load<MASK>(a, c1, L1);
+    if (o0) stress_pml_store(a, L0);
+    if (o1) stress_pml_store(a, L1);
+}
+template <int MASK>
+__device__ __forceinline__ void vel_pml_two(const PArgs& a, int b2, int t) {
+    PmlPt c0, c1;
+    const bool o0 = pml_point(a, 2 * b2, t, c0);
+    const bool o1 = 2 * b2 + 1 < a.nblocks && pml_point(a, 2 * b2 + 1, t, c1);
+    PmlVIn L0, L1;
+    if (o0) vel_pml_load<MASK>(a, c0, L0);
+    if (o1) vel_pml_load<MASK>(a, c1, L1);
+    if (o0) vel_pml_store(a, L0);
+    if (o1) vel_pml_store(a, L1);
 }
 
 // One thread per shell point.  MASK: the axes damped somewhere in the parts
@@ -680,6 +759,11 @@ __global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml(const PArgs
     PmlPt c;
     if (pml_point(a, blockIdx.x, threadIdx.x, c)) vel_pml_at<MASK>(a, c);
 }
+// two points per thread (block b covers blocks 2b and 2b + 1 of the parts)
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 4 : 5) k_stress_pml2(const PArgs a) { stress_pml_two<MASK>(a, blockIdx.x, threadIdx.x); }
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 4 : 5) k_vel_pml2(const PArgs a) { vel_pml_two<MASK>(a, blockIdx.x, threadIdx.x); }
 // batched: block b is block e.y of member e.x's launch, e = blocks[b]
 template <int MASK>
 __global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_stress_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {

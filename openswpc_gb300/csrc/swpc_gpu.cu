@@ -154,13 +154,31 @@ void Sim::launch_pml(bool stress, cudaStream_t st, bool timed) {
         cudaEventRecord(pe.b, st);
         pending.push_back(pe);
     };
+    // one launch of a class: one or two shell points per thread
+    auto go = [&](int mask, const PArgs& a) {
+        if (pml_np == 2) {
+            const unsigned nb = (unsigned)((a.nblocks + 1) / 2);
+            switch (mask) {
+            case 1: stress ? k_stress_pml2<1><<<nb, PTPB, 0, st>>>(a) : k_vel_pml2<1><<<nb, PTPB, 0, st>>>(a); break;
+            case 2: stress ? k_stress_pml2<2><<<nb, PTPB, 0, st>>>(a) : k_vel_pml2<2><<<nb, PTPB, 0, st>>>(a); break;
+            case 4: stress ? k_stress_pml2<4><<<nb, PTPB, 0, st>>>(a) : k_vel_pml2<4><<<nb, PTPB, 0, st>>>(a); break;
+            default: stress ? k_stress_pml2<7><<<nb, PTPB, 0, st>>>(a) : k_vel_pml2<7><<<nb, PTPB, 0, st>>>(a); break;
+            }
+            return;
+        }
+        const unsigned nb = (unsigned)a.nblocks;
+        switch (mask) {
+        case 1: stress ? k_stress_pml<1><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<1><<<nb, PTPB, 0, st>>>(a); break;
+        case 2: stress ? k_stress_pml<2><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<2><<<nb, PTPB, 0, st>>>(a); break;
+        case 4: stress ? k_stress_pml<4><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<4><<<nb, PTPB, 0, st>>>(a); break;
+        default: stress ? k_stress_pml<7><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<7><<<nb, PTPB, 0, st>>>(a); break;
+        }
+    };
     if (!pml_split) {
         if (pml_all.nblocks == 0) return;
-        const unsigned nb = (unsigned)pml_all.nblocks;
         Pending pe{};
         if (timed) pe = ev(base + PML_NCLASS - 1);
-        if (stress) k_stress_pml<7><<<nb, PTPB, 0, st>>>(pml_all);
-        else k_vel_pml<7><<<nb, PTPB, 0, st>>>(pml_all);
+        go(7, pml_all);
         if (timed) done(pe);
         ++launches;
         return;
@@ -168,15 +186,9 @@ void Sim::launch_pml(bool stress, cudaStream_t st, bool timed) {
     for (int q = 0; q < PML_NCLASS; ++q) {
         const PArgs& a = pml_cls[q];
         if (a.nblocks == 0) continue;
-        const unsigned nb = (unsigned)a.nblocks;
         Pending pe{};
         if (timed) pe = ev(base + q);
-        switch (PML_CLASS_MASK[q]) {
-        case 1: stress ? k_stress_pml<1><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<1><<<nb, PTPB, 0, st>>>(a); break;
-        case 2: stress ? k_stress_pml<2><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<2><<<nb, PTPB, 0, st>>>(a); break;
-        case 4: stress ? k_stress_pml<4><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<4><<<nb, PTPB, 0, st>>>(a); break;
-        default: stress ? k_stress_pml<7><<<nb, PTPB, 0, st>>>(a) : k_vel_pml<7><<<nb, PTPB, 0, st>>>(a); break;
-        }
+        go(PML_CLASS_MASK[q], a);
         if (timed) done(pe);
         ++launches;
     }
@@ -1007,6 +1019,7 @@ int Sim::allocate() {
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
     variant = dims.reserved[0] == 1 ? 1 : 0;
+    pml_np = dims.reserved[2] == 2 ? 2 : 1;
     // PML shell beside the interior: pays off only when the interior launch
     // cannot fill the GPU by itself (measured: 128x128x64 0.134 vs 0.16 ms per
     // step; 1024x1024x512 27.9 serial vs 28.3 ms concurrent)

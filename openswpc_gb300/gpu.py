@@ -186,11 +186,13 @@ def _ptr(a):
 
 
 def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xbeg=0.0, ybeg=0.0, zbeg=0.0,
-              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0, concurrent=None):
+              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0, concurrent=None, pml_points=0):
     """swpc_dims for swpc_gpu_create.  variant 0 selects the TMA-fed interior
     kernels, 1 the shared-memory sweep without TMA (kept for comparison);
     concurrent runs the PML shell kernels beside the interior kernels on a
-    second stream (True/False; None lets the library choose by grid size)."""
+    second stream (True/False; None lets the library choose by grid size);
+    pml_points: shell points per thread of the PML kernels (1 or 2; 0 lets
+    the library choose)."""
     d = Dims()
     d.nx, d.ny, d.nz, d.nt, d.na, d.nm = nx, ny, nz, nt, na, 3
     d.abc_type = 0 if abc == "pml" else 1
@@ -200,6 +202,7 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     d.fcut, d.M0, d.UC, d.ntdec_r = fcut, M0, UC, ntdec_r
     d.reserved[0] = int(variant)
     d.reserved[1] = 0 if concurrent is None else (2 if concurrent else 1)
+    d.reserved[2] = int(pml_points)
     return d
 
 
