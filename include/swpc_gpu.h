@@ -79,7 +79,8 @@ typedef struct swpc_dims {
     int ntdec_r;         /* divergence-check interval (m_report.f90:134); 0 = off */
     int reserved[7];     /* 0 (all zero: library defaults); [0] 1 = interior kernels without TMA,
                             [1] 1/2 = PML kernels in series/beside the interior ones,
-                            [2] 1/2 = PML shell points per thread */
+                            [2] 1/2 = PML shell points per thread (0: two for the stress update
+                            of the y and z classes, one elsewhere) */
 } swpc_dims;
 
 /* Create a simulation and allocate its device state on the current CUDA

@@ -777,6 +777,23 @@ __global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml_batch(const
     PmlPt c;
     if (pml_point(all[e.x], e.y, threadIdx.x, c)) vel_pml_at<MASK>(all[e.x], c);
 }
+// batched, two shell points per thread: block b takes table entries 2b and
+// 2b + 1 (which may belong to different members)
+template <int MASK>
+__global__ void __launch_bounds__(PTPB, 5) k_stress_pml2_batch(const PArgs* __restrict__ all,
+                                                               const int2* __restrict__ blocks, int n) {
+    const int i0 = 2 * blockIdx.x, i1 = i0 + 1;
+    const int2 e0 = blocks[i0];
+    const int2 e1 = i1 < n ? blocks[i1] : e0;
+    PmlPt c0, c1;
+    const bool o0 = pml_point(all[e0.x], e0.y, threadIdx.x, c0);
+    const bool o1 = i1 < n && pml_point(all[e1.x], e1.y, threadIdx.x, c1);
+    PmlSIn L0, L1;
+    if (o0) stress_pml_load<MASK>(all[e0.x], c0, L0);
+    if (o1) stress_pml_load<MASK>(all[e1.x], c1, L1);
+    if (o0) stress_pml_store(all[e0.x], L0);
+    if (o1) stress_pml_store(all[e1.x], L1);
+}
 // the launch classes: x only, y only, z only, any
 constexpr int PML_NCLASS = 4;
 constexpr int PML_CLASS_MASK[PML_NCLASS] = {1, 2, 4, 7};

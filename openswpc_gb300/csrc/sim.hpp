@@ -51,7 +51,7 @@ struct Sim {
     int kchunk_v = 1, kchunk_v_auto = 1;  // and of the velocity kernels
     int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
     int ty_s = TTY, ty_v = TTY;  // tile rows of the stress and velocity TMA kernels (8 or 16)
-    int pml_np = 1;              // shell points per thread of the PML kernels (1 or 2)
+    int pml_np = 0;              // shell points per thread of the PML kernels (1, 2; 0: by launch class)
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
     size_t smem_stress = 0, smem_vel = 0;
 

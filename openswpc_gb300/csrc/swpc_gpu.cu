@@ -154,9 +154,14 @@ void Sim::launch_pml(bool stress, cudaStream_t st, bool timed) {
         cudaEventRecord(pe.b, st);
         pending.push_back(pe);
     };
-    // one launch of a class: one or two shell points per thread
+    // one launch of a class: one or two shell points per thread.  By
+    // default the stress update of the y and z classes takes two (their
+    // loads are whole rows; 0.376 -> 0.340 and 0.358 -> 0.341 ms on the
+    // 1024x1024x512 grid), every other launch one (two were slower there:
+    // corners 0.143 -> 0.165 ms, velocity classes up to 0.115 -> 0.146 ms)
     auto go = [&](int mask, const PArgs& a) {
-        if (pml_np == 2) {
+        const bool two = pml_np == 2 || (pml_np == 0 && stress && (mask == 2 || mask == 4));
+        if (two) {
             const unsigned nb = (unsigned)((a.nblocks + 1) / 2);
             switch (mask) {
             case 1: stress ? k_stress_pml2<1><<<nb, PTPB, 0, st>>>(a) : k_vel_pml2<1><<<nb, PTPB, 0, st>>>(a); break;
@@ -1019,7 +1024,7 @@ int Sim::allocate() {
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
     variant = dims.reserved[0] == 1 ? 1 : 0;
-    pml_np = dims.reserved[2] == 2 ? 2 : 1;
+    pml_np = dims.reserved[2] == 2 ? 2 : dims.reserved[2] == 1 ? 1 : 0;  // 0: per launch class
     // PML shell beside the interior: pays off only when the interior launch
     // cannot fill the GPU by itself (measured: 128x128x64 0.134 vs 0.16 ms per
     // step; 1024x1024x512 27.9 serial vs 28.3 ms concurrent)
@@ -1692,6 +1697,15 @@ struct Batch {
             const unsigned nb = (unsigned)n_pblocks[q];
             const PArgs* a = d_pargs[q];
             const int2* t = d_pblocks[q];
+            // the stress update of the y and z classes takes two points per
+            // thread, as in the single-simulation launches
+            if (stress && (PML_CLASS_MASK[q] == 2 || PML_CLASS_MASK[q] == 4)) {
+                const unsigned nb2 = (nb + 1) / 2;
+                if (PML_CLASS_MASK[q] == 2) k_stress_pml2_batch<2><<<nb2, PTPB, 0, stream2>>>(a, t, (int)nb);
+                else k_stress_pml2_batch<4><<<nb2, PTPB, 0, stream2>>>(a, t, (int)nb);
+                ++launches;
+                continue;
+            }
             switch (PML_CLASS_MASK[q]) {
             case 1: stress ? k_stress_pml_batch<1><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<1><<<nb, PTPB, 0, stream2>>>(a, t); break;
             case 2: stress ? k_stress_pml_batch<2><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<2><<<nb, PTPB, 0, stream2>>>(a, t); break;

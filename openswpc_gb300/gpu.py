@@ -192,7 +192,7 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     concurrent runs the PML shell kernels beside the interior kernels on a
     second stream (True/False; None lets the library choose by grid size);
     pml_points: shell points per thread of the PML kernels (1 or 2; 0 lets
-    the library choose)."""
+    the library choose per launch class)."""
     d = Dims()
     d.nx, d.ny, d.nz, d.nt, d.na, d.nm = nx, ny, nz, nt, na, 3
     d.abc_type = 0 if abc == "pml" else 1

@@ -25,8 +25,9 @@ def _sim(n, pml_points, nt=30):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [(96, 80, 64), (288, 288, 144)])
-def test_two_points_per_thread_equal_one(n):
-    a, b = _sim(n, 1), _sim(n, 2)
+@pytest.mark.parametrize("other", [2, 0])
+def test_two_points_per_thread_equal_one(n, other):
+    a, b = _sim(n, 1), _sim(n, other)
     a.run(1, 30)
     b.run(1, 30)
     for name in gpu.FIELDS:
