@@ -559,9 +559,12 @@ def run_gpu(args, w):
         cb = cpu_sample()
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
-    batch = None
+    batch = serve = prec = None
     if rank == 0 and world == 1 and not args.no_batch:
         batch = batch_block(args)
+        serve = serve_block()
+        if args.store == "fp32":
+            prec = precision_block(w, med, ms_max / args.steps)
 
     if rank == 0:
         line = {
@@ -587,6 +590,8 @@ def run_gpu(args, w):
             "cpu_baseline": cpu,
             "parity": parity_statement(),
             "batched": batch,
+            "served": serve,
+            "precision": prec,
             "setup_s": t_setup,
             "medium_setup": med["where"],
         }
@@ -741,26 +746,23 @@ def serve_inputs(n, seed, nt, root, tail=0.1):
     return infs, sizes
 
 
-def run_serve(args):
-    """Serving form: Poisson arrivals at each rate of --rates submitted to the
+def serve_measure(requests, nt, rates, budget_gb, quantum, seed=20261203):
+    """Serving form: Poisson arrivals at each rate submitted to the
     continuous-batching server (swpc_serve_*), latency = completion minus
     arrival; then the same requests one after another on the plain path
     (host set-up + run + trace read-back each), which also gives every
     request's result alone for the misfit check."""
     from openswpc_gb300 import gpu
     gpu.lib()
-    rates = [float(r) for r in args.rates.split(",")]
-    out = {"metric": "served solves/s and latency", "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
     with tempfile.TemporaryDirectory() as root:
-        infs, sizes = serve_inputs(args.requests, 20261203, args.nt, root)
+        infs, sizes = serve_inputs(requests, seed, nt, root)
         pts = [int(np.prod(s)) for s in sizes]
         # sequential plain path: each request alone, end to end
         alone = []
         t0 = time.perf_counter()
         for f in infs:
             s = gpu.Simulation.from_inf(f)
-            s.run(1, args.nt)
+            s.run(1, nt)
             s.sync()
             alone.append(s.waveforms())
             s.close()
@@ -770,7 +772,7 @@ def run_serve(args):
         for lam in rates:
             rng = np.random.default_rng(int(lam * 1000) + 7)
             gaps = rng.exponential(1.0 / lam, size=len(infs))
-            with gpu.Server(hbm_budget=args.budget_gb * 1e9, quantum=args.quantum, prep_threads=8) as srv:
+            with gpu.Server(hbm_budget=budget_gb * 1e9, quantum=quantum, prep_threads=8) as srv:
                 ids = []
                 tstart = time.perf_counter()
                 tnext = tstart
@@ -799,17 +801,65 @@ def run_serve(args):
                              "quanta": int(st["quanta"]), "batch_rebuilds": int(st["rebuilds"]),
                              "grid_pt_updates_per_s": st["updates"] / t_all})
     best = max(per_rate, key=lambda r: r["solves_per_s"])
-    out.update({"value": best["solves_per_s"], "rates": per_rate,
-                "sequential_solves_per_s": len(infs) / t_seq, "sequential_wall_s": t_seq,
-                "speedup_vs_sequential": best["solves_per_s"] / (len(infs) / t_seq),
-                "misfit_vs_alone_max": worst,
-                "config": {"workload": "serving: Poisson arrivals, %d requests per rate, axes in {96..256} with 10%% "
-                                       "512x512x256, nt=%d" % (len(infs), args.nt),
-                           "hbm_budget_gb": args.budget_gb, "quantum_steps": args.quantum,
-                           "points_total": int(sum(pts)),
-                           "timing": "wall clock from first arrival to last completion, host set-up included"}})
+    return {"requests": len(infs), "nt": nt, "rates": per_rate, "best_solves_per_s": best["solves_per_s"],
+            "sequential_solves_per_s": len(infs) / t_seq, "sequential_wall_s": t_seq,
+            "speedup_vs_sequential": best["solves_per_s"] / (len(infs) / t_seq), "misfit_vs_alone_max": worst,
+            "points_total": int(sum(pts)), "hbm_budget_gb": budget_gb, "quantum_steps": quantum}
+
+
+def serve_block():
+    """Short serving block of the default run: 24 requests of the serving
+    workload (10 % of them 512 x 512 x 256), nt = 300, arriving at 20 per s."""
+    try:
+        r = serve_measure(24, 300, [20.0], 150.0, 50)
+        r["workload"] = "serving: 24 Poisson requests at 20/s, axes in {96..256} with 10% 512x512x256, nt=300"
+        return r
+    except Exception as e:  # the headline line is still printed
+        return {"error": str(e)}
+
+
+def run_serve(args):
+    rates = [float(r) for r in args.rates.split(",")]
+    r = serve_measure(args.requests, args.nt, rates, args.budget_gb, args.quantum)
+    out = {"metric": "served solves/s and latency", "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "value": r["best_solves_per_s"],
+           "config": {"workload": "serving: Poisson arrivals, %d requests per rate, axes in {96..256} with 10%% "
+                                  "512x512x256, nt=%d" % (r["requests"], args.nt),
+                      "hbm_budget_gb": args.budget_gb, "quantum_steps": args.quantum,
+                      "points_total": r["points_total"],
+                      "timing": "wall clock from first arrival to last completion, host set-up included"}}
+    out.update({k: v for k, v in r.items() if k not in ("points_total", "hbm_budget_gb", "quantum_steps")})
     print(json.dumps(out), flush=True)
     return 0
+
+
+def precision_block(w, med, ms_fp32, steps=20, warmup=3):
+    """Short precision block of the default run: the headline workload with
+    FP16 memory variables, timed like the headline (graph replay, CUDA events
+    over `steps` steps) against the FP32 step time."""
+    try:
+        import torch
+        sim = build_sim(w, med, w["nt"], store="fp16")
+        st = torch.cuda.ExternalStream(sim.stream())
+        sim.run(1, warmup)
+        sim.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sim.run(warmup + 1, warmup + steps)
+        e1.record(st)
+        e1.synchronize()
+        sim.sync()
+        sim.close()
+        ms = e0.elapsed_time(e1) / steps
+        n_int, n_pml = counts(w)
+        b16, bp, _ = byte_model("fp16")
+        return {"workload": "large single source, FP16 memory variables", "ms_per_step": ms,
+                "updates_per_s": w["nx"] * w["ny"] * w["nz"] / (ms / 1e3), "speedup_vs_fp32": ms_fp32 / ms,
+                "bytes_per_step": b16 * n_int + bp * n_pml,
+                "misfit": "see the precision workload (bench.py --workload precision)"}
+    except Exception as e:
+        return {"error": str(e)}
 
 
 def run_precision(args):
