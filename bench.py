@@ -188,7 +188,8 @@ def source_and_stations(w, kfs, zbeg, seed):
     return src, mij, sta
 
 
-def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None, seed=20261203, pml_points=0):
+def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None, seed=20261203, pml_points=0,
+              pml_fused=None):
     """A simulation of the workload: medium (built on the device or uploaded,
     see make_medium), the moment-tensor source, the receivers and the xy
     velocity snapshot."""
@@ -196,7 +197,7 @@ def build_sim(w, med, nt, store="fp32", ntdec_r=100, variant=0, concurrent=None,
     dims = gpu.make_dims(w["nx"], w["ny"], w["nz"], nt, w["dx"], w["dx"], w["dx"], w["dt"], na=20, store=store,
                          xbeg=-w["nx"] * w["dx"] / 2, ybeg=-w["ny"] * w["dx"] / 2, zbeg=med["zbeg"], fcut=1.0,
                          M0=1e16, UC=1e-15, ntdec_r=ntdec_r, variant=variant, concurrent=concurrent,
-                         pml_points=pml_points)
+                         pml_points=pml_points, pml_fused=pml_fused)
     sim = gpu.Simulation(dims)
     if med["where"] == "device":
         maps, _ = sim.build_medium_rmed(med["bg"], med["xi"], med["kxi0"], fq_min=0.05, fq_max=5.0, fq_ref=1.0)
@@ -409,6 +410,27 @@ def timed_window(w, steps, warmup):
     return 1 + m * nts - steps // 2
 
 
+def interior_tile_points(w, rows, na=20):
+    """Interior points inside the tiles that the interior kernels sweep when
+    the tile kernels sweep the shell too (interior_tiles of kernels_tma.cuh):
+    whole 32-column tiles of the grid shifted so that the interior starts on
+    a tile boundary, whole rows-row tiles from y = 0, the interior's planes."""
+    x0 = y0 = na
+    nxi, nyi, nzi = w["nx"] - 2 * na, w["ny"] - 2 * na, w["nz"] - na
+    tx0 = x0 - 32 * (-(-x0 // 32))
+    bxl, byl = (x0 - tx0 + 31) // 32, (y0 + rows - 1) // rows
+    bxh, byh = max(bxl, (x0 + nxi - tx0) // 32), max(byl, (y0 + nyi) // rows)
+    return (bxh - bxl) * 32 * (byh - byl) * rows * nzi
+
+
+def shell_bytes(sim):
+    """PML shell points and their algorithmic bytes per step in each phase
+    (the per-point figures of pml_class_report, summed over the classes)."""
+    _, _, pts, ax = sim.profile_read_pml()
+    n, a = float(pts.sum()), float(ax.sum())
+    return int(n), {"stress": 68.0 * n + 24.0 * a, "vel": 52.0 * n + 24.0 * a}
+
+
 def pml_class_report(sim, peak):
     """Per launch class of the PML kernels: time per launch and the
     algorithmic bytes of its points.  Per shell point the stress update
@@ -447,7 +469,7 @@ def run_gpu(args, w):
     t_setup = time.time()
     med = make_medium(w, seed, args.medium)
     sim = build_sim(w, med, w["nt"], store=args.store, variant=args.variant, concurrent=args.pml_overlap, seed=seed,
-                    pml_points=args.pml_points)
+                    pml_points=args.pml_points, pml_fused=args.pml_form == "tiles")
     if args.tiles:
         sim.set_tiles(*[int(v) for v in args.tiles.split(",")])
     if args.zchunks:
@@ -485,7 +507,9 @@ def run_gpu(args, w):
     sim.run(it, it + args.steps - 1)
     it += args.steps
     kms, kn = sim.profile_read()
+    fused = sim.pml_fused
     pml = pml_class_report(sim, peak)
+    shell_pts, shell_b = shell_bytes(sim)
     sim_tiles, sim_z = sim.tiles(), sim.zchunks()
     sim.profile(False)
     sim.sync()
@@ -496,22 +520,40 @@ def run_gpu(args, w):
     b_int, b_pml, kbytes = byte_model(args.store)
     step_bytes = b_int * n_int + b_pml * n_pml
     kern = {}
-    for q, nm in enumerate(["stress_interior", "vel_interior"]):
-        t = float(kms[q] / max(kn[q], 1))
-        kern[nm] = {"ms": t, "bytes": kbytes[nm] * n_int, "GBps": kbytes[nm] * n_int / (t / 1e3) / 1e9 if t > 0 else None}
-        kern[nm]["frac"] = kern[nm]["GBps"] / peak if kern[nm]["GBps"] else None
-    kern.update(pml)
+    if fused:
+        # the interior kernels sweep the tiles wholly inside the interior, the
+        # shell-tile kernels the rest: the shell points (bytes as in the
+        # shell launches' accounting, see pml_class_report) and the interior
+        # points of the tiles that straddle the interior's edge
+        for q, (ph, kb, sb, rows) in enumerate((("stress", "stress_interior", "stress", sim_tiles[0]),
+                                                ("vel", "vel_interior", "vel", sim_tiles[1]))):
+            n_it = interior_tile_points(w, rows)
+            for nm, cls, b in ((ph + "_interior", q, kbytes[kb] * n_it),
+                               (ph + "_shell", 2 + q, kbytes[kb] * (n_int - n_it) + shell_b[sb])):
+                t = float(kms[cls] / max(kn[cls], 1))
+                kern[nm] = {"ms": t, "bytes": b, "GBps": b / (t / 1e3) / 1e9 if t > 0 else None}
+                kern[nm]["frac"] = kern[nm]["GBps"] / peak if kern[nm]["GBps"] else None
+            kern[ph + "_interior"]["points"] = n_it
+            kern[ph + "_shell"].update({"shell_points": shell_pts, "interior_points": n_int - n_it})
+        top = "stress_interior"
+    else:
+        for q, nm in enumerate(["stress_interior", "vel_interior"]):
+            t = float(kms[q] / max(kn[q], 1))
+            kern[nm] = {"ms": t, "bytes": kbytes[nm] * n_int,
+                        "GBps": kbytes[nm] * n_int / (t / 1e3) / 1e9 if t > 0 else None}
+            kern[nm]["frac"] = kern[nm]["GBps"] / peak if kern[nm]["GBps"] else None
+        kern.update(pml)
+        top = "stress_interior"
     tot = sum(kern[k]["ms"] for k in kern)
     for k in kern:
         kern[k]["share"] = kern[k]["ms"] / tot if tot > 0 else None
-    top = "stress_interior"
     achieved = kern[top]["GBps"]
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp) and args.store == "fp32" and w is WORKLOADS["large"]:
         try:
             with open(tp) as f:
-                traffic = json.load(f).get(top + "_bytes_per_launch")
+                traffic = json.load(f).get(("fused_" if fused else "") + top + "_bytes_per_launch")
         except Exception:
             traffic = None
     sim.close()
@@ -534,7 +576,7 @@ def run_gpu(args, w):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sim2 = build_sim(w, med_p, args.steps, store=args.store, variant=args.variant, concurrent=args.pml_overlap,
-                         seed=seed, pml_points=args.pml_points)
+                         seed=seed, pml_points=args.pml_points, pml_fused=args.pml_form == "tiles")
         if args.tiles:
             sim2.set_tiles(*[int(v) for v in args.tiles.split(",")])
         if args.zchunks:
@@ -572,7 +614,11 @@ def run_gpu(args, w):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": arm_config(w, args, world),
-            "kernel_shape": {"tiles": list(sim_tiles), "zchunks": list(sim_z), "pml_points": args.pml_points or 1},
+            "kernel_shape": {"tiles": list(sim_tiles), "zchunks": list(sim_z),
+                             "pml_shell": "swept by the tile kernels" if fused else
+                             "own launches, %s" % ({0: "two points per thread for the stress y/z classes, one elsewhere",
+                                                    1: "one point per thread", 2: "two points per thread"}
+                                                   [args.pml_points])},
             "timed_window": "it=%d..%d (graph replay; snapshot frame at it=%s)"
                             % (it - 2 * args.steps, it - args.steps - 1, ",".join(map(str, frames))),
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,
@@ -580,7 +626,7 @@ def run_gpu(args, w):
                                   "model": "%d B/interior pt + %d B/PML pt per step" % (b_int, b_pml)},
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "traffic": traffic,
-                         "bytes_per_point": kbytes[top], "peak_source": peak_kind},
+                         "algorithmic_bytes_per_launch": kern[top]["bytes"], "peak_source": peak_kind},
             "kernels": kern,
             "kernel_timing": "per-launch CUDA events on the simulation's stream over the %d steps after the "
                              "timed region (launched one by one)" % args.steps,
@@ -969,6 +1015,8 @@ def main():
                     help="build the random medium on the GPU (default) or on the host and upload it")
     ap.add_argument("--store", default="fp32", choices=["fp32", "fp16", "bf16"])
     ap.add_argument("--variant", type=int, default=0, help="0: TMA-fed interior kernels, 1: plain smem sweep")
+    ap.add_argument("--pml-form", choices=["launches", "tiles"], default="launches",
+                    help="PML shell in launches of its own, or swept by shell-tile kernels beside the interior ones")
     ap.add_argument("--pml-overlap", type=lambda v: {"auto": None, "on": True, "off": False}[v], default=None,
                     help="auto|on|off: run the PML kernels beside the interior ones")
     args = ap.parse_args()

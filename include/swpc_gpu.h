@@ -80,7 +80,10 @@ typedef struct swpc_dims {
     int reserved[7];     /* 0 (all zero: library defaults); [0] 1 = interior kernels without TMA,
                             [1] 1/2 = PML kernels in series/beside the interior ones,
                             [2] 1/2 = PML shell points per thread (0: two for the stress update
-                            of the y and z classes, one elsewhere) */
+                            of the y and z classes, one elsewhere),
+                            [3] 2 = the TMA tile kernels sweep the PML shell too (interior
+                            kernels over the tiles inside the interior, shell-tile kernels over
+                            the rest; 0 or 1: the shell in launches of its own) */
 } swpc_dims;
 
 /* Create a simulation and allocate its device state on the current CUDA
@@ -290,6 +293,14 @@ int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel);
  * persistent batch form runs 8-row tiles.  No counterpart in the reference. */
 int swpc_gpu_set_tiles(swpc_sim* sim, int rows_stress, int rows_vel);
 int swpc_gpu_get_tiles(swpc_sim* sim, int* rows_stress, int* rows_vel);
+
+/* 1 when the simulation's TMA tile kernels sweep the PML shell too
+ * (swpc_dims.reserved[3] = 2 with a PML and the TMA kernels: per phase one
+ * launch over the tiles inside the interior and one over the tiles that
+ * hold shell points), 0 when the shell runs in launches of its own; < 0 on a
+ * bad handle.  Either form gives the same bits (absorb_p__update_stress /
+ * __update_vel of m_absorb_p.f90:246-317, 429-531). */
+int swpc_gpu_pml_fused(swpc_sim* sim);
 int swpc_gpu_get_zchunks(swpc_sim* sim, int* kstress, int* kvel);
 int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk);
 int swpc_gpu_get_zchunk(swpc_sim* sim);

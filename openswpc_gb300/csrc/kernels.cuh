@@ -60,6 +60,30 @@ struct Coef {
     float dt;
 };
 
+// One box of the PML shell and its compact ADE storage (the shell's layout
+// is described with the PML kernels below).
+struct PmlBox {
+    int x0, y0, z0, nx, ny, nz;
+    int pitch;           // ADE row pitch (= nx: rows stored without padding)
+    int qs;              // stride between the box's nine auxiliary arrays (nx * ny * nz)
+    long long off;       // offset of this box in the ADE buffers (elements)
+};
+
+// The PML shell swept by the TMA tile kernels together with the interior:
+// damping profiles, ADE storage and the five boxes in a fixed order
+// (x < x0, x >= x0 + nxi, y < y0, y >= y0 + nyi, z >= nzi).
+struct PmlShell {
+    const float* prof;  // null: the shell runs in launches of its own
+    float* adeV;
+    float* adeS;
+    int pxc, pxe, pyc, pye, pzc, pze;
+    // damped indices of the six profiles (x centre, x edge, y c, y e, z c,
+    // z e): i is damped (g4 != 0) exactly when i < dlo or i >= dhi
+    int dlo[6], dhi[6];
+    float r20x, r20y, r20z, dt;
+    PmlBox box[5];
+};
+
 // Interior (viscoelastic, 4th-order) sweep arguments.
 struct ZArgs {
     Geo g;
@@ -69,13 +93,17 @@ struct ZArgs {
     void* R;           // memory variables, storage type per template
     const int4* band;  // per interior column: kfs_top, kfs_bot, kob_top, kob_bot (1-based k)
     int x0, y0, nxi, nyi;  // interior box (0-based origin, extent)
-    int kz_end;            // interior planes [0, kz_end)
+    int kz_end;            // planes [0, kz_end) swept by the tile kernels
+    int nzi;               // interior planes [0, nzi)
+    int tx0, ty0;          // origin of the tile grid (the interior's, or left of it when the shell is swept too)
+    int sx, sy;            // extent of the swept box from (tx0, ty0) in x and y (tiles: ceil(sx / 32), ceil(sy / TY))
     int kchunk;            // planes per block in z (stress kernels)
     int kchunk_v;          // planes per block in z (velocity kernels)
     int rpitch;            // R row pitch (elements)
     const float* cer;      // Cerjan profiles (null for PML): xc xb yc yb zc zb, each padded
     int cer_off[6];
     Coef c;
+    PmlShell sh;           // sh.prof null: interior only
 };
 
 // 2nd-order band test of m_kernel.f90:103-111 / 188-196: inside a free-surface
@@ -401,15 +429,11 @@ __global__ void __launch_bounds__(TBX * TBY, 2) k_vel_interior(const ZArgs a) {
 
 // ---------------------------------------------------------------------------
 // PML shell (ADE-CFS, m_absorb_p.f90).  The shell is five boxes; each has its
-// own compact ADE storage [z][y][9][x] for the V-derivative auxiliaries
-// (used by the stress update) and for the S-derivative auxiliaries (used by
-// the velocity update).  One thread per shell point.
+// own compact ADE storage [9][z][y][x] (one array per auxiliary, so the rows
+// of the 20-cell x-side boxes run on without gaps) for the V-derivative
+// auxiliaries (used by the stress update) and for the S-derivative
+// auxiliaries (used by the velocity update).  One thread per shell point.
 // ---------------------------------------------------------------------------
-struct PmlBox {
-    int x0, y0, z0, nx, ny, nz;
-    int pitch;           // ADE row pitch (= nx: rows stored without padding)
-    long long off;       // offset of this box in the ADE buffers (elements)
-};
 
 // threads (shell points) per block of the PML kernels
 #ifndef PML_TPB
@@ -498,6 +522,14 @@ struct PmlSIn {
     float lamv, m000, m100, m010, m110, m001, m011, m101;
     float ad[9], sv[6];
 };
+// the auxiliaries of point L (its profiles and ADE address set)
+__device__ __forceinline__ void stress_pml_aux(PmlSIn& L) {
+    const bool live[9] = {L.gxc.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gye.w != 0.f, L.gze.w != 0.f,
+                          L.gxe.w != 0.f, L.gze.w != 0.f, L.gxe.w != 0.f, L.gye.w != 0.f};
+    const float* __restrict__ A = L.A;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) L.ad[q] = live[q] ? A[(long long)q * L.AP] : 0.f;
+}
 template <int MASK>
 __device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, PmlSIn& L) {
     const PmlBox& B = a.box[c.b];
@@ -509,13 +541,13 @@ __device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, P
     const long long oV = (long long)goff(g, 3, 0, ix, jy, kz);
     const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
     const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
-    const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
+    const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * B.pitch + c.lx;
     const float* __restrict__ V = a.V + oV;
     const float* __restrict__ M = a.M + oM;
     L.S = a.S + oS;
     L.A = a.adeV + oA;
     L.P = P;
-    L.AP = B.pitch;
+    L.AP = B.qs;
     L.gxc = pml_prof<MASK, 0>(a, a.pxc, ix); L.gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
     L.gyc = pml_prof<MASK, 1>(a, a.pyc, jy); L.gye = pml_prof<MASK, 1>(a, a.pye, jy);
     L.gzc = pml_prof<MASK, 2>(a, a.pzc, kz); L.gze = pml_prof<MASK, 2>(a, a.pze, kz);
@@ -530,16 +562,15 @@ __device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, P
     // point lies outside that axis's layer) starts at zero and its update
     // g3 * 0 + 0 keeps it zero: it is neither loaded nor stored.  Order:
     // axVx ayVy azVz ayVx azVx axVy azVy axVz ayVz
-    const bool live[9] = {L.gxc.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gye.w != 0.f, L.gze.w != 0.f,
-                          L.gxe.w != 0.f, L.gze.w != 0.f, L.gxe.w != 0.f, L.gye.w != 0.f};
-    const float* __restrict__ A = L.A;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) L.ad[q] = live[q] ? A[q * L.AP] : 0.f;
+    stress_pml_aux(L);
     const float* __restrict__ S = L.S;
 #pragma unroll
     for (int q = 0; q < 6; ++q) L.sv[q] = S[q * P];
 }
-__device__ __forceinline__ void stress_pml_store(const PArgs& a, const PmlSIn& L) {
+// K: any argument block with dt, r20x, r20y, r20z (the PML launches' or the
+// tile kernels' shell arguments)
+template <class K>
+__device__ __forceinline__ void stress_pml_store(const K& a, const PmlSIn& L) {
     const float eps = 1.1920928955078125e-07f;
     const int P = L.P, AP = L.AP;
     float* __restrict__ S = L.S;
@@ -569,8 +600,8 @@ __device__ __forceinline__ void stress_pml_store(const PArgs& a, const PmlSIn& L
     S[2 * P] = __fmaf_rn(__fmaf_rn(lam2mu, dza, __fmul_rn(lamR, __fadd_rn(dxa, dya))), dt, sv[2]);
     auto ade = [dt](float4 gp, float aux, float d) { return __fmaf_rn(gp.z, aux, __fmul_rn(__fmul_rn(gp.w, d), dt)); };
     if (live[0]) A[0] = ade(gxc, ad[0], dxVx);
-    if (live[1]) A[AP] = ade(gyc, ad[1], dyVy);
-    if (live[2]) A[2 * AP] = ade(gzc, ad[2], dzVz);
+    if (live[1]) A[1LL * AP] = ade(gyc, ad[1], dyVy);
+    if (live[2]) A[2LL * AP] = ade(gzc, ad[2], dzVz);
     // shear part (m_absorb_p.f90:477-518)
     const float dxVy = __fmul_rn(__fsub_rn(L.vye, vy), a.r20x);
     const float dxVz = __fmul_rn(__fsub_rn(L.vze, vz), a.r20x);
@@ -602,12 +633,12 @@ __device__ __forceinline__ void stress_pml_store(const PArgs& a, const PmlSIn& L
     S[3 * P] = __fmaf_rn(__fmul_rn(muyz, sum4(gye, dyVz, gze, dzVy, ayVz, azVy)), dt, sv[3]);
     S[4 * P] = __fmaf_rn(__fmul_rn(muxz, sum4(gxe, dxVz, gze, dzVx, axVz, azVx)), dt, sv[4]);
     S[5 * P] = __fmaf_rn(__fmul_rn(muxy, sum4(gxe, dxVy, gye, dyVx, axVy, ayVx)), dt, sv[5]);
-    if (live[3]) A[3 * AP] = ade(gye, ayVx, dyVx);
-    if (live[4]) A[4 * AP] = ade(gze, azVx, dzVx);
-    if (live[5]) A[5 * AP] = ade(gxe, axVy, dxVy);
-    if (live[6]) A[6 * AP] = ade(gze, azVy, dzVy);
-    if (live[7]) A[7 * AP] = ade(gxe, axVz, dxVz);
-    if (live[8]) A[8 * AP] = ade(gye, ayVz, dyVz);
+    if (live[3]) A[3LL * AP] = ade(gye, ayVx, dyVx);
+    if (live[4]) A[4LL * AP] = ade(gze, azVx, dzVx);
+    if (live[5]) A[5LL * AP] = ade(gxe, axVy, dxVy);
+    if (live[6]) A[6LL * AP] = ade(gze, azVy, dzVy);
+    if (live[7]) A[7LL * AP] = ade(gxe, axVz, dxVz);
+    if (live[8]) A[8LL * AP] = ade(gye, ayVz, dyVz);
 }
 template <int MASK>
 __device__ __forceinline__ void stress_pml_at(const PArgs& a, const PmlPt c) {
@@ -627,6 +658,13 @@ struct PmlVIn {
     float r0, rx, ry, rz;
     float ad[9], v0, v1, v2;
 };
+__device__ __forceinline__ void vel_pml_aux(PmlVIn& L) {
+    const bool live[9] = {L.gxe.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gxc.w != 0.f, L.gye.w != 0.f,
+                          L.gzc.w != 0.f, L.gxc.w != 0.f, L.gyc.w != 0.f, L.gze.w != 0.f};
+    const float* __restrict__ A = L.A;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) L.ad[q] = live[q] ? A[(long long)q * L.AP] : 0.f;
+}
 template <int MASK>
 __device__ __forceinline__ void vel_pml_load(const PArgs& a, const PmlPt c, PmlVIn& L) {
     const PmlBox& B = a.box[c.b];
@@ -638,13 +676,13 @@ __device__ __forceinline__ void vel_pml_load(const PArgs& a, const PmlPt c, PmlV
     const long long oV = (long long)goff(g, 3, 0, ix, jy, kz);
     const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
     const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
-    const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * 9 * B.pitch + c.lx;
+    const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * B.pitch + c.lx;
     const float* __restrict__ S = a.S + oS;
     const float* __restrict__ M = a.M + oM;
     L.V = a.V + oV;
     L.A = a.adeS + oA;
     L.P = P;
-    L.AP = B.pitch;
+    L.AP = B.qs;
     L.gxc = pml_prof<MASK, 0>(a, a.pxc, ix); L.gxe = pml_prof<MASK, 0>(a, a.pxe, ix);
     L.gyc = pml_prof<MASK, 1>(a, a.pyc, jy); L.gye = pml_prof<MASK, 1>(a, a.pye, jy);
     L.gzc = pml_prof<MASK, 2>(a, a.pzc, kz); L.gze = pml_prof<MASK, 2>(a, a.pze, kz);
@@ -656,15 +694,12 @@ __device__ __forceinline__ void vel_pml_load(const PArgs& a, const PmlPt c, PmlV
     L.r0 = M[0]; L.rx = M[1]; L.ry = M[rowM]; L.rz = M[planeM];
     // auxiliaries of undamped axes stay zero (as in the stress update).
     // Order: axSxx aySxy azSxz axSxy aySyy azSyz axSxz aySyz azSzz
-    const bool live[9] = {L.gxe.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gxc.w != 0.f, L.gye.w != 0.f,
-                          L.gzc.w != 0.f, L.gxc.w != 0.f, L.gyc.w != 0.f, L.gze.w != 0.f};
-    const float* __restrict__ A = L.A;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) L.ad[q] = live[q] ? A[q * L.AP] : 0.f;
+    vel_pml_aux(L);
     const float* __restrict__ V = L.V;
     L.v0 = V[0]; L.v1 = V[P]; L.v2 = V[2 * P];
 }
-__device__ __forceinline__ void vel_pml_store(const PArgs& a, const PmlVIn& L) {
+template <class K>
+__device__ __forceinline__ void vel_pml_store(const K& a, const PmlVIn& L) {
     const int P = L.P, AP = L.AP;
     float* __restrict__ V = L.V;
     float* __restrict__ A = L.A;
@@ -703,15 +738,37 @@ __device__ __forceinline__ void vel_pml_store(const PArgs& a, const PmlVIn& L) {
     V[2 * P] = __fmaf_rn(__fmul_rn(bz, sum6(gxc, dxSxz, gyc, dySyz, gze, dzSzz, axSxz, aySyz, azSzz)), dt, L.v2);
     auto ade = [dt](float4 gp, float aux, float d) { return __fmaf_rn(gp.z, aux, __fmul_rn(__fmul_rn(gp.w, d), dt)); };
     if (live[0]) A[0] = ade(gxe, axSxx, dxSxx);
-    if (live[1]) A[AP] = ade(gyc, aySxy, dySxy);
-    if (live[2]) A[2 * AP] = ade(gzc, azSxz, dzSxz);
-    if (live[3]) A[3 * AP] = ade(gxc, axSxy, dxSxy);
-    if (live[4]) A[4 * AP] = ade(gye, aySyy, dySyy);
-    if (live[5]) A[5 * AP] = ade(gzc, azSyz, dzSyz);
-    if (live[6]) A[6 * AP] = ade(gxc, axSxz, dxSxz);
-    if (live[7]) A[7 * AP] = ade(gyc, aySyz, dySyz);
-    if (live[8]) A[8 * AP] = ade(gze, azSzz, dzSzz);
+    if (live[1]) A[1LL * AP] = ade(gyc, aySxy, dySxy);
+    if (live[2]) A[2LL * AP] = ade(gzc, azSxz, dzSxz);
+    if (live[3]) A[3LL * AP] = ade(gxc, axSxy, dxSxy);
+    if (live[4]) A[4LL * AP] = ade(gye, aySyy, dySyy);
+    if (live[5]) A[5LL * AP] = ade(gzc, azSyz, dzSyz);
+    if (live[6]) A[6LL * AP] = ade(gxc, axSxz, dxSxz);
+    if (live[7]) A[7LL * AP] = ade(gyc, aySyz, dySyz);
+    if (live[8]) A[8LL * AP] = ade(gze, azSzz, dzSzz);
 }
+// One component of the velocity shell update (the tile kernels update the
+// three components one after the other):
+// V = v0 + b (p.x d1 + q.x d2 + r.x d3 + p.y a1 + q.y a2 + r.y a3) dt, with
+// the auxiliaries a1..a3 (arrays q1..q3 of A; zero where g4 of their profile
+// is zero, and then neither stored) advanced as in vel_pml_store, whose
+// operations and order this repeats bit for bit.
+__device__ __forceinline__ void vel_pml_component(float dt, float4 p, float d1, float4 q, float d2, float4 r, float d3,
+                                                  float a1, float a2, float a3, float* __restrict__ A, long long AP,
+                                                  int q1, int q2, int q3, float b, float v0, float* __restrict__ out) {
+    float t = __fmul_rn(p.x, d1);
+    t = __fmaf_rn(q.x, d2, t);
+    t = __fmaf_rn(r.x, d3, t);
+    t = __fmaf_rn(p.y, a1, t);
+    t = __fmaf_rn(q.y, a2, t);
+    t = __fmaf_rn(r.y, a3, t);
+    *out = __fmaf_rn(__fmul_rn(b, t), dt, v0);
+    auto ade = [dt](float4 gp, float aux, float d) { return __fmaf_rn(gp.z, aux, __fmul_rn(__fmul_rn(gp.w, d), dt)); };
+    if (p.w != 0.f) A[q1 * AP] = ade(p, a1, d1);
+    if (q.w != 0.f) A[q2 * AP] = ade(q, a2, d2);
+    if (r.w != 0.f) A[q3 * AP] = ade(r, a3, d3);
+}
+
 template <int MASK>
 __device__ __forceinline__ void vel_pml_at(const PArgs& a, const PmlPt c) {
     PmlVIn L;

@@ -122,11 +122,129 @@ static_assert(sizeof(Slot3<float, TTY + 4, 6, 40>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot3<float, 17, 4, 36>) % 128 == 0 && sizeof(Slot2<float, 17, 36>) % 128 == 0, "slot size");
 static_assert(sizeof(StressSmem<float, 16>) <= 227 * 1024 && sizeof(VelSmem<16>) <= 227 * 1024, "16-row rings fit");
 
+// Shell-tile kernels: the auxiliaries of every thread's shell point staged one
+// plane ahead by cp.async (nine words per thread), after the rings.
+template <int TY> struct AuxStage { float a[9][32 * TY]; };
+template <class RT, int TY, bool SHELL> struct StressSm : StressSmem<RT, TY> {};
+template <class RT, int TY> struct StressSm<RT, TY, true> : StressSmem<RT, TY> { AuxStage<TY> aux; };
+template <int TY, bool SHELL> struct VelSm : VelSmem<TY> {};
+template <int TY> struct VelSm<TY, true> : VelSmem<TY> { AuxStage<TY> aux; };
+// blocks per SM of the shell-tile kernels (8-row tiles; 16-row tiles one)
+template <int TY> struct ShellOcc { static constexpr int stress = 2, vel = 2; };
+template <> struct ShellOcc<16> { static constexpr int stress = 1, vel = 1; };
+static_assert(2 * sizeof(StressSm<float, 8, true>) <= 226 * 1024 && 2 * sizeof(VelSm<8, true>) <= 226 * 1024,
+              "two shell-tile blocks fit on an SM");
+
+// 4-byte asynchronous copy global -> shared; with `read` false the word is
+// zero-filled and the source is not read
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool read) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(read ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Damped flags of index i for the profiles of PmlShell: bit p set when
+// profile p (x centre, x edge, y c, y e, z c, z e) damps i.
+__device__ __forceinline__ int damped_bit(const PmlShell& sh, int p, int i) {
+    return (i < sh.dlo[p] || i >= sh.dhi[p]) ? (1 << p) : 0;
+}
+// the profile (bit of the flags above) whose g4 keeps auxiliary q live, in
+// the auxiliary order of the stress update (axVx ayVy azVz ayVx azVx axVy
+// azVy axVz ayVz) and of the velocity update (axSxx aySxy azSxz axSxy aySyy
+// azSyz axSxz aySyz azSzz)
+__host__ __device__ constexpr int aux_prof(bool vel, int q) {
+    return vel ? (q == 0 ? 1 : q == 1 ? 2 : q == 2 ? 4 : q == 3 ? 0 : q == 4 ? 3 : q == 5 ? 4 : q == 6 ? 0 : q == 7 ? 2 : 5)
+               : (q == 0 ? 0 : q == 1 ? 2 : q == 2 ? 4 : q == 3 ? 3 : q == 4 ? 5 : q == 5 ? 1 : q == 6 ? 5 : q == 7 ? 1 : 3);
+}
+// Stage the nine auxiliaries of a shell point (ADE address A, stride qs)
+// with damped flags fl into the thread's slots: dead ones as zeros.
+template <bool VEL, int TY>
+__device__ __forceinline__ void stage_aux(AuxStage<TY>& st, int tid, const float* A, long long qs, int fl) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) cp_async4(&st.a[q][tid], A + q * qs, (fl >> aux_prof(VEL, q)) & 1);
+    cp_async_commit();
+}
+
+// The tiles of a sweep grid run by the interior kernels: with the shell
+// swept too, the tiles whose columns all lie inside the interior box (the
+// others go to the shell-tile kernels); without, every tile of the interior
+// box, the last ones partly filled.
+__host__ __device__ inline void interior_tiles(const ZArgs& a, int TY, int& bxl, int& bxh, int& byl, int& byh) {
+    if (a.sh.prof) {
+        bxl = (a.x0 - a.tx0 + 31) / 32;
+        bxh = max(bxl, (a.x0 + a.nxi - a.tx0) / 32);
+        byl = (a.y0 - a.ty0 + TY - 1) / TY;
+        byh = max(byl, (a.y0 + a.nyi - a.ty0) / TY);
+    } else {
+        bxl = 0;
+        bxh = (a.nxi + 31) / 32;
+        byl = 0;
+        byh = (a.nyi + TY - 1) / TY;
+    }
+}
+// end of the z chunk that starts at kz0 (chunks never cross the interior's
+// last plane)
+__host__ __device__ inline int chunk_end(const ZArgs& a, int kz0, int kc) {
+    return min(kz0 + kc, kz0 < a.nzi ? a.nzi : a.kz_end);
+}
+
+// The shell tiles of a sweep over the shell too, for chunks of kc planes:
+// over the interior's chunks every tile outside interior_tiles (rows above,
+// the left and right edge tiles of the middle rows, rows below), then every
+// tile over the chunks of the planes below the interior.  Tile L of that list
+// -> (bx, by, kz0); the count of the list.
+__host__ __device__ inline int shell_tile_count(const ZArgs& a, int TY, int kc) {
+    if (!a.sh.prof) return 0;
+    int bxl, bxh, byl, byh;
+    interior_tiles(a, TY, bxl, bxh, byl, byh);
+    const int ntx = (a.sx + 31) / 32, nty = (a.sy + TY - 1) / TY;
+    const int edge = ntx * nty - (bxh - bxl) * (byh - byl);
+    const int nci = (a.nzi + kc - 1) / kc, ncz = (a.kz_end - a.nzi + kc - 1) / kc;
+    return nci * edge + ncz * ntx * nty;
+}
+__host__ __device__ inline void shell_tile(const ZArgs& a, int TY, int kc, int L, int& bx, int& by, int& kz0) {
+    int bxl, bxh, byl, byh;
+    interior_tiles(a, TY, bxl, bxh, byl, byh);
+    const int ntx = (a.sx + 31) / 32, nty = (a.sy + TY - 1) / TY;
+    const int edge = ntx * nty - (bxh - bxl) * (byh - byl);
+    const int nci = (a.nzi + kc - 1) / kc;
+    if (L < nci * edge) {
+        const int c = L / edge;
+        int r = L - c * edge;
+        kz0 = c * kc;
+        const int top = byl * ntx;
+        if (r < top) {
+            by = r / ntx;
+            bx = r - by * ntx;
+            return;
+        }
+        r -= top;
+        const int w = ntx - (bxh - bxl), mid = (byh - byl) * w;
+        if (r < mid) {
+            const int q = r / w, e = r - q * w;
+            by = byl + q;
+            bx = e < bxl ? e : bxh + (e - bxl);
+            return;
+        }
+        r -= mid;
+        by = byh + r / ntx;
+        bx = r - (r / ntx) * ntx;
+        return;
+    }
+    L -= nci * edge;
+    const int c = L / (ntx * nty), r = L - c * (ntx * nty);
+    kz0 = a.nzi + c * kc;
+    by = r / ntx;
+    bx = r - by * ntx;
+}
+
 // Start-up check of a TMA destination (128-byte boundary) and of the
-// innermost box coordinate (a multiple of 16 bytes); a block that fails it
-// issues no copy at all.
+// innermost box coordinate (a multiple of 16 bytes; the edge tiles of a
+// sweep over the PML shell load from x < 0, which the copy fills with zeros);
+// a block that fails it issues no copy at all.
 __device__ __forceinline__ bool tma_ok(const void* dst, int x, int esize) {
-    return (smem_u32(dst) & 127u) == 0 && ((x * esize) & 15) == 0 && x >= 0;
+    return (smem_u32(dst) & 127u) == 0 && ((x * esize) & 15) == 0;
 }
 
 // Position of a plane in a ring of N slots that is filled in plane order:
@@ -154,32 +272,52 @@ struct FillLog {
     }
 };
 
+// Column (ix, jy) of a tile: interior, PML shell (inside the grid, outside
+// the interior box; only when the tile kernels sweep the shell) or neither,
+// and the shell box holding its ADE storage (box 4, the z layer below the
+// interior, for an interior column).
+struct ShellCol {
+    bool interior, shell;
+    int box;
+};
+__device__ __forceinline__ ShellCol shell_col(const ZArgs& a, int ix, int jy) {
+    ShellCol c;
+    const bool inx = ix >= a.x0 && ix < a.x0 + a.nxi, iny = jy >= a.y0 && jy < a.y0 + a.nyi;
+    c.interior = inx && iny;
+    c.shell = a.sh.prof != nullptr && !c.interior && ix >= 0 && ix < a.g.nx && jy >= 0 && jy < a.g.ny;
+    c.box = ix < a.x0 ? 0 : ix >= a.x0 + a.nxi ? 1 : jy < a.y0 ? 2 : jy >= a.y0 + a.nyi ? 3 : 4;
+    return c;
+}
+
 // ---------------------------------------------------------------------------
 // Interior stress update (m_kernel.f90:142-348), TMA pipeline.
 //   R+S ring: 2 planes (k, k+1 in flight)
 //   M ring:   3 planes (k, k+1 for mu(k+1), k+2 in flight)
 //   V ring:   6 planes (k-2 .. k+2 for the z stencil, k+3 in flight)
 // ---------------------------------------------------------------------------
-// One 32 x TTY column tile and z chunk (bx, by, bz) of one simulation; `ta`
-// lives in kernel parameter space (single simulation) or in global memory
-// (batched launch).
+// One 32 x TY column tile (bx, by) of the sweep grid and the z chunk that
+// starts at plane kz0, of one simulation; `ta` lives in kernel parameter
+// space (single simulation) or in global memory (batched launch).  SHELL:
+// the tile may hold PML shell points (shell-tile kernels), updated as in the
+// shell launches from the same staged planes, with their auxiliaries staged
+// one plane ahead.
 // Returns whether the block initialised its mbarriers (a caller that reuses
 // the shared memory for other work invalidates them first).
-template <class RT, int TY = TTY>
-__device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
+template <class RT, int TY = TTY, bool SHELL = false>
+__device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, const int by, const int kz0) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    StressSmem<RT, TY>& sm = *reinterpret_cast<StressSmem<RT, TY>*>(smraw);
+    StressSm<RT, TY, SHELL>& sm = *reinterpret_cast<StressSm<RT, TY, SHELL>*>(smraw);
     int& bad = sm.bad;
     const ZArgs& a = ta.z;
     const Coef cf = a.c;
     const Geo& g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TY;
+    const int xt = a.tx0 + bx * 32, yt = a.ty0 + by * TY;
     const int ix = xt + tx, jy = yt + ty;
-    const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
-    const int kz0 = bz * a.kchunk;
-    const int kz1 = min(kz0 + a.kchunk, a.kz_end);
-    if (kz0 >= kz1) return false;
+    const ShellCol sc = shell_col(a, ix, jy);
+    const bool act = sc.interior;
+    const int kz1 = chunk_end(a, kz0, a.kchunk);
+    if (kz0 >= kz1 || kz0 < 0) return false;
 
     constexpr uint32_t BR = sizeof(RT) * TY * 18 * 32, BS = 4 * TY * 6 * 32;
     constexpr uint32_t BM = 4 * (TY + 1) * 4 * 36, BV = 4 * (TY + 4) * 3 * 40;
@@ -250,6 +388,27 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
     RT* __restrict__ Rg = (RT*)a.R;
     const int P = g.pitch;
 
+    // shell point of this thread in the chunk (a chunk never crosses the
+    // interior's last plane, so a thread is a shell point on every plane of
+    // its chunk or on none): ADE column, damped flags, auxiliaries of the
+    // first plane staged
+    const bool shl = SHELL && (sc.shell || (act && kz0 >= a.nzi));
+    const float* Ab = nullptr;
+    long long aqs = 0, apl = 0;
+    int az0 = 0, fxy = 0;
+    if constexpr (SHELL) {
+        if (shl) {
+            const PmlBox& B = a.sh.box[sc.box];
+            Ab = a.sh.adeV + B.off + (long long)(jy - B.y0) * B.pitch + (ix - B.x0);
+            aqs = B.qs;
+            apl = (long long)B.ny * B.pitch;
+            az0 = B.z0;
+            fxy = damped_bit(a.sh, 0, ix) | damped_bit(a.sh, 1, ix) | damped_bit(a.sh, 2, jy) | damped_bit(a.sh, 3, jy);
+            stage_aux<false, TY>(sm.aux, tid, Ab + (kz0 - az0) * apl, aqs,
+                                 fxy | damped_bit(a.sh, 4, kz0) | damped_bit(a.sh, 5, kz0));
+        }
+    }
+
     // consumer ring positions: R+S of plane k, M of plane k+1, V of plane k+2;
     // the slots of M(k) and of V(k-2 .. k+1) ride along
     RingPos<2> cRS{0, 0u};
@@ -266,13 +425,13 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
         if (!ok) bad = 1;
         const int sRS = cRS.slot, sM1 = cM1.slot;
         sV[4] = cV2.slot;
-        if (act && ok) {
+        const int lx = tx + 4, ly = ty + 2;
+        if (act && !shl && ok) {
             const int kk = k + 1;
             const bool nb = in_band(kk, band);
             const float e40x = nb ? cf.e2x : cf.e4x0, e41x = nb ? 0.f : cf.e4x1;
             const float e40y = nb ? cf.e2y : cf.e4y0, e41y = nb ? 0.f : cf.e4y1;
             const float e40z = nb ? cf.e2z : cf.e4z0, e41z = nb ? 0.f : cf.e4z1;
-            const int lx = tx + 4, ly = ty + 2;
             // V(k) plane tile: [y][c][x]
             float (*Vk)[3][40] = sm.V[sV[2]].d;
             auto X = [&](int dy, int dx) { return Vk[ly + dy][0][lx + dx]; };
@@ -361,6 +520,43 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
 #pragma unroll
             for (int f = 0; f < 18; ++f) St<RT>::st(Rg + oR + (long long)f * a.rpitch, r[f]);
         }
+        if constexpr (SHELL) {
+            if (shl && ok) {
+                // PML shell point (m_absorb_p.f90:429-531): the same
+                // explicitly rounded update as the shell launches, from the
+                // staged tiles and auxiliaries
+                const PmlShell& sh = a.sh;
+                PmlSIn L;
+                L.S = Sg + bS + k * planeS;
+                L.P = P;
+                L.A = const_cast<float*>(Ab) + (k - az0) * apl;
+                L.AP = (int)aqs;
+                L.gxc = ld4(sh.prof + sh.pxc + 4 * ix); L.gxe = ld4(sh.prof + sh.pxe + 4 * ix);
+                L.gyc = ld4(sh.prof + sh.pyc + 4 * jy); L.gye = ld4(sh.prof + sh.pye + 4 * jy);
+                L.gzc = ld4(sh.prof + sh.pzc + 4 * k); L.gze = ld4(sh.prof + sh.pze + 4 * k);
+                float (*Vk)[3][40] = sm.V[sV[2]].d;
+                L.vx = Vk[ly][0][lx]; L.vy = Vk[ly][1][lx]; L.vz = Vk[ly][2][lx];
+                L.vxw = Vk[ly][0][lx - 1]; L.vys = Vk[ly - 1][1][lx]; L.vzu = sm.V[sV[1]].d[ly][2][lx];
+                L.vye = Vk[ly][1][lx + 1]; L.vze = Vk[ly][2][lx + 1];
+                L.vxn = Vk[ly + 1][0][lx]; L.vzn = Vk[ly + 1][2][lx];
+                L.vxd = sm.V[sV[3]].d[ly][0][lx]; L.vyd = sm.V[sV[3]].d[ly][1][lx];
+                float (*M0)[4][36] = sm.M[sM0].d;
+                float (*M1)[4][36] = sm.M[sM1].d;
+                L.lamv = M0[ty][0][tx]; L.m000 = M0[ty][1][tx]; L.m100 = M1[ty][1][tx]; L.m010 = M0[ty][1][tx + 1];
+                L.m110 = M1[ty][1][tx + 1]; L.m001 = M0[ty + 1][1][tx]; L.m011 = M0[ty + 1][1][tx + 1];
+                L.m101 = M1[ty + 1][1][tx];
+#pragma unroll
+                for (int q = 0; q < 6; ++q) L.sv[q] = sm.S[sRS].d[ty][q][tx];
+                cp_async_wait_all();
+#pragma unroll
+                for (int q = 0; q < 9; ++q) L.ad[q] = sm.aux.a[q][tid];
+                stress_pml_store(sh, L);
+                // the stores above used every staged word: refill for k + 1
+                if (k + 1 < kz1)
+                    stage_aux<false, TY>(sm.aux, tid, Ab + (k + 1 - az0) * apl, aqs,
+                                         fxy | damped_bit(sh, 4, k + 1) | damped_bit(sh, 5, k + 1));
+            }
+        }
         __syncthreads();  // every thread is done with R/S(k), M(k), V(k-2)
         if (bad) break;
         if (tid == 0) {
@@ -375,6 +571,7 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
         for (int q = 0; q < 4; ++q) sV[q] = sV[q + 1];
         cV2.advance();
     }
+    if constexpr (SHELL) cp_async_wait_all();  // no staged copy outlives the block
     if (bad && tid == 0) {
         atomicExch(ta.err, 1);
         // drain this block's copies still in flight (bounded)
@@ -385,6 +582,47 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
     return true;
 }
 
+// PML shell point of the velocity tile (m_absorb_p.f90:246-317): the
+// operations of the shell launches, one component at a time, from the
+// staged plane k (Sk), the point's Sxz, Syz at k - 1 and Szz at k + 1, and
+// its staged auxiliaries aux[q * stride] (ADE address A, stride AP).
+__device__ __forceinline__ void vel_shell_point(const PmlShell& sh, int ix, int jy, int k, int tx, int ty,
+                                             float (*Sk)[6][40], float sxz_u, float syz_u, float szz_d,
+                                             float (*R0)[36], float (*R1)[36], float (*Vk)[3][32], float* Vo, int P,
+                                             const float* aux, int stride, float* A, long long AP) {
+    const int lx = tx + 4, ly = ty + 2;
+    const float r0 = R0[ty][tx];
+    const float4 gxc = ld4(sh.prof + sh.pxc + 4 * ix), gyc = ld4(sh.prof + sh.pyc + 4 * jy);
+    const float4 gzc = ld4(sh.prof + sh.pzc + 4 * k);
+    {
+        const float4 gxe = ld4(sh.prof + sh.pxe + 4 * ix);
+        const float dxSxx = __fmul_rn(__fsub_rn(Sk[ly][0][lx + 1], Sk[ly][0][lx]), sh.r20x);
+        const float dySxy = __fmul_rn(__fsub_rn(Sk[ly][5][lx], Sk[ly - 1][5][lx]), sh.r20y);
+        const float dzSxz = __fmul_rn(__fsub_rn(Sk[ly][4][lx], sxz_u), sh.r20z);
+        const float b = __fdiv_rn(2.f, __fadd_rn(r0, R0[ty][tx + 1]));
+        vel_pml_component(sh.dt, gxe, dxSxx, gyc, dySxy, gzc, dzSxz, aux[0], aux[stride], aux[2 * stride], A, AP, 0,
+                          1, 2, b, Vk[ty][0][tx], Vo);
+    }
+    {
+        const float4 gye = ld4(sh.prof + sh.pye + 4 * jy);
+        const float dxSxy = __fmul_rn(__fsub_rn(Sk[ly][5][lx], Sk[ly][5][lx - 1]), sh.r20x);
+        const float dySyy = __fmul_rn(__fsub_rn(Sk[ly + 1][1][lx], Sk[ly][1][lx]), sh.r20y);
+        const float dzSyz = __fmul_rn(__fsub_rn(Sk[ly][3][lx], syz_u), sh.r20z);
+        const float b = __fdiv_rn(2.f, __fadd_rn(r0, R0[ty + 1][tx]));
+        vel_pml_component(sh.dt, gxc, dxSxy, gye, dySyy, gzc, dzSyz, aux[3 * stride], aux[4 * stride],
+                          aux[5 * stride], A, AP, 3, 4, 5, b, Vk[ty][1][tx], Vo + P);
+    }
+    {
+        const float4 gze = ld4(sh.prof + sh.pze + 4 * k);
+        const float dxSxz = __fmul_rn(__fsub_rn(Sk[ly][4][lx], Sk[ly][4][lx - 1]), sh.r20x);
+        const float dySyz = __fmul_rn(__fsub_rn(Sk[ly][3][lx], Sk[ly - 1][3][lx]), sh.r20y);
+        const float dzSzz = __fmul_rn(__fsub_rn(szz_d, Sk[ly][2][lx]), sh.r20z);
+        const float b = __fdiv_rn(2.f, __fadd_rn(r0, R1[ty][tx]));
+        vel_pml_component(sh.dt, gxc, dxSxz, gyc, dySyz, gze, dzSzz, aux[6 * stride], aux[7 * stride],
+                          aux[8 * stride], A, AP, 6, 7, 8, b, Vk[ty][2][tx], Vo + 2 * P);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Interior velocity update (m_kernel.f90:75-140), TMA pipeline.
 //   S ring:   VRING planes (k .. k+2 live, k+3 .. k+VRING-1 in flight; the
@@ -392,21 +630,21 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
 //   rho ring: 3 planes (k, k+1, k+2 in flight)
 //   V ring:   4 planes (k, k+1 .. k+3 in flight)
 // ---------------------------------------------------------------------------
-template <int TY = TTY>
-__device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, const int by, const int bz) {
+template <int TY = TTY, bool SHELL = false>
+__device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, const int by, const int kz0) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    VelSmem<TY>& sm = *reinterpret_cast<VelSmem<TY>*>(smraw);
+    VelSm<TY, SHELL>& sm = *reinterpret_cast<VelSm<TY, SHELL>*>(smraw);
     int& bad = sm.bad;
     const ZArgs& a = ta.z;
     const Coef cf = a.c;
     const Geo& g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int xt = a.x0 + bx * 32, yt = a.y0 + by * TY;
+    const int xt = a.tx0 + bx * 32, yt = a.ty0 + by * TY;
     const int ix = xt + tx, jy = yt + ty;
-    const bool act = (ix < a.x0 + a.nxi) && (jy < a.y0 + a.nyi);
-    const int kz0 = bz * a.kchunk_v;
-    const int kz1 = min(kz0 + a.kchunk_v, a.kz_end);
-    if (kz0 >= kz1) return false;
+    const ShellCol sc = shell_col(a, ix, jy);
+    const bool act = sc.interior;
+    const int kz1 = chunk_end(a, kz0, a.kchunk_v);
+    if (kz0 >= kz1 || kz0 < 0) return false;
 
     constexpr uint32_t BSH = 4 * (TY + 4) * 6 * 40, BRHO = 4 * (TY + 1) * 36, BVC = 4 * TY * 3 * 32;
     if (tid == 0) {
@@ -471,6 +709,24 @@ __device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, cons
     float* __restrict__ Vg = a.V;
     const int P = g.pitch;
 
+    // shell point of this thread in the chunk, as in the stress tile
+    const bool shl = SHELL && (sc.shell || (act && kz0 >= a.nzi));
+    float* Ab = nullptr;
+    long long aqs = 0, apl = 0;
+    int az0 = 0, fxy = 0;
+    if constexpr (SHELL) {
+        if (shl) {
+            const PmlBox& B = a.sh.box[sc.box];
+            Ab = a.sh.adeS + B.off + (long long)(jy - B.y0) * B.pitch + (ix - B.x0);
+            aqs = B.qs;
+            apl = (long long)B.ny * B.pitch;
+            az0 = B.z0;
+            fxy = damped_bit(a.sh, 0, ix) | damped_bit(a.sh, 1, ix) | damped_bit(a.sh, 2, jy) | damped_bit(a.sh, 3, jy);
+            stage_aux<true, TY>(sm.aux, tid, Ab + (kz0 - az0) * apl, aqs,
+                                fxy | damped_bit(a.sh, 4, kz0) | damped_bit(a.sh, 5, kz0));
+        }
+    }
+
     // consumer positions: S of plane k+2 (slots of k-2 .. k+1 ride along),
     // rho of plane k+1 (slot of rho(k) rides along), V of plane k
     RingPos<VRING> cS2{4, 0u};
@@ -509,7 +765,7 @@ __device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, cons
         sS[4] = cS2.slot;
         const int sM1 = cM1.slot;
         czz[3] = sm.S[sS[4]].d[ly][2][lx];
-        if (act && ok) {
+        if (act && !shl && ok) {
             const int kk = k + 1;
             const bool nb = in_band(kk, band);
             const float e40x = nb ? cf.e2x : cf.e4x0, e41x = nb ? 0.f : cf.e4x1;
@@ -550,6 +806,20 @@ __device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, cons
             const long long oV = bV + k * planeV;
             Vg[oV] = vx; Vg[oV + P] = vy; Vg[oV + 2 * P] = vz;
         }
+        if constexpr (SHELL) {
+            if (shl && ok) {
+                // the z neighbours come from the rolled columns: the slots of
+                // planes below k are refilled early at the start of a chunk
+                cp_async_wait_all();
+                vel_shell_point(a.sh, ix, jy, k, tx, ty, sm.S[sS[2]].d, cxz[1], cyz[1], czz[2], sm.M[sM0].d,
+                                sm.M[sM1].d, sm.V[cV.slot].d, Vg + bV + k * planeV, P, &sm.aux.a[0][tid], 32 * TY,
+                                Ab + (k - az0) * apl, aqs);
+                // every staged word went into the stores above: refill for k + 1
+                if (k + 1 < kz1)
+                    stage_aux<true, TY>(sm.aux, tid, Ab + (k + 1 - az0) * apl, aqs,
+                                        fxy | damped_bit(a.sh, 4, k + 1) | damped_bit(a.sh, 5, k + 1));
+            }
+        }
         __syncthreads();  // every thread is done with S(k), rho(k), V(k)
         if (bad) break;
         if (tid == 0) {
@@ -572,6 +842,7 @@ __device__ __forceinline__ bool vel_tma_tile(const TArgs& ta, const int bx, cons
         cM1.advance();
         cV.advance();
     }
+    if constexpr (SHELL) cp_async_wait_all();  // no staged copy outlives the block
     if (bad && tid == 0) {
         atomicExch(ta.err, 1);
         lS.drain(sm.barS, VRING);
@@ -603,16 +874,39 @@ __device__ __forceinline__ void grouped_tile(int L, int tx, int ty, int nzc, int
     by = g * STRESS_YGROUP + r2 / tx;
     bx = r2 - (r2 / tx) * tx;
 }
+// Interior kernels: the tiles of interior_tiles over the interior's chunks
+// (stress in the grouped order, velocity in a 3-D grid).
 template <class RT, int TY = TTY>
 __global__ void __launch_bounds__(32 * TY, TileOcc<TY>::stress) k_stress_tma(const __grid_constant__ TArgs ta) {
     const ZArgs& a = ta.z;
+    int bxl, bxh, byl, byh;
+    interior_tiles(a, TY, bxl, bxh, byl, byh);
+    const int ntx = bxh - bxl, nty = byh - byl, ntz = (a.nzi + a.kchunk - 1) / a.kchunk;
+    if ((int)blockIdx.x >= ntx * nty * ntz) return;
     int bx, by, bz;
-    grouped_tile(blockIdx.x, (a.nxi + 31) / 32, (a.nyi + TY - 1) / TY, (a.kz_end + a.kchunk - 1) / a.kchunk, bx, by, bz);
-    stress_tma_tile<RT, TY>(ta, bx, by, bz);
+    grouped_tile(blockIdx.x, ntx, nty, ntz, bx, by, bz);
+    stress_tma_tile<RT, TY, false>(ta, bxl + bx, byl + by, bz * a.kchunk);
 }
 template <int TY = TTY>
 __global__ void __launch_bounds__(32 * TY, TileOcc<TY>::vel) k_vel_tma(const __grid_constant__ TArgs ta) {
-    vel_tma_tile<TY>(ta, blockIdx.x, blockIdx.y, blockIdx.z);
+    int bxl, bxh, byl, byh;
+    interior_tiles(ta.z, TY, bxl, bxh, byl, byh);
+    vel_tma_tile<TY, false>(ta, bxl + blockIdx.x, byl + blockIdx.y, blockIdx.z * ta.z.kchunk_v);
+}
+// Shell-tile kernels: block b sweeps tile b of the shell_tile list.
+template <class RT, int TY = TTY>
+__global__ void __launch_bounds__(32 * TY, ShellOcc<TY>::stress) k_stress_tma_shell(const __grid_constant__ TArgs ta) {
+    if ((int)blockIdx.x >= shell_tile_count(ta.z, TY, ta.z.kchunk)) return;
+    int bx, by, kz0;
+    shell_tile(ta.z, TY, ta.z.kchunk, blockIdx.x, bx, by, kz0);
+    stress_tma_tile<RT, TY, true>(ta, bx, by, kz0);
+}
+template <int TY = TTY>
+__global__ void __launch_bounds__(32 * TY, ShellOcc<TY>::vel) k_vel_tma_shell(const __grid_constant__ TArgs ta) {
+    if ((int)blockIdx.x >= shell_tile_count(ta.z, TY, ta.z.kchunk_v)) return;
+    int bx, by, kz0;
+    shell_tile(ta.z, TY, ta.z.kchunk_v, blockIdx.x, bx, by, kz0);
+    vel_tma_tile<TY, true>(ta, bx, by, kz0);
 }
 
 // Self-test of the bounded wait: an mbarrier that expects one arrival which
@@ -629,8 +923,7 @@ __global__ void k_wait_selftest(int* err) {
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
 }
 
-// Batched launches: block b works on tile (e.y, e.z, e.w) of simulation e.x,
-// with e = blocks[b]; every simulation's tensor maps live in `all` (global
+// Batched launches: every simulation's tensor maps live in `all` (global
 // memory, 128-byte aligned).
 // The tables were written by host copies, so the issuing thread makes the
 // tensor maps visible to the TMA unit with a system-scope tensormap-proxy
@@ -649,19 +942,21 @@ __device__ __forceinline__ void tmaps_acquire(const TArgs& t) {
         tmap_acquire(&t.tmVc);
     }
 }
-template <class RT, int TY = TTY>
-__global__ void __launch_bounds__(32 * TY, TileOcc<TY>::stress) k_stress_tma_batch(const TArgs* __restrict__ all,
-                                                                                  const int4* __restrict__ blocks) {
+// Batched launches: block b sweeps tile (e.y, e.z) of simulation e.x over
+// the chunk that starts at plane e.w, e = blocks[b]; SHELL: the shell tiles.
+template <class RT, int TY = TTY, bool SHELL = false>
+__global__ void __launch_bounds__(32 * TY, SHELL ? ShellOcc<TY>::stress : TileOcc<TY>::stress)
+    k_stress_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
     const int4 e = blocks[blockIdx.x];
     tmaps_acquire(all[e.x]);
-    stress_tma_tile<RT, TY>(all[e.x], e.y, e.z, e.w);
+    stress_tma_tile<RT, TY, SHELL>(all[e.x], e.y, e.z, e.w);
 }
-template <int TY = TTY>
-__global__ void __launch_bounds__(32 * TY, TileOcc<TY>::vel) k_vel_tma_batch(const TArgs* __restrict__ all,
-                                                                            const int4* __restrict__ blocks) {
+template <int TY = TTY, bool SHELL = false>
+__global__ void __launch_bounds__(32 * TY, SHELL ? ShellOcc<TY>::vel : TileOcc<TY>::vel)
+    k_vel_tma_batch(const TArgs* __restrict__ all, const int4* __restrict__ blocks) {
     const int4 e = blocks[blockIdx.x];
     tmaps_acquire(all[e.x]);
-    vel_tma_tile<TY>(all[e.x], e.y, e.z, e.w);
+    vel_tma_tile<TY, SHELL>(all[e.x], e.y, e.z, e.w);
 }
 
 }  // namespace swpc

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS, 2) k_batch_persistent(const _
             }
             case IT_STRESS: {
                 tmaps_acquire(P.targs[m]);
-                const bool bars = stress_tma_tile<RT, TTY>(P.targs[m], it.y, it.z, it.w);
+                const bool bars = stress_tma_tile<RT, TTY, false>(P.targs[m], it.y, it.z, it.w);
                 __syncthreads();
                 if (bars && tid == 0) inval_stress_bars<RT>();
                 break;
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(PERSIST_THREADS, 2) k_batch_persistent(const _
             }
             case IT_VEL: {
                 tmaps_acquire(P.targs[m]);
-                const bool bars = vel_tma_tile<TTY>(P.targs[m], it.y, it.z, it.w);
+                const bool bars = vel_tma_tile<TTY, false>(P.targs[m], it.y, it.z, it.w);
                 __syncthreads();
                 if (bars && tid == 0) inval_vel_bars();
                 break;

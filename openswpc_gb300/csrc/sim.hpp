@@ -52,8 +52,11 @@ struct Sim {
     int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
     int ty_s = TTY, ty_v = TTY;  // tile rows of the stress and velocity TMA kernels (8 or 16)
     int pml_np = 0;              // shell points per thread of the PML kernels (1, 2; 0: by launch class)
+    bool pml_fused = false;      // the TMA tile kernels sweep the PML shell (interior and shell-tile kernels)
+    int shell_dlo[6] = {}, shell_dhi[6] = {};  // damped index runs of the six profiles (PmlShell::dlo, dhi)
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)
     size_t smem_stress = 0, smem_vel = 0;
+    size_t smem_stress_sh = 0, smem_vel_sh = 0;  // shell-tile kernels (rings + staged auxiliaries)
 
     PArgs pml_args{};                 // pointers, profiles and boxes of the PML kernels
     PArgs pml_cls[PML_NCLASS]{};      // the same with the parts of each launch class
@@ -101,7 +104,10 @@ struct Sim {
     int set_green(int n, const int* ijk, int ntdec_w, int bforce);
     const SnapPlane* find_plane(int sec, int kind) const;
     int nframes_done() const;
-    void fill_zargs(ZArgs& z) const;
+    // shell_view: with pml_fused, the sweep over the whole grid (its x
+    // origin moved left so that the interior starts on a tile boundary) for
+    // the interior and shell-tile kernels; otherwise the interior box
+    void fill_zargs(ZArgs& z, bool shell_view = true) const;
     int launch_step(bool timed);
     int ensure_graph();
     int check_divergence();

@@ -79,7 +79,10 @@ static int plan(const swpc_dims* d, Plan& p) {
             if (bx[b][3] <= 0 || bx[b][4] <= 0 || bx[b][5] <= 0) continue;
             PmlBox& B = p.box[p.nbox++];
             B.x0 = bx[b][0]; B.y0 = bx[b][1]; B.z0 = bx[b][2]; B.nx = bx[b][3]; B.ny = bx[b][4]; B.nz = bx[b][5];
-            B.pitch = B.nx;  // rows of one point contiguous: no partly used lines in the 20-wide x-side boxes
+            B.pitch = B.nx;  // rows without padding, one array per auxiliary
+            const long long vol = (long long)B.nx * B.ny * B.nz;
+            if (vol > 0x7fffffffLL) return set_err(SWPC_E_ARG, "a PML box holds more than 2^31 - 1 cells");
+            B.qs = (int)vol;
             B.off = p.nade;
             p.nade += 9LL * B.pitch * B.ny * B.nz;
             first += (long long)B.nx * B.ny * B.nz;
@@ -130,10 +133,28 @@ static void cerjan_profile(int n, int na, double d, std::vector<float>& c, std::
 // ---------------------------------------------------------------------------
 // launches
 // ---------------------------------------------------------------------------
-void Sim::fill_zargs(ZArgs& z) const {
+void Sim::fill_zargs(ZArgs& z, bool shell_view) const {
+    // shell_view: the sweep over the whole grid when the tile kernels sweep
+    // the shell (interior and shell-tile kernels); otherwise the interior box
+    const bool f = shell_view && pml_fused;
     z.g = p.g;
     z.V = V; z.S = S; z.M = M; z.R = R; z.band = band;
-    z.x0 = p.x0; z.y0 = p.y0; z.nxi = p.nxi; z.nyi = p.nyi; z.kz_end = p.nzi;
+    z.x0 = p.x0; z.y0 = p.y0; z.nxi = p.nxi; z.nyi = p.nyi; z.nzi = p.nzi;
+    z.kz_end = f ? p.g.nz : p.nzi;
+    z.tx0 = f ? p.x0 - 32 * ((p.x0 + 31) / 32) : p.x0;
+    z.ty0 = f ? 0 : p.y0;
+    z.sx = f ? p.g.nx - z.tx0 : p.nxi;
+    z.sy = f ? p.g.ny : p.nyi;
+    z.sh = PmlShell{};
+    if (f) {
+        const PArgs& a = pml_args;
+        PmlShell& h = z.sh;
+        h.prof = a.prof; h.adeV = a.adeV; h.adeS = a.adeS;
+        h.pxc = a.pxc; h.pxe = a.pxe; h.pyc = a.pyc; h.pye = a.pye; h.pzc = a.pzc; h.pze = a.pze;
+        for (int q = 0; q < 6; ++q) { h.dlo[q] = shell_dlo[q]; h.dhi[q] = shell_dhi[q]; }
+        h.r20x = a.r20x; h.r20y = a.r20y; h.r20z = a.r20z; h.dt = a.dt;
+        for (int b = 0; b < 5; ++b) h.box[b] = p.box[b];
+    }
     z.kchunk = kchunk; z.kchunk_v = kchunk_v; z.rpitch = p.rpitch;
     z.cer = p.pml ? nullptr : cer;
     for (int q = 0; q < 6; ++q) z.cer_off[q] = cer_off[q];
@@ -218,7 +239,9 @@ int Sim::launch_step(bool timed) {
     };
     // the PML shell kernels run beside the interior kernels on a second
     // stream (two branches of the captured graph); they touch disjoint points
-    const bool two = p.pml && concurrent;
+    // (none when the tile kernels sweep the shell themselves)
+    const bool shell = p.pml && !pml_fused;
+    const bool two = shell && concurrent;
     cudaStream_t sp = two ? stream2 : stream;
     if (vmax_args.ntdec_r > 0) { k_vmax<<<64, 256, 0, stream>>>(vmax_args); ++launches; }
     if (tap_args.n > 0) {
@@ -237,22 +260,44 @@ int Sim::launch_step(bool timed) {
     fill_zargs(z);
     targs.z = z;
     const dim3 tblk(32, ty_s), tblk_v(32, ty_v);
-    const dim3 tgrd((p.nxi + 31) / 32, (p.nyi + ty_s - 1) / ty_s, (p.nzi + kchunk - 1) / kchunk);
-    const dim3 tgrd_v((p.nxi + 31) / 32, (p.nyi + ty_v - 1) / ty_v, (p.nzi + kchunk_v - 1) / kchunk_v);
+    // interior kernels over interior_tiles; with the shell swept by the tile
+    // kernels, the shell-tile kernels over the rest (timing classes 2 and 3)
+    int bxl, bxh, byl, byh;
+    interior_tiles(z, ty_s, bxl, bxh, byl, byh);
+    const unsigned nlin = (unsigned)((bxh - bxl) * (byh - byl) * ((p.nzi + kchunk - 1) / kchunk));
+    interior_tiles(z, ty_v, bxl, bxh, byl, byh);
+    const dim3 tgrd_v(bxh - bxl, byh - byl, (p.nzi + kchunk_v - 1) / kchunk_v);
+    const unsigned nsh_s = (unsigned)shell_tile_count(z, ty_s, kchunk), nsh_v = (unsigned)shell_tile_count(z, ty_v, kchunk_v);
     if (pw && p.pml) { k_pw_ghost<<<256, 256, 0, stream>>>(V, p.g, 3); ++launches; }
     if (two) {
         cudaEventRecord(ev_fork, stream);
         cudaStreamWaitEvent(stream2, ev_fork, 0);
     }
-    if (p.pml) {
+    if (shell) {
         ev0(2, sp);
         launch_pml(true, sp, timed);
         ev1(2, sp);
         if (two) cudaEventRecord(ev_join, stream2);
     }
+    if (nsh_s) {
+        ev0(2, stream);
+        if (ty_s == 16) {
+            if (p.rbytes == 4) k_stress_tma_shell<float, 16><<<nsh_s, tblk, smem_stress_sh, stream>>>(targs);
+            else if (dims.store == SWPC_STORE_FP16) k_stress_tma_shell<__half, 16><<<nsh_s, tblk, smem_stress_sh, stream>>>(targs);
+            else k_stress_tma_shell<__nv_bfloat16, 16><<<nsh_s, tblk, smem_stress_sh, stream>>>(targs);
+        } else {
+            if (p.rbytes == 4) k_stress_tma_shell<float><<<nsh_s, tblk, smem_stress_sh, stream>>>(targs);
+            else if (dims.store == SWPC_STORE_FP16) k_stress_tma_shell<__half><<<nsh_s, tblk, smem_stress_sh, stream>>>(targs);
+            else k_stress_tma_shell<__nv_bfloat16><<<nsh_s, tblk, smem_stress_sh, stream>>>(targs);
+        }
+        ++launches;
+        ev1(2, stream);
+    }
     ev0(0, stream);
-    if (variant == 0) {
-        const unsigned nlin = tgrd.x * tgrd.y * tgrd.z;  // 1-D grid, grouped block order
+    if (variant == 0 && nlin == 0) {
+        // no tile lies wholly inside the interior: the shell-tile kernel did all
+    } else if (variant == 0) {
+        // 1-D grid, grouped block order
         if (ty_s == 16) {
             if (p.rbytes == 4) k_stress_tma<float, 16><<<nlin, tblk, smem_stress, stream>>>(targs);
             else if (dims.store == SWPC_STORE_FP16) k_stress_tma<__half, 16><<<nlin, tblk, smem_stress, stream>>>(targs);
@@ -267,7 +312,7 @@ int Sim::launch_step(bool timed) {
         else if (dims.store == SWPC_STORE_FP16) k_stress_interior<__half><<<grd, blk, 0, stream>>>(z);
         else k_stress_interior<__nv_bfloat16><<<grd, blk, 0, stream>>>(z);
     }
-    ++launches;
+    if (variant != 0 || nlin) ++launches;
     ev1(0, stream);
     if (two) cudaStreamWaitEvent(stream, ev_join, 0);
     if (src_args.n > 0 && !bf_mode) {
@@ -280,20 +325,29 @@ int Sim::launch_step(bool timed) {
         cudaEventRecord(ev_fork2, stream);
         cudaStreamWaitEvent(stream2, ev_fork2, 0);
     }
-    if (p.pml) {
+    if (shell) {
         ev0(3, sp);
         launch_pml(false, sp, timed);
         ev1(3, sp);
         if (two) cudaEventRecord(ev_join2, stream2);
     }
+    if (nsh_v) {
+        ev0(3, stream);
+        if (ty_v == 16) k_vel_tma_shell<16><<<nsh_v, tblk_v, smem_vel_sh, stream>>>(targs);
+        else k_vel_tma_shell<><<<nsh_v, tblk_v, smem_vel_sh, stream>>>(targs);
+        ++launches;
+        ev1(3, stream);
+    }
     ev0(1, stream);
-    if (variant == 0) {
+    if (variant == 0 && tgrd_v.x * tgrd_v.y * tgrd_v.z == 0) {
+        // every tile went to the shell-tile kernel
+    } else if (variant == 0) {
         if (ty_v == 16) k_vel_tma<16><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
         else k_vel_tma<><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
     } else {
         k_vel_interior<<<grd_v, blk, 0, stream>>>(z);
     }
-    ++launches;
+    if (variant != 0 || tgrd_v.x * tgrd_v.y * tgrd_v.z) ++launches;
     ev1(1, stream);
     if (two) cudaStreamWaitEvent(stream, ev_join2, 0);
     if (src_args.n > 0 && bf_mode) {
@@ -410,6 +464,9 @@ int Sim::build_tensor_maps() {
     if (ts_ == 16) smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float, 16>) : sizeof(StressSmem<__half, 16>);
     else smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>);
     smem_vel = tv_ == 16 ? sizeof(VelSmem<16>) : sizeof(VelSmem<>);
+    if (ts_ == 16) smem_stress_sh = p.rbytes == 4 ? sizeof(StressSm<float, 16, true>) : sizeof(StressSm<__half, 16, true>);
+    else smem_stress_sh = p.rbytes == 4 ? sizeof(StressSm<float, 8, true>) : sizeof(StressSm<__half, 8, true>);
+    smem_vel_sh = tv_ == 16 ? sizeof(VelSm<16, true>) : sizeof(VelSm<8, true>);
     return tile_kernel_attributes();
 }
 
@@ -449,6 +506,23 @@ int tile_kernel_attributes() {
         set((const void*)k_stress_tma_batch<__nv_bfloat16, 16>, sizeof(StressSmem<__nv_bfloat16, 16>), false);
         set((const void*)k_vel_tma_batch<>, sizeof(VelSmem<>), true);
         set((const void*)k_vel_tma_batch<16>, sizeof(VelSmem<16>), true);
+        // shell-tile kernels (rings + staged auxiliaries), single and batched
+        set((const void*)k_stress_tma_shell<float>, sizeof(StressSm<float, 8, true>), false);
+        set((const void*)k_stress_tma_shell<__half>, sizeof(StressSm<__half, 8, true>), false);
+        set((const void*)k_stress_tma_shell<__nv_bfloat16>, sizeof(StressSm<__nv_bfloat16, 8, true>), false);
+        set((const void*)k_stress_tma_shell<float, 16>, sizeof(StressSm<float, 16, true>), false);
+        set((const void*)k_stress_tma_shell<__half, 16>, sizeof(StressSm<__half, 16, true>), false);
+        set((const void*)k_stress_tma_shell<__nv_bfloat16, 16>, sizeof(StressSm<__nv_bfloat16, 16, true>), false);
+        set((const void*)k_vel_tma_shell<>, sizeof(VelSm<8, true>), true);
+        set((const void*)k_vel_tma_shell<16>, sizeof(VelSm<16, true>), true);
+        set((const void*)k_stress_tma_batch<float, 8, true>, sizeof(StressSm<float, 8, true>), false);
+        set((const void*)k_stress_tma_batch<__half, 8, true>, sizeof(StressSm<__half, 8, true>), false);
+        set((const void*)k_stress_tma_batch<__nv_bfloat16, 8, true>, sizeof(StressSm<__nv_bfloat16, 8, true>), false);
+        set((const void*)k_stress_tma_batch<float, 16, true>, sizeof(StressSm<float, 16, true>), false);
+        set((const void*)k_stress_tma_batch<__half, 16, true>, sizeof(StressSm<__half, 16, true>), false);
+        set((const void*)k_stress_tma_batch<__nv_bfloat16, 16, true>, sizeof(StressSm<__nv_bfloat16, 16, true>), false);
+        set((const void*)k_vel_tma_batch<8, true>, sizeof(VelSm<8, true>), true);
+        set((const void*)k_vel_tma_batch<16, true>, sizeof(VelSm<16, true>), true);
     }
     if (err != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(err));
     set_on[dev] = true;
@@ -1011,25 +1085,29 @@ int Sim::allocate() {
     cudaGetDevice(&dev);
     device = dev;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    variant = dims.reserved[0] == 1 ? 1 : 0;
+    pml_np = dims.reserved[2] == 2 ? 2 : dims.reserved[2] == 1 ? 1 : 0;  // 0: per launch class
+    // reserved[3] = 2: the TMA tile kernels sweep the PML shell too (interior
+    // and shell-tile kernels); otherwise the shell runs in launches of its own
+    pml_fused = p.pml && variant == 0 && p.nbox == 5 && dims.reserved[3] == 2;
+    const int nzs = p.nzi;  // chunks of the interior's planes (the planes below take chunks of the same depth)
     long long cols = (long long)((p.nxi + TBX - 1) / TBX) * ((p.nyi + TBY - 1) / TBY);
     long long want = 8LL * nsm;
-    int nchunk = (int)std::max(1LL, std::min((long long)(p.nzi / 8), (want + cols - 1) / cols));
-    const int kfill = (p.nzi + nchunk - 1) / nchunk;
+    int nchunk = (int)std::max(1LL, std::min((long long)(nzs / 8), (want + cols - 1) / cols));
+    const int kfill = (nzs + nchunk - 1) / nchunk;
     auto even = [&](int cap) {  // equal chunks of at most cap planes
-        const int nc = (p.nzi + cap - 1) / cap;
-        return (p.nzi + nc - 1) / nc;
+        const int nc = (nzs + cap - 1) / cap;
+        return (nzs + nc - 1) / nc;
     };
     kchunk = kchunk_auto = even(std::min(kfill, p.rbytes == 4 ? 8 : 32));
     kchunk_v = kchunk_v_auto = even(std::min(kfill, 128));
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
-    variant = dims.reserved[0] == 1 ? 1 : 0;
-    pml_np = dims.reserved[2] == 2 ? 2 : dims.reserved[2] == 1 ? 1 : 0;  // 0: per launch class
     // PML shell beside the interior: pays off only when the interior launch
     // cannot fill the GPU by itself (measured: 128x128x64 0.134 vs 0.16 ms per
     // step; 1024x1024x512 27.9 serial vs 28.3 ms concurrent)
     {
-        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + ty_s - 1) / ty_s) * ((p.nzi + kfill - 1) / kfill);
+        const long long tiles = (long long)((p.nxi + 31) / 32) * ((p.nyi + ty_s - 1) / ty_s) * ((nzs + kfill - 1) / kfill);
         concurrent = dims.reserved[1] == 2 || (dims.reserved[1] == 0 && tiles < 4LL * nsm);
     }
     if ((rc = build_tensor_maps())) return rc;
@@ -1072,6 +1150,24 @@ void Sim::plan_pml_parts(const std::vector<float>& prof) {
         while (i < n[ax] && !damp[ax][i]) ++i;
         while (i < n[ax] && damp[ax][i]) ++i;
         if (i != n[ax]) ends_only = false;
+    }
+    // the shell-tile kernels test damping by index ranges: every profile's
+    // damped indices must be its two end runs (else the shell keeps its own
+    // launches)
+    {
+        const int offs[6] = {a.pxc, a.pxe, a.pyc, a.pye, a.pzc, a.pze};
+        bool runs = true;
+        for (int q = 0; q < 6; ++q) {
+            const int n1 = n[q / 2];
+            auto d = [&](int i) { return prof[offs[q] + 4 * i + 3] != 0.f; };
+            int lo = 0, hi = n1;
+            while (lo < n1 && d(lo)) ++lo;
+            while (hi > lo && d(hi - 1)) --hi;
+            for (int i = lo; i < hi; ++i) runs = runs && !d(i);
+            shell_dlo[q] = lo;
+            shell_dhi[q] = hi;
+        }
+        if (!runs) pml_fused = false;
     }
     std::vector<PmlPart> cls[PML_NCLASS];
     long long cls_pts[PML_NCLASS] = {}, cls_ax[PML_NCLASS] = {};
@@ -1563,13 +1659,18 @@ struct Batch {
     std::vector<Sim*> pw_members;  // plane-wave members: lateral ghost extrapolation before the PML updates
     VmaxArgs* d_vmax = nullptr;
     int** d_its = nullptr;
-    int4* d_tblocks = nullptr;   // stress tiles
+    int4* d_tblocks = nullptr;   // stress tiles (interior kernels)
     int4* d_tblocks_v = nullptr; // velocity tiles
+    int4* d_tblocks_sh = nullptr;   // stress shell tiles (members whose tile kernels sweep the shell)
+    int4* d_tblocks_vsh = nullptr;  // velocity shell tiles
+    int n_tblocks_sh = 0, n_tblocks_vsh = 0;
+    TArgs* d_targs_np = nullptr;        // the persistent form's view of every member (interior box)
+    PArgs* d_pargs_np[PML_NCLASS] = {}; // and its PML blocks
     int2* d_pblocks[PML_NCLASS] = {}; // per launch class: (member, block of its launch)
     int n_pblocks[PML_NCLASS] = {};
     int n_tblocks = 0, n_tblocks_v = 0, max_nst = 0, max_src = 0, max_pix = 0, max_planes = 0;
     bool any_vmax = false, any_snap = false, any_bf = false, any_mt = false;
-    size_t smem_stress = 0, smem_vel = 0;
+    size_t smem_stress = 0, smem_vel = 0, smem_stress_sh = 0, smem_vel_sh = 0;
     long long launches = 0, launches_per_graph = 0;
     // persistent fused form: the work queue of one time step of every
     // member, the per-member finished counters and the launch shape
@@ -1670,8 +1771,8 @@ struct Batch {
         PersistArgs& P = pargs;
         P.items = d_items; P.need = d_need; P.n_items = n_items;
         P.head = d_ctr; P.err = d_ctr + 1; P.done = d_ctr + 2;
-        P.targs = d_targs;
-        for (int c = 0; c < PML_NCLASS; ++c) P.pargs[c] = d_pargs[c];
+        P.targs = d_targs_np;
+        for (int c = 0; c < PML_NCLASS; ++c) P.pargs[c] = d_pargs_np[c];
         P.src = d_src; P.tap = d_tap; P.snap = d_snap; P.green = d_green; P.its = d_its;
         // one block of the 8-row tile kernels' shape holds either tile's rings
         smem_persist = std::max(rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>), sizeof(VelSmem<>));
@@ -1746,7 +1847,23 @@ struct Batch {
             launch_pml(true);
             cudaEventRecord(ev[1], stream2);
         }
-        if (ty_s == 16) {
+        if (n_tblocks_sh) {  // shell tiles of the members whose tile kernels sweep the shell
+            if (ty_s == 16) {
+                if (rbytes == 4) k_stress_tma_batch<float, 16, true><<<n_tblocks_sh, tblk, smem_stress_sh, stream>>>(d_targs, d_tblocks_sh);
+                else if (store == SWPC_STORE_FP16)
+                    k_stress_tma_batch<__half, 16, true><<<n_tblocks_sh, tblk, smem_stress_sh, stream>>>(d_targs, d_tblocks_sh);
+                else k_stress_tma_batch<__nv_bfloat16, 16, true><<<n_tblocks_sh, tblk, smem_stress_sh, stream>>>(d_targs, d_tblocks_sh);
+            } else {
+                if (rbytes == 4) k_stress_tma_batch<float, 8, true><<<n_tblocks_sh, tblk, smem_stress_sh, stream>>>(d_targs, d_tblocks_sh);
+                else if (store == SWPC_STORE_FP16)
+                    k_stress_tma_batch<__half, 8, true><<<n_tblocks_sh, tblk, smem_stress_sh, stream>>>(d_targs, d_tblocks_sh);
+                else k_stress_tma_batch<__nv_bfloat16, 8, true><<<n_tblocks_sh, tblk, smem_stress_sh, stream>>>(d_targs, d_tblocks_sh);
+            }
+            ++launches;
+        }
+        if (n_tblocks == 0) {
+            // every tile of every member went to the shell-tile kernel
+        } else if (ty_s == 16) {
             if (rbytes == 4) k_stress_tma_batch<float, 16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
             else if (store == SWPC_STORE_FP16)
                 k_stress_tma_batch<__half, 16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
@@ -1756,7 +1873,7 @@ struct Batch {
             else if (store == SWPC_STORE_FP16) k_stress_tma_batch<__half><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
             else k_stress_tma_batch<__nv_bfloat16><<<n_tblocks, tblk, smem_stress, stream>>>(d_targs, d_tblocks);
         }
-        ++launches;
+        if (n_tblocks) ++launches;
         if (pml) cudaStreamWaitEvent(stream, ev[1], 0);
         if (any_mt) { k_stressglut_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
         for (Sim* m : pw_members) { k_pw_ghost<<<256, 256, 0, stream>>>(m->S, m->p.g, 6); ++launches; }
@@ -1766,9 +1883,16 @@ struct Batch {
             launch_pml(false);
             cudaEventRecord(ev[3], stream2);
         }
-        if (ty_v == 16) k_vel_tma_batch<16><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
-        else k_vel_tma_batch<><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
-        ++launches;
+        if (n_tblocks_vsh) {
+            if (ty_v == 16) k_vel_tma_batch<16, true><<<n_tblocks_vsh, tblk_v, smem_vel_sh, stream>>>(d_targs, d_tblocks_vsh);
+            else k_vel_tma_batch<8, true><<<n_tblocks_vsh, tblk_v, smem_vel_sh, stream>>>(d_targs, d_tblocks_vsh);
+            ++launches;
+        }
+        if (n_tblocks_v) {
+            if (ty_v == 16) k_vel_tma_batch<16><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
+            else k_vel_tma_batch<><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
+            ++launches;
+        }
         if (pml) cudaStreamWaitEvent(stream, ev[3], 0);
         if (any_bf) { k_bodyforce_batch<<<dim3((max_src + 127) / 128, n), 128, 0, stream>>>(d_src); ++launches; }
         k_advance_batch<<<(n + 127) / 128, 128, 0, stream>>>(d_its, n); ++launches;
@@ -1792,6 +1916,12 @@ int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel) {
 }
 
 int swpc_gpu_set_zchunk(swpc_sim* sim, int kchunk) { return swpc_gpu_set_zchunks(sim, kchunk, kchunk); }
+
+int swpc_gpu_pml_fused(swpc_sim* sim) {
+    Sim* s = reinterpret_cast<Sim*>(sim);
+    if (!s) return set_err(SWPC_E_ARG, "null simulation");
+    return s->pml_fused ? 1 : 0;
+}
 
 int swpc_gpu_set_tiles(swpc_sim* sim, int rows_stress, int rows_vel) {
     Sim* s = reinterpret_cast<Sim*>(sim);
@@ -1855,27 +1985,65 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         return fail(set_err(SWPC_E_CUDA, "stream creation failed"));
     for (auto& e : b->ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(set_err(SWPC_E_CUDA, "event creation failed"));
-    std::vector<TArgs> ta(n);
-    std::vector<PArgs> pa[PML_NCLASS];
+    // ta, pa, tb, tbv, tbs, tbvs: the phase launches (a member whose tile
+    // kernels sweep its shell has interior and shell-tile blocks and no PML
+    // blocks); ta_np, pa_np, tb_np, tbv_np: the persistent form, which runs
+    // every member's interior tiles and PML blocks
+    std::vector<TArgs> ta(n), ta_np(n);
+    std::vector<PArgs> pa[PML_NCLASS], pa_np[PML_NCLASS];
     std::vector<SrcArgs> sa(n);
     std::vector<TapArgs> tp(n);
     std::vector<SnapArgs> sn(n);
     std::vector<GreenArgs> gr(n);
     std::vector<VmaxArgs> vm(n);
     std::vector<int*> its(n);
-    std::vector<int4> tb, tbv;
+    std::vector<int4> tb, tbv, tbs, tbvs, tb_np, tbv_np;
     std::vector<int2> pb[PML_NCLASS];
+    // interior tiles of a member's view: stress in the grouped order of the
+    // single-simulation launch, velocity x fastest; entries (member, bx, by,
+    // first plane of the chunk)
+    auto interior_lists = [&](int q, const Sim* s, const ZArgs& z, std::vector<int4>& st, std::vector<int4>& vt) {
+        int bxl, bxh, byl, byh;
+        interior_tiles(z, s->ty_s, bxl, bxh, byl, byh);
+        const int gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
+        for (int y0 = byl; y0 < byh; y0 += STRESS_YGROUP)
+            for (int bz = 0; bz < gz; ++bz)
+                for (int by = y0; by < std::min(byh, y0 + STRESS_YGROUP); ++by)
+                    for (int bx = bxl; bx < bxh; ++bx) st.push_back(make_int4(q, bx, by, bz * s->kchunk));
+        interior_tiles(z, s->ty_v, bxl, bxh, byl, byh);
+        const int gzv = (s->p.nzi + s->kchunk_v - 1) / s->kchunk_v;
+        for (int bz = 0; bz < gzv; ++bz)
+            for (int by = byl; by < byh; ++by)
+                for (int bx = bxl; bx < bxh; ++bx) vt.push_back(make_int4(q, bx, by, bz * s->kchunk_v));
+    };
     for (int q = 0; q < n; ++q) {
         Sim* s = b->sims[q];
         CK(cudaStreamSynchronize(s->stream));
-        ZArgs z;
+        ZArgs z, znp;
         s->fill_zargs(z);
+        s->fill_zargs(znp, false);
         ta[q] = s->targs;
         ta[q].z = z;
+        ta_np[q] = s->targs;
+        ta_np[q].z = znp;
         for (int c = 0; c < PML_NCLASS; ++c) {
-            pa[c].push_back(s->pml_cls[c]);
-            if (!s->p.pml) pa[c].back().nblocks = 0;
+            pa_np[c].push_back(s->pml_cls[c]);
+            if (!s->p.pml) pa_np[c].back().nblocks = 0;
+            pa[c].push_back(pa_np[c].back());
+            if (s->pml_fused) pa[c].back().nblocks = 0;
             for (int bk = 0; bk < pa[c].back().nblocks; ++bk) pb[c].push_back(make_int2(q, bk));
+        }
+        interior_lists(q, s, z, tb, tbv);
+        interior_lists(q, s, znp, tb_np, tbv_np);
+        for (int L = 0, ns = shell_tile_count(z, s->ty_s, s->kchunk); L < ns; ++L) {
+            int bx, by, kz0;
+            shell_tile(z, s->ty_s, s->kchunk, L, bx, by, kz0);
+            tbs.push_back(make_int4(q, bx, by, kz0));
+        }
+        for (int L = 0, ns = shell_tile_count(z, s->ty_v, s->kchunk_v); L < ns; ++L) {
+            int bx, by, kz0;
+            shell_tile(z, s->ty_v, s->kchunk_v, L, bx, by, kz0);
+            tbvs.push_back(make_int4(q, bx, by, kz0));
         }
         sa[q] = s->src_args;
         tp[q] = s->tap_args;
@@ -1885,16 +2053,6 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
         if (s->pw && s->p.pml) b->pw_members.push_back(s);
         vm[q] = s->vmax_args;
         its[q] = s->d_it;
-        const int gx = (s->p.nxi + 31) / 32, gy = (s->p.nyi + s->ty_s - 1) / s->ty_s, gz = (s->p.nzi + s->kchunk - 1) / s->kchunk;
-        const int gyv = (s->p.nyi + s->ty_v - 1) / s->ty_v, gzv = (s->p.nzi + s->kchunk_v - 1) / s->kchunk_v;
-        // stress tiles in the grouped order of the single-simulation launch
-        for (int y0 = 0; y0 < gy; y0 += STRESS_YGROUP)
-            for (int bz = 0; bz < gz; ++bz)
-                for (int by = y0; by < std::min(gy, y0 + STRESS_YGROUP); ++by)
-                    for (int bx = 0; bx < gx; ++bx) tb.push_back(make_int4(q, bx, by, bz));
-        for (int bz = 0; bz < gzv; ++bz)
-            for (int by = 0; by < gyv; ++by)
-                for (int bx = 0; bx < gx; ++bx) tbv.push_back(make_int4(q, bx, by, bz));
         b->max_nst = std::max(b->max_nst, s->tap_args.n);
         b->max_src = std::max(b->max_src, s->src_args.n);
         if (s->src_args.n > 0) { if (s->bf_mode) b->any_bf = true; else b->any_mt = true; }
@@ -1907,18 +2065,26 @@ int swpc_batch_create(swpc_sim* const* sims, int n, swpc_batch** out) {
     }
     int rc;
     for (int c = 0; c < PML_NCLASS; ++c)
-        if ((rc = b->upload(&b->d_pargs[c], pa[c])) || (rc = b->upload(&b->d_pblocks[c], pb[c]))) return fail(rc);
-    if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_src, sa)) ||
+        if ((rc = b->upload(&b->d_pargs[c], pa[c])) || (rc = b->upload(&b->d_pblocks[c], pb[c])) ||
+            (rc = b->upload(&b->d_pargs_np[c], pa_np[c])))
+            return fail(rc);
+    if ((rc = b->upload(&b->d_targs, ta)) || (rc = b->upload(&b->d_targs_np, ta_np)) || (rc = b->upload(&b->d_src, sa)) ||
         (rc = b->upload(&b->d_tap, tp)) || (rc = b->upload(&b->d_snap, sn)) || (rc = b->upload(&b->d_green, gr)) || (rc = b->upload(&b->d_vmax, vm)) ||
-        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_tblocks_v, tbv)))
+        (rc = b->upload(&b->d_its, its)) || (rc = b->upload(&b->d_tblocks, tb)) || (rc = b->upload(&b->d_tblocks_v, tbv)) ||
+        (rc = b->upload(&b->d_tblocks_sh, tbs)) || (rc = b->upload(&b->d_tblocks_vsh, tbvs)))
         return fail(rc);
-    if (((uintptr_t)b->d_targs & 127) != 0) return fail(set_err(SWPC_E_CUDA, "tensor-map table is not 128-byte aligned"));
+    if (((uintptr_t)b->d_targs & 127) != 0 || ((uintptr_t)b->d_targs_np & 127) != 0)
+        return fail(set_err(SWPC_E_CUDA, "tensor-map table is not 128-byte aligned"));
     b->n_tblocks = (int)tb.size();
     b->n_tblocks_v = (int)tbv.size();
+    b->n_tblocks_sh = (int)tbs.size();
+    b->n_tblocks_vsh = (int)tbvs.size();
     for (int c = 0; c < PML_NCLASS; ++c) b->n_pblocks[c] = (int)pb[c].size();
     b->smem_stress = b->sims[0]->smem_stress;
     b->smem_vel = b->sims[0]->smem_vel;
-    if ((rc = b->build_queue(tb, tbv, pa))) return fail(rc);
+    b->smem_stress_sh = b->sims[0]->smem_stress_sh;
+    b->smem_vel_sh = b->sims[0]->smem_vel_sh;
+    if ((rc = b->build_queue(tb_np, tbv_np, pa_np))) return fail(rc);
     *out = reinterpret_cast<swpc_batch*>(b);
     return 0;
 }

@@ -61,7 +61,7 @@ EXPORTS = [
     "swpc_serve_times", "swpc_serve_release", "swpc_serve_drain", "swpc_serve_stats", "swpc_serve_destroy",
     "swpc_gpu_profile_read_pml", "swpc_host_banner", "swpc_host_ntdec_r",
     "swpc_batch_set_persistent", "swpc_batch_item_count", "swpc_gpu_build_medium_rmed",
-    "swpc_gpu_set_tiles", "swpc_gpu_get_tiles",
+    "swpc_gpu_set_tiles", "swpc_gpu_get_tiles", "swpc_gpu_pml_fused",
 ]
 
 
@@ -126,6 +126,7 @@ def lib(build=True):
     L.swpc_gpu_set_zchunks.argtypes = [vp, i, i]
     L.swpc_gpu_set_tiles.argtypes = [vp, i, i]
     L.swpc_gpu_get_tiles.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
+    L.swpc_gpu_pml_fused.argtypes = [vp]
     L.swpc_gpu_get_zchunks.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p]
     L.swpc_batch_create.argtypes = [ctypes.c_void_p, i, ctypes.POINTER(vp)]
     L.swpc_batch_run.argtypes = [vp, i]
@@ -186,9 +187,14 @@ def _ptr(a):
 
 
 def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xbeg=0.0, ybeg=0.0, zbeg=0.0,
-              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0, concurrent=None, pml_points=0):
+              tbeg=0.0, fcut=1.0, M0=1.0, UC=1e-15, ntdec_r=0, variant=0, concurrent=None, pml_points=0,
+              pml_fused=None):
     """swpc_dims for swpc_gpu_create.  variant 0 selects the TMA-fed interior
     kernels, 1 the shared-memory sweep without TMA (kept for comparison);
+    pml_fused (with variant 0): True makes the tile kernels sweep the PML
+    shell too (interior kernels over the tiles inside the interior,
+    shell-tile kernels over the rest); False or None (the library default)
+    runs the shell in launches of its own, where the next two options apply;
     concurrent runs the PML shell kernels beside the interior kernels on a
     second stream (True/False; None lets the library choose by grid size);
     pml_points: shell points per thread of the PML kernels (1 or 2; 0 lets
@@ -203,6 +209,7 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     d.reserved[0] = int(variant)
     d.reserved[1] = 0 if concurrent is None else (2 if concurrent else 1)
     d.reserved[2] = int(pml_points)
+    d.reserved[3] = 0 if pml_fused is None else (2 if pml_fused else 1)
     return d
 
 
@@ -434,6 +441,14 @@ class Simulation:
         a, b = ctypes.c_int(), ctypes.c_int()
         _ck(lib().swpc_gpu_get_tiles(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    @property
+    def pml_fused(self):
+        """True when the tile kernels sweep the PML shell with the interior."""
+        rc = lib().swpc_gpu_pml_fused(self._h)
+        if rc < 0:
+            _ck(rc)
+        return rc == 1
 
     def zchunks(self):
         ks, kv = ctypes.c_int(), ctypes.c_int()
