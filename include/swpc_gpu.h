@@ -286,8 +286,9 @@ int swpc_gpu_reset(swpc_sim* sim);
  * set_zchunk sets both to one depth; get_zchunk returns the stress depth. */
 int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel);
 /* Tile shape of the interior stress and velocity kernels: 32 columns by 8
- * (default) or 16 rows each, with 8-row tiles two stress blocks or three
- * velocity blocks share an SM, with 16-row tiles one (fewer halo rows per
+ * (default) or 16 rows each, or 12 rows for the velocity kernels; with
+ * 8-row tiles two stress blocks or three velocity blocks share an SM, with
+ * 12-row velocity tiles two, with 16-row tiles one (fewer halo rows per
  * point, fewer blocks); 0 restores 8.  The autotuner sets them together with
  * the z-sweep depths.  Batched members must share their tile shapes, and the
  * persistent batch form runs 8-row tiles.  No counterpart in the reference. */

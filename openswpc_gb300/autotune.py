@@ -1,7 +1,7 @@
 """Autotuner of the tile shapes and z-sweep depths of the interior kernels.
 
 Each interior block sweeps a chunk of z planes of a tile of 32 columns by 8
-or 16 rows.  Taller tiles read fewer halo rows per point but run fewer
+or 16 rows (velocity also 12).  Taller tiles read fewer halo rows per point but run fewer
 blocks per SM.  Long chunks amortise the
 pipeline prologue (the first planes of every ring are loaded before any
 compute); short chunks create more blocks, which small grids need to fill the
@@ -23,7 +23,8 @@ import numpy as np
 from . import gpu
 
 CANDIDATES = (8, 16, 32, 64, 128, 0)  # 0 = the library's automatic choice
-TILE_ROWS = (8, 16)  # rows of the 32-column tiles
+TILE_ROWS = (8, 16)  # rows of the 32-column stress tiles
+TILE_ROWS_VEL = (8, 12, 16)  # and of the velocity tiles
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 
@@ -63,7 +64,7 @@ def _time(runner, stream, steps):
 
 
 def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=CANDIDATES, batch=None,
-         rows=TILE_ROWS):
+         rows=TILE_ROWS, rows_vel=TILE_ROWS_VEL):
     """Pick the tile shapes and z-sweep depths of the stress and velocity
     kernels for `sims` (one simulation, or the members of a batch when
     len(sims) > 1), apply them to every member and return {"tiles": [stress
@@ -79,7 +80,7 @@ def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=
     reset afterwards, so call this after set-up and before the production
     run.
     """
-    key = _shape_key(sims, store) + "-tiles"
+    key = _shape_key(sims, store) + "-tiles12"
     db = _load(cache) if cache else {}
     if key in db and "tiles" in db[key]:
         r = db[key]
@@ -115,7 +116,7 @@ def tune(sims, store="fp32", warmup=8, steps=8, cache=DEFAULT_CACHE, candidates=
 
     t_s = {(r, z): measure(r, z, 8, 0) for r in rows for z in candidates}
     best_s = min(t_s, key=t_s.get)
-    t_v = {(r, z): measure(best_s[0], best_s[1], r, z) for r in rows for z in candidates}
+    t_v = {(r, z): measure(best_s[0], best_s[1], r, z) for r in rows_vel for z in candidates}
     best_v = min(t_v, key=t_v.get)
     for s in sims:
         s.set_tiles(best_s[0], best_v[0])

@@ -115,12 +115,17 @@ struct VelSmem {
 // VMINB (velocity), 16-row tiles one (their rings take 181 and 125 KB)
 template <int TY> struct TileOcc { static constexpr int stress = 2, vel = VMINB; };
 template <> struct TileOcc<16> { static constexpr int stress = 1, vel = 1; };
+// 12-row tiles (velocity only): two 99 KB blocks per SM, the same 80
+// registers per thread as three 8-row blocks, a third less S halo per point
+template <> struct TileOcc<12> { static constexpr int stress = 1, vel = 2; };
 static_assert(sizeof(Slot3<float, TTY + 1, 4, 36>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot2<float, TTY + 1, 36>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot3<__half, TTY, 18, 32>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot3<float, TTY + 4, 6, 40>) % 128 == 0, "slot size");
 static_assert(sizeof(Slot3<float, 17, 4, 36>) % 128 == 0 && sizeof(Slot2<float, 17, 36>) % 128 == 0, "slot size");
 static_assert(sizeof(StressSmem<float, 16>) <= 227 * 1024 && sizeof(VelSmem<16>) <= 227 * 1024, "16-row rings fit");
+static_assert(2 * sizeof(VelSmem<12>) <= 226 * 1024, "two 12-row velocity blocks fit on an SM");
+static_assert(sizeof(Slot3<float, 16, 6, 40>) % 128 == 0 && sizeof(Slot3<float, 12, 3, 32>) % 128 == 0, "slot size");
 
 // Shell-tile kernels: the auxiliaries of every thread's shell point staged one
 // plane ahead by cp.async (nine words per thread), after the rings.
@@ -132,6 +137,7 @@ template <int TY> struct VelSm<TY, true> : VelSmem<TY> { AuxStage<TY> aux; };
 // blocks per SM of the shell-tile kernels (8-row tiles; 16-row tiles one)
 template <int TY> struct ShellOcc { static constexpr int stress = 2, vel = 2; };
 template <> struct ShellOcc<16> { static constexpr int stress = 1, vel = 1; };
+template <> struct ShellOcc<12> { static constexpr int stress = 1, vel = 1; };
 static_assert(2 * sizeof(StressSm<float, 8, true>) <= 226 * 1024 && 2 * sizeof(VelSm<8, true>) <= 226 * 1024,
               "two shell-tile blocks fit on an SM");
 

@@ -334,6 +334,7 @@ int Sim::launch_step(bool timed) {
     if (nsh_v) {
         ev0(3, stream);
         if (ty_v == 16) k_vel_tma_shell<16><<<nsh_v, tblk_v, smem_vel_sh, stream>>>(targs);
+        else if (ty_v == 12) k_vel_tma_shell<12><<<nsh_v, tblk_v, smem_vel_sh, stream>>>(targs);
         else k_vel_tma_shell<><<<nsh_v, tblk_v, smem_vel_sh, stream>>>(targs);
         ++launches;
         ev1(3, stream);
@@ -343,6 +344,7 @@ int Sim::launch_step(bool timed) {
         // every tile went to the shell-tile kernel
     } else if (variant == 0) {
         if (ty_v == 16) k_vel_tma<16><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
+        else if (ty_v == 12) k_vel_tma<12><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
         else k_vel_tma<><<<tgrd_v, tblk_v, smem_vel, stream>>>(targs);
     } else {
         k_vel_interior<<<grd_v, blk, 0, stream>>>(z);
@@ -463,10 +465,10 @@ int Sim::build_tensor_maps() {
     targs.err = d_err;
     if (ts_ == 16) smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float, 16>) : sizeof(StressSmem<__half, 16>);
     else smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>);
-    smem_vel = tv_ == 16 ? sizeof(VelSmem<16>) : sizeof(VelSmem<>);
+    smem_vel = tv_ == 16 ? sizeof(VelSmem<16>) : tv_ == 12 ? sizeof(VelSmem<12>) : sizeof(VelSmem<>);
     if (ts_ == 16) smem_stress_sh = p.rbytes == 4 ? sizeof(StressSm<float, 16, true>) : sizeof(StressSm<__half, 16, true>);
     else smem_stress_sh = p.rbytes == 4 ? sizeof(StressSm<float, 8, true>) : sizeof(StressSm<__half, 8, true>);
-    smem_vel_sh = tv_ == 16 ? sizeof(VelSm<16, true>) : sizeof(VelSm<8, true>);
+    smem_vel_sh = tv_ == 16 ? sizeof(VelSm<16, true>) : tv_ == 12 ? sizeof(VelSm<12, true>) : sizeof(VelSm<8, true>);
     return tile_kernel_attributes();
 }
 
@@ -498,6 +500,7 @@ int tile_kernel_attributes() {
         set((const void*)k_stress_tma<__nv_bfloat16, 16>, sizeof(StressSmem<__nv_bfloat16, 16>), false);
         set((const void*)k_vel_tma<>, sizeof(VelSmem<>), true);
         set((const void*)k_vel_tma<16>, sizeof(VelSmem<16>), true);
+        set((const void*)k_vel_tma<12>, sizeof(VelSmem<12>), true);
         set((const void*)k_stress_tma_batch<float>, sizeof(StressSmem<float>), false);
         set((const void*)k_stress_tma_batch<__half>, sizeof(StressSmem<__half>), false);
         set((const void*)k_stress_tma_batch<__nv_bfloat16>, sizeof(StressSmem<__nv_bfloat16>), false);
@@ -506,6 +509,7 @@ int tile_kernel_attributes() {
         set((const void*)k_stress_tma_batch<__nv_bfloat16, 16>, sizeof(StressSmem<__nv_bfloat16, 16>), false);
         set((const void*)k_vel_tma_batch<>, sizeof(VelSmem<>), true);
         set((const void*)k_vel_tma_batch<16>, sizeof(VelSmem<16>), true);
+        set((const void*)k_vel_tma_batch<12>, sizeof(VelSmem<12>), true);
         // shell-tile kernels (rings + staged auxiliaries), single and batched
         set((const void*)k_stress_tma_shell<float>, sizeof(StressSm<float, 8, true>), false);
         set((const void*)k_stress_tma_shell<__half>, sizeof(StressSm<__half, 8, true>), false);
@@ -515,6 +519,7 @@ int tile_kernel_attributes() {
         set((const void*)k_stress_tma_shell<__nv_bfloat16, 16>, sizeof(StressSm<__nv_bfloat16, 16, true>), false);
         set((const void*)k_vel_tma_shell<>, sizeof(VelSm<8, true>), true);
         set((const void*)k_vel_tma_shell<16>, sizeof(VelSm<16, true>), true);
+        set((const void*)k_vel_tma_shell<12>, sizeof(VelSm<12, true>), true);
         set((const void*)k_stress_tma_batch<float, 8, true>, sizeof(StressSm<float, 8, true>), false);
         set((const void*)k_stress_tma_batch<__half, 8, true>, sizeof(StressSm<__half, 8, true>), false);
         set((const void*)k_stress_tma_batch<__nv_bfloat16, 8, true>, sizeof(StressSm<__nv_bfloat16, 8, true>), false);
@@ -523,6 +528,7 @@ int tile_kernel_attributes() {
         set((const void*)k_stress_tma_batch<__nv_bfloat16, 16, true>, sizeof(StressSm<__nv_bfloat16, 16, true>), false);
         set((const void*)k_vel_tma_batch<8, true>, sizeof(VelSm<8, true>), true);
         set((const void*)k_vel_tma_batch<16, true>, sizeof(VelSm<16, true>), true);
+        set((const void*)k_vel_tma_batch<12, true>, sizeof(VelSm<12, true>), true);
     }
     if (err != cudaSuccess) return set_err(SWPC_E_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(err));
     set_on[dev] = true;
@@ -1885,11 +1891,13 @@ struct Batch {
         }
         if (n_tblocks_vsh) {
             if (ty_v == 16) k_vel_tma_batch<16, true><<<n_tblocks_vsh, tblk_v, smem_vel_sh, stream>>>(d_targs, d_tblocks_vsh);
+            else if (ty_v == 12) k_vel_tma_batch<12, true><<<n_tblocks_vsh, tblk_v, smem_vel_sh, stream>>>(d_targs, d_tblocks_vsh);
             else k_vel_tma_batch<8, true><<<n_tblocks_vsh, tblk_v, smem_vel_sh, stream>>>(d_targs, d_tblocks_vsh);
             ++launches;
         }
         if (n_tblocks_v) {
             if (ty_v == 16) k_vel_tma_batch<16><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
+            else if (ty_v == 12) k_vel_tma_batch<12><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
             else k_vel_tma_batch<><<<n_tblocks_v, tblk_v, smem_vel, stream>>>(d_targs, d_tblocks_v);
             ++launches;
         }
@@ -1928,8 +1936,9 @@ int swpc_gpu_set_tiles(swpc_sim* sim, int rows_stress, int rows_vel) {
     if (!s) return set_err(SWPC_E_ARG, "null simulation");
     if (rows_stress == 0) rows_stress = TTY;
     if (rows_vel == 0) rows_vel = TTY;
-    if ((rows_stress != 8 && rows_stress != 16) || (rows_vel != 8 && rows_vel != 16))
-        return set_err(SWPC_E_ARG, "tile rows must be 8 or 16 (0: the default 8)");
+    if ((rows_stress != 8 && rows_stress != 16) || (rows_vel != 8 && rows_vel != 12 && rows_vel != 16))
+        return set_err(SWPC_E_ARG, "tile rows must be 8 or 16 for the stress kernels, 8, 12 or 16 for the velocity "
+                                   "kernels (0: the default 8)");
     CK(cudaStreamSynchronize(s->stream));
     s->ty_s = rows_stress;
     s->ty_v = rows_vel;

@@ -74,7 +74,8 @@ def test_reset_and_autotune_leave_results_unchanged(infs, tmp_path):
     sims = [gpu.Simulation.from_inf(f) for f in infs]
     rec = autotune.tune(sims, cache=str(tmp_path / "tune.json"), steps=3, candidates=(8, 0))
     assert rec["zchunk"] in (8, 0) and rec["zchunk_vel"] in (8, 0)
-    assert all(r in (8, 16) for r in rec["tiles"]) and len(rec["ms_per_step"]) == 4
+    assert rec["tiles"][0] in (8, 16) and rec["tiles"][1] in (8, 12, 16) and len(rec["ms_per_step"]) == 4
+    assert len(rec["ms_per_step_vel"]) == 6
     assert sims[0].tiles() == tuple(rec["tiles"])
     b = gpu.Batch(sims)
     b.run(NT)
@@ -112,14 +113,15 @@ def test_persistent_batch_in_pieces_and_graph(infs):
 
 
 @pytest.mark.gpu
-def test_batch_with_16_row_tiles_equals_alone(infs):
-    """Members with 16-row stress and velocity tiles, advanced by the phase
-    launches, give the traces of the members alone (8-row tiles); the
-    persistent form refuses other than 8-row tiles."""
+@pytest.mark.parametrize("rows", [(16, 16), (8, 12)])
+def test_batch_with_other_tiles_equals_alone(infs, rows):
+    """Members with 16-row stress and 16- or 12-row velocity tiles, advanced
+    by the phase launches, give the traces of the members alone (8-row
+    tiles); the persistent form refuses other than 8-row tiles."""
     alone = [_alone(f) for f in infs]
     sims = [gpu.Simulation.from_inf(f) for f in infs]
     for s in sims:
-        s.set_tiles(16, 16)
+        s.set_tiles(*rows)
     b = gpu.Batch(sims)
     with pytest.raises(gpu.SwpcError):
         b.set_persistent(True)

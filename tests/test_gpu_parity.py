@@ -103,7 +103,7 @@ def test_vmax_matches_oracle(small_inf):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("rows", [(16, 8), (8, 16), (16, 16)])
+@pytest.mark.parametrize("rows", [(16, 8), (8, 16), (16, 16), (8, 12), (16, 12)])
 def test_tile_shapes_give_identical_fields(small_inf, rows):
     """Every tile shape evaluates the same expressions on the same values:
     the fields after 60 steps equal those of the default 8-row tiles bit

@@ -51,13 +51,16 @@ def test_two_points_per_thread_equal_one(n, other):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,store,na", [((96, 80, 64), "fp32", 20), ((100, 84, 70), "fp32", 13),
-                                        ((288, 288, 144), "fp32", 20), ((100, 84, 70), "fp16", 20)])
-def test_shell_in_tile_kernels_equals_shell_launches(n, store, na):
+@pytest.mark.parametrize("n,store,na,rows", [((96, 80, 64), "fp32", 20, (8, 8)), ((100, 84, 70), "fp32", 13, (8, 8)),
+                                             ((288, 288, 144), "fp32", 20, (8, 8)), ((100, 84, 70), "fp16", 20, (8, 8)),
+                                             ((100, 84, 70), "fp32", 20, (16, 12)), ((96, 80, 64), "fp32", 20, (16, 16))])
+def test_shell_in_tile_kernels_equals_shell_launches(n, store, na, rows):
     """The tile kernels' sweep of the shell (x origin left of the grid, edge
     tiles loading from x < 0, odd interior widths, the z layer below the
-    interior) against the shell's own launches, every wavefield bit for bit."""
+    interior, every tile shape) against the shell's own launches, every
+    wavefield bit for bit."""
     a, b = _sim(n, 0, fused=False, store=store, na=na), _sim(n, 0, fused=True, store=store, na=na)
+    b.set_tiles(*rows)
     a.run(1, 30)
     b.run(1, 30)
     for name in gpu.FIELDS:
