@@ -424,8 +424,11 @@ def interior_tile_points(w, rows, na=20):
 
 
 def shell_bytes(sim):
-    """PML shell points and their algorithmic bytes per step in each phase
-    (the per-point figures of pml_class_report, summed over the classes)."""
+    """PML shell points and their algorithmic bytes per step in each phase of
+    the shell-tile kernels, which take the edge moduli and buoyancies from
+    the staged medium tiles instead of the precomputed arrays: per point the
+    figures of pml_class_report without those 12 B (and with rho, 4 B, for
+    the velocity update), summed over the classes."""
     _, _, pts, ax = sim.profile_read_pml()
     n, a = float(pts.sum()), float(ax.sum())
     return int(n), {"stress": 68.0 * n + 24.0 * a, "vel": 52.0 * n + 24.0 * a}
@@ -434,13 +437,14 @@ def shell_bytes(sim):
 def pml_class_report(sim, peak):
     """Per launch class of the PML kernels: time per launch and the
     algorithmic bytes of its points.  Per shell point the stress update
-    reads V (12 B) and lam, mu (8 B) and rewrites S (48 B), the velocity
-    update reads S (24 B) and rho (4 B) and rewrites V (24 B); every damped
+    reads V (12 B), lam, mu (8 B) and the three precomputed edge moduli
+    (12 B) and rewrites S (48 B); the velocity update reads S (24 B) and the
+    three precomputed buoyancies (12 B) and rewrites V (24 B); every damped
     axis adds three auxiliaries read and written (24 B)."""
     ms, n, pts, ax = sim.profile_read_pml()
     names = ["x", "y", "z", "general"]
     out = {}
-    for u, (kname, base) in enumerate((("stress_pml", 68), ("vel_pml", 52))):
+    for u, (kname, base) in enumerate((("stress_pml", 80), ("vel_pml", 60))):
         tot_b, tot_ms = 0.0, 0.0
         cls = {}
         for q in range(4):
@@ -616,9 +620,8 @@ def run_gpu(args, w):
             "config": arm_config(w, args, world),
             "kernel_shape": {"tiles": list(sim_tiles), "zchunks": list(sim_z),
                              "pml_shell": "swept by the tile kernels" if fused else
-                             "own launches, %s" % ({0: "two points per thread for the stress y/z classes, one elsewhere",
-                                                    1: "one point per thread", 2: "two points per thread"}
-                                                   [args.pml_points])},
+                             "own launches, %s" % ({0: "one point per thread", 1: "one point per thread",
+                                                    2: "two points per thread"}[args.pml_points])},
             "timed_window": "it=%d..%d (graph replay; snapshot frame at it=%s)"
                             % (it - 2 * args.steps, it - args.steps - 1, ",".join(map(str, frames))),
             "hbm_fraction_step": {"bytes_per_step": step_bytes, "GBps": step_bytes / (ms_max / args.steps / 1e3) / 1e9,

@@ -79,8 +79,7 @@ typedef struct swpc_dims {
     int ntdec_r;         /* divergence-check interval (m_report.f90:134); 0 = off */
     int reserved[7];     /* 0 (all zero: library defaults); [0] 1 = interior kernels without TMA,
                             [1] 1/2 = PML kernels in series/beside the interior ones,
-                            [2] 1/2 = PML shell points per thread (0: two for the stress update
-                            of the y and z classes, one elsewhere),
+                            [2] 2 = two PML shell points per thread (0 or 1: one),
                             [3] 2 = the TMA tile kernels sweep the PML shell too (interior
                             kernels over the tiles inside the interior, shell-tile kernels over
                             the rest; 0 or 1: the shell in launches of its own) */

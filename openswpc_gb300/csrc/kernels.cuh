@@ -67,6 +67,7 @@ struct PmlBox {
     int pitch;           // ADE row pitch (= nx: rows stored without padding)
     int qs;              // stride between the box's nine auxiliary arrays (nx * ny * nz)
     long long off;       // offset of this box in the ADE buffers (elements)
+    long long moff;      // offset of the box's six medium arrays in the shell-medium buffer
 };
 
 // The PML shell swept by the TMA tile kernels together with the interior:
@@ -460,6 +461,7 @@ struct PArgs {
     float* adeV;        // axVx ayVy azVz ayVx azVx axVy azVy axVz ayVz
     float* adeS;        // axSxx aySxy azSxz axSxy aySyy azSyz axSxz aySyz azSzz
     const float* prof;  // gxc gxe (4 x nx each, l-major), gyc gye, gzc gze
+    const float* shm;   // shell medium per box [6][z][y][x]: mu_xz mu_xy mu_yz (harmonic means), bx by bz
     int pxc, pxe, pyc, pye, pzc, pze;  // offsets of each profile (array of 4*n, l fastest)
     PmlBox box[5];
     int nbox;
@@ -519,9 +521,21 @@ struct PmlSIn {
     int P, AP;
     float4 gxc, gxe, gyc, gye, gzc, gze;
     float vx, vy, vz, vxw, vys, vzu, vye, vze, vxn, vzn, vxd, vyd;
-    float lamv, m000, m100, m010, m110, m001, m011, m101;
+    float lamv, m000, muxz, muxy, muyz;
     float ad[9], sv[6];
 };
+// Harmonic mean of four moduli, 4 m1 m2 m3 m4 / (sum of the triple products
+// + eps) (m_absorb_p.f90:477-518), in explicitly rounded operations.
+__device__ __forceinline__ float pml_hmean(float m1, float m2, float m3, float m4) {
+    const float eps = 1.1920928955078125e-07f;
+    const float num = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(4.f, m1), m2), m3), m4);
+    const float m12 = __fmul_rn(m1, m2);
+    float den = __fmul_rn(m12, m3);
+    den = __fadd_rn(den, __fmul_rn(m12, m4));
+    den = __fadd_rn(den, __fmul_rn(__fmul_rn(m1, m3), m4));
+    den = __fadd_rn(den, __fmul_rn(__fmul_rn(m2, m3), m4));
+    return __fdiv_rn(num, __fadd_rn(den, eps));
+}
 // the auxiliaries of point L (its profiles and ADE address set)
 __device__ __forceinline__ void stress_pml_aux(PmlSIn& L) {
     const bool live[9] = {L.gxc.w != 0.f, L.gyc.w != 0.f, L.gzc.w != 0.f, L.gye.w != 0.f, L.gze.w != 0.f,
@@ -536,7 +550,6 @@ __device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, P
     const Geo& g = a.g;
     const int P = g.pitch;
     const long long rowV = 3LL * P, planeV = rowV * g.nyp;
-    const long long rowM = 5LL * P, planeM = rowM * g.nyp;
     const int ix = B.x0 + c.lx, jy = B.y0 + c.ly, kz = B.z0 + c.lz;
     const long long oV = (long long)goff(g, 3, 0, ix, jy, kz);
     const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
@@ -555,9 +568,10 @@ __device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, P
     L.vxw = V[-1]; L.vys = V[P - rowV]; L.vzu = V[2 * P - planeV];
     L.vye = V[P + 1]; L.vze = V[2 * P + 1]; L.vxn = V[rowV]; L.vzn = V[2 * P + rowV];
     L.vxd = V[planeV]; L.vyd = V[P + planeV];
-    L.lamv = M[P]; L.m000 = M[2 * P]; L.m100 = M[2 * P + planeM]; L.m010 = M[2 * P + 1];
-    L.m110 = M[2 * P + planeM + 1]; L.m001 = M[2 * P + rowM]; L.m011 = M[2 * P + rowM + 1];
-    L.m101 = M[2 * P + planeM + rowM];
+    L.lamv = M[P]; L.m000 = M[2 * P];
+    // the shear moduli at the edges, precomputed once per medium
+    const float* __restrict__ H = a.shm + B.moff + ((long long)c.lz * B.ny + c.ly) * B.pitch + c.lx;
+    L.muxz = H[0]; L.muxy = H[B.qs]; L.muyz = H[2LL * B.qs];
     // an auxiliary variable whose axis has no damping here (g4 = 0, the
     // point lies outside that axis's layer) starts at zero and its update
     // g3 * 0 + 0 keeps it zero: it is neither loaded nor stored.  Order:
@@ -571,7 +585,6 @@ __device__ __forceinline__ void stress_pml_load(const PArgs& a, const PmlPt c, P
 // tile kernels' shell arguments)
 template <class K>
 __device__ __forceinline__ void stress_pml_store(const K& a, const PmlSIn& L) {
-    const float eps = 1.1920928955078125e-07f;
     const int P = L.P, AP = L.AP;
     float* __restrict__ S = L.S;
     float* __restrict__ A = L.A;
@@ -609,19 +622,7 @@ __device__ __forceinline__ void stress_pml_store(const K& a, const PmlSIn& L) {
     const float dyVz = __fmul_rn(__fsub_rn(L.vzn, vz), a.r20y);
     const float dzVx = __fmul_rn(__fsub_rn(L.vxd, vx), a.r20z);
     const float dzVy = __fmul_rn(__fsub_rn(L.vyd, vy), a.r20z);
-    // harmonic mean of four moduli: 4 m1 m2 m3 m4 / (sum of the triple products + eps)
-    auto hmean = [eps](float m1, float m2, float m3, float m4) {
-        const float num = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(4.f, m1), m2), m3), m4);
-        const float m12 = __fmul_rn(m1, m2);
-        float den = __fmul_rn(m12, m3);
-        den = __fadd_rn(den, __fmul_rn(m12, m4));
-        den = __fadd_rn(den, __fmul_rn(__fmul_rn(m1, m3), m4));
-        den = __fadd_rn(den, __fmul_rn(__fmul_rn(m2, m3), m4));
-        return __fdiv_rn(num, __fadd_rn(den, eps));
-    };
-    const float muxz = hmean(L.m000, L.m100, L.m010, L.m110);
-    const float muxy = hmean(L.m000, L.m010, L.m001, L.m011);
-    const float muyz = hmean(L.m000, L.m100, L.m001, L.m101);
+    const float muxz = L.muxz, muxy = L.muxy, muyz = L.muyz;
     const float ayVx = ad[3], azVx = ad[4], axVy = ad[5], azVy = ad[6], axVz = ad[7], ayVz = ad[8];
     // (g1 d1 + g1' d2 + g2 a1 + g2' a2) in a fixed order
     auto sum4 = [](float4 p, float d1, float4 q, float d2, float a1, float a2) {
@@ -655,7 +656,7 @@ struct PmlVIn {
     int P, AP;
     float4 gxc, gxe, gyc, gye, gzc, gze;
     float sxx, syy, szz, syz, sxz, sxy, sxxe, syyn, szzd, syzs, syzu, sxzw, sxzu, sxyw, sxys;
-    float r0, rx, ry, rz;
+    float bx, by, bz;  // buoyancies 2 / (rho + rho') at the faces, precomputed once per medium
     float ad[9], v0, v1, v2;
 };
 __device__ __forceinline__ void vel_pml_aux(PmlVIn& L) {
@@ -671,14 +672,11 @@ __device__ __forceinline__ void vel_pml_load(const PArgs& a, const PmlPt c, PmlV
     const Geo& g = a.g;
     const int P = g.pitch;
     const long long rowS = 6LL * P, planeS = rowS * g.nyp;
-    const long long rowM = 5LL * P, planeM = rowM * g.nyp;
     const int ix = B.x0 + c.lx, jy = B.y0 + c.ly, kz = B.z0 + c.lz;
     const long long oV = (long long)goff(g, 3, 0, ix, jy, kz);
-    const long long oM = (long long)goff(g, 5, 0, ix, jy, kz);
     const long long oS = (long long)goff(g, 6, 0, ix, jy, kz);
     const long long oA = B.off + ((long long)c.lz * B.ny + c.ly) * B.pitch + c.lx;
     const float* __restrict__ S = a.S + oS;
-    const float* __restrict__ M = a.M + oM;
     L.V = a.V + oV;
     L.A = a.adeS + oA;
     L.P = P;
@@ -691,7 +689,8 @@ __device__ __forceinline__ void vel_pml_load(const PArgs& a, const PmlPt c, PmlV
     L.syzs = S[3 * P - rowS]; L.syzu = S[3 * P - planeS];
     L.sxzw = S[4 * P - 1]; L.sxzu = S[4 * P - planeS];
     L.sxyw = S[5 * P - 1]; L.sxys = S[5 * P - rowS];
-    L.r0 = M[0]; L.rx = M[1]; L.ry = M[rowM]; L.rz = M[planeM];
+    const float* __restrict__ H = a.shm + B.moff + ((long long)c.lz * B.ny + c.ly) * B.pitch + c.lx;
+    L.bx = H[3LL * B.qs]; L.by = H[4LL * B.qs]; L.bz = H[5LL * B.qs];
     // auxiliaries of undamped axes stay zero (as in the stress update).
     // Order: axSxx aySxy azSxz axSxy aySyy azSyz axSxz aySyz azSzz
     vel_pml_aux(L);
@@ -718,9 +717,7 @@ __device__ __forceinline__ void vel_pml_store(const K& a, const PmlVIn& L) {
     const float dzSxz = __fmul_rn(__fsub_rn(L.sxz, L.sxzu), a.r20z);
     const float dxSxy = __fmul_rn(__fsub_rn(L.sxy, L.sxyw), a.r20x);
     const float dySxy = __fmul_rn(__fsub_rn(L.sxy, L.sxys), a.r20y);
-    const float bx = __fdiv_rn(2.f, __fadd_rn(L.r0, L.rx));
-    const float by = __fdiv_rn(2.f, __fadd_rn(L.r0, L.ry));
-    const float bz = __fdiv_rn(2.f, __fadd_rn(L.r0, L.rz));
+    const float bx = L.bx, by = L.by, bz = L.bz;
     const float* ad = L.ad;
     const float axSxx = ad[0], aySxy = ad[1], azSxz = ad[2], axSxy = ad[3], aySyy = ad[4];
     const float azSyz = ad[5], axSxz = ad[6], aySyz = ad[7], azSzz = ad[8];
@@ -801,6 +798,34 @@ __device__ __forceinline__ void vel_pml_two(const PArgs& a, int b2, int t) {
     if (o1) vel_pml_store(a, L1);
 }
 
+// The shell's medium terms that the PML updates take from several cells --
+// the harmonic-mean shear moduli at the cell edges (m_absorb_p.f90:477-518)
+// and the buoyancies at the faces (m_absorb_p.f90:265-305) -- computed once
+// per medium with the operations the updates used, so that the updates give
+// the same bits: one thread per shell point of the whole boxes (a.part[] with
+// one part per box, as the general launch).
+__global__ void k_shell_medium(const PArgs a, float* __restrict__ shm) {
+    PmlPt c;
+    if (!pml_point(a, blockIdx.x, threadIdx.x, c)) return;
+    const PmlBox& B = a.box[c.b];
+    const Geo& g = a.g;
+    const int P = g.pitch;
+    const long long rowM = 5LL * P, planeM = rowM * g.nyp;
+    const int ix = B.x0 + c.lx, jy = B.y0 + c.ly, kz = B.z0 + c.lz;
+    const float* __restrict__ M = a.M + (long long)goff(g, 5, 0, ix, jy, kz);
+    const float m000 = M[2 * P], m100 = M[2 * P + planeM], m010 = M[2 * P + 1], m110 = M[2 * P + planeM + 1];
+    const float m001 = M[2 * P + rowM], m011 = M[2 * P + rowM + 1], m101 = M[2 * P + planeM + rowM];
+    const float r0 = M[0], rx = M[1], ry = M[rowM], rz = M[planeM];
+    float* H = shm + B.moff + ((long long)c.lz * B.ny + c.ly) * B.pitch + c.lx;
+    const long long q = B.qs;
+    H[0] = pml_hmean(m000, m100, m010, m110);
+    H[q] = pml_hmean(m000, m010, m001, m011);
+    H[2 * q] = pml_hmean(m000, m100, m001, m101);
+    H[3 * q] = __fdiv_rn(2.f, __fadd_rn(r0, rx));
+    H[4 * q] = __fdiv_rn(2.f, __fadd_rn(r0, ry));
+    H[5 * q] = __fdiv_rn(2.f, __fadd_rn(r0, rz));
+}
+
 // One thread per shell point.  MASK: the axes damped somewhere in the parts
 // of the launch (7 = any, checked per point).  With one damped axis the
 // kernels skip two thirds of the auxiliaries and profiles and fit 64
@@ -833,23 +858,6 @@ __global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml_batch(const
     const int2 e = blocks[blockIdx.x];
     PmlPt c;
     if (pml_point(all[e.x], e.y, threadIdx.x, c)) vel_pml_at<MASK>(all[e.x], c);
-}
-// batched, two shell points per thread: block b takes table entries 2b and
-// 2b + 1 (which may belong to different members)
-template <int MASK>
-__global__ void __launch_bounds__(PTPB, 5) k_stress_pml2_batch(const PArgs* __restrict__ all,
-                                                               const int2* __restrict__ blocks, int n) {
-    const int i0 = 2 * blockIdx.x, i1 = i0 + 1;
-    const int2 e0 = blocks[i0];
-    const int2 e1 = i1 < n ? blocks[i1] : e0;
-    PmlPt c0, c1;
-    const bool o0 = pml_point(all[e0.x], e0.y, threadIdx.x, c0);
-    const bool o1 = i1 < n && pml_point(all[e1.x], e1.y, threadIdx.x, c1);
-    PmlSIn L0, L1;
-    if (o0) stress_pml_load<MASK>(all[e0.x], c0, L0);
-    if (o1) stress_pml_load<MASK>(all[e1.x], c1, L1);
-    if (o0) stress_pml_store(all[e0.x], L0);
-    if (o1) stress_pml_store(all[e1.x], L1);
 }
 // the launch classes: x only, y only, z only, any
 constexpr int PML_NCLASS = 4;

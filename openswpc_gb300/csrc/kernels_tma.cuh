@@ -548,9 +548,10 @@ __device__ __forceinline__ bool stress_tma_tile(const TArgs& ta, const int bx, c
                 L.vxd = sm.V[sV[3]].d[ly][0][lx]; L.vyd = sm.V[sV[3]].d[ly][1][lx];
                 float (*M0)[4][36] = sm.M[sM0].d;
                 float (*M1)[4][36] = sm.M[sM1].d;
-                L.lamv = M0[ty][0][tx]; L.m000 = M0[ty][1][tx]; L.m100 = M1[ty][1][tx]; L.m010 = M0[ty][1][tx + 1];
-                L.m110 = M1[ty][1][tx + 1]; L.m001 = M0[ty + 1][1][tx]; L.m011 = M0[ty + 1][1][tx + 1];
-                L.m101 = M1[ty + 1][1][tx];
+                L.lamv = M0[ty][0][tx]; L.m000 = M0[ty][1][tx];
+                L.muxz = pml_hmean(L.m000, M1[ty][1][tx], M0[ty][1][tx + 1], M1[ty][1][tx + 1]);
+                L.muxy = pml_hmean(L.m000, M0[ty][1][tx + 1], M0[ty + 1][1][tx], M0[ty + 1][1][tx + 1]);
+                L.muyz = pml_hmean(L.m000, M1[ty][1][tx], M0[ty + 1][1][tx], M1[ty + 1][1][tx]);
 #pragma unroll
                 for (int q = 0; q < 6; ++q) L.sv[q] = sm.S[sRS].d[ty][q][tx];
                 cp_async_wait_all();

@@ -18,7 +18,7 @@ struct Plan {
     bool pml;
     int x0, y0, nxi, nyi, nzi;  // viscoelastic interior box
     int rpitch, rbytes;
-    long long nV, nS, nM, nR, nade, npml, bytes;
+    long long nV, nS, nM, nR, nade, nshm, npml, bytes;
     PmlBox box[5];
     int nbox;
 };
@@ -40,6 +40,7 @@ struct Sim {
     void* R = nullptr;
     int4* band = nullptr;
     float *adeV = nullptr, *adeS = nullptr;
+    float* shm = nullptr;  // the shell's precomputed medium terms (k_shell_medium)
     float* cer = nullptr;
     int cer_off[6] = {0, 0, 0, 0, 0, 0};
     int* d_it = nullptr;
@@ -51,7 +52,7 @@ struct Sim {
     int kchunk_v = 1, kchunk_v_auto = 1;  // and of the velocity kernels
     int variant = 0;        // 0: TMA-fed interior kernels, 1: shared-memory sweep without TMA
     int ty_s = TTY, ty_v = TTY;  // tile rows of the stress and velocity TMA kernels (8 or 16)
-    int pml_np = 0;              // shell points per thread of the PML kernels (1, 2; 0: by launch class)
+    int pml_np = 0;              // shell points per thread of the PML kernels (2; 0 or 1: one)
     bool pml_fused = false;      // the TMA tile kernels sweep the PML shell (interior and shell-tile kernels)
     int shell_dlo[6] = {}, shell_dhi[6] = {};  // damped index runs of the six profiles (PmlShell::dlo, dhi)
     TArgs targs;            // tensor maps of the TMA kernels (64-byte aligned)

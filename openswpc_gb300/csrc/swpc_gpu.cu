@@ -70,6 +70,7 @@ static int plan(const swpc_dims* d, Plan& p) {
     // PML shell boxes
     p.nbox = 0;
     p.nade = 0;
+    p.nshm = 0;
     long long first = 0;
     if (p.pml) {
         const int na = d->na, nx = d->nx, ny = d->ny, nz = d->nz;
@@ -85,11 +86,13 @@ static int plan(const swpc_dims* d, Plan& p) {
             B.qs = (int)vol;
             B.off = p.nade;
             p.nade += 9LL * B.pitch * B.ny * B.nz;
+            B.moff = p.nshm;
+            p.nshm += 6LL * B.pitch * B.ny * B.nz;
             first += (long long)B.nx * B.ny * B.nz;
         }
     }
     p.npml = first;
-    p.bytes = 4 * (p.nV + p.nS + p.nM) + p.rbytes * p.nR + 4 * 2 * p.nade + 16LL * p.nxi * p.nyi;
+    p.bytes = 4 * (p.nV + p.nS + p.nM) + p.rbytes * p.nR + 4 * (2 * p.nade + p.nshm) + 16LL * p.nxi * p.nyi;
     return 0;
 }
 
@@ -176,12 +179,12 @@ void Sim::launch_pml(bool stress, cudaStream_t st, bool timed) {
         pending.push_back(pe);
     };
     // one launch of a class: one or two shell points per thread.  By
-    // default the stress update of the y and z classes takes two (their
-    // loads are whole rows; 0.376 -> 0.340 and 0.358 -> 0.341 ms on the
-    // 1024x1024x512 grid), every other launch one (two were slower there:
-    // corners 0.143 -> 0.165 ms, velocity classes up to 0.115 -> 0.146 ms)
+    // default one: with the shell's edge moduli and buoyancies precomputed,
+    // two points per thread are no faster for any class on the
+    // 1024x1024x512 grid (stress y 0.320 -> 0.328 ms, z 0.327 -> 0.331 ms,
+    // corners 0.129 -> 0.146 ms, velocity y 0.263 -> 0.274 ms)
     auto go = [&](int mask, const PArgs& a) {
-        const bool two = pml_np == 2 || (pml_np == 0 && stress && (mask == 2 || mask == 4));
+        const bool two = pml_np == 2;
         if (two) {
             const unsigned nb = (unsigned)((a.nblocks + 1) / 2);
             switch (mask) {
@@ -1064,6 +1067,7 @@ int Sim::allocate() {
         };
         const size_t oV = carve(p.nV * 4), oS = carve(p.nS * 4), oM = carve(p.nM * 4), oR = carve(p.nR * p.rbytes);
         const size_t oAV = p.pml ? carve(p.nade * 4) : 0, oAS = p.pml ? carve(p.nade * 4) : 0;
+        const size_t oSH = p.pml ? carve(p.nshm * 4) : 0;
         char* arena = nullptr;
         if ((rc = dalloc((void**)&arena, off))) return rc;
         V = reinterpret_cast<float*>(arena + oV);
@@ -1073,6 +1077,7 @@ int Sim::allocate() {
         if (p.pml) {
             adeV = reinterpret_cast<float*>(arena + oAV);
             adeS = reinterpret_cast<float*>(arena + oAS);
+            shm = reinterpret_cast<float*>(arena + oSH);
         }
     }
     if ((rc = dalloc((void**)&band, 16 * (size_t)p.nxi * p.nyi))) return rc;
@@ -1092,7 +1097,7 @@ int Sim::allocate() {
     device = dev;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     variant = dims.reserved[0] == 1 ? 1 : 0;
-    pml_np = dims.reserved[2] == 2 ? 2 : dims.reserved[2] == 1 ? 1 : 0;  // 0: per launch class
+    pml_np = dims.reserved[2] == 2 ? 2 : 1;
     // reserved[3] = 2: the TMA tile kernels sweep the PML shell too (interior
     // and shell-tile kernels); otherwise the shell runs in launches of its own
     pml_fused = p.pml && variant == 0 && p.nbox == 5 && dims.reserved[3] == 2;
@@ -1431,13 +1436,19 @@ int Sim::finish_medium(const double* ts) {
         int rc = dalloc((void**)&dp, prof.size() * 4);
         if (rc) return rc;
         CK(cudaMemcpyAsync(dp, prof.data(), prof.size() * 4, cudaMemcpyHostToDevice, stream));
-        a.g = g; a.V = V; a.S = S; a.M = M; a.adeV = adeV; a.adeS = adeS; a.prof = dp;
+        a.g = g; a.V = V; a.S = S; a.M = M; a.adeV = adeV; a.adeS = adeS; a.prof = dp; a.shm = shm;
         a.nbox = p.nbox;
         for (int b = 0; b < p.nbox; ++b) a.box[b] = p.box[b];
         a.npart = 0;
         a.nblocks = 0;
         a.r20x = (float)(1.0 / dx); a.r20y = (float)(1.0 / dy); a.r20z = (float)(1.0 / dz); a.dt = (float)dt;
         plan_pml_parts(prof);
+        // the shell's harmonic means and buoyancies, once per medium
+        if (pml_all.nblocks) {
+            k_shell_medium<<<pml_all.nblocks, PTPB, 0, stream>>>(pml_all, shm);
+            ++launches;
+            CK(cudaGetLastError());
+        }
     } else {
         std::vector<float> c, b, all;
         int n[3] = {g.nx, g.ny, g.nz};
@@ -1804,15 +1815,6 @@ struct Batch {
             const unsigned nb = (unsigned)n_pblocks[q];
             const PArgs* a = d_pargs[q];
             const int2* t = d_pblocks[q];
-            // the stress update of the y and z classes takes two points per
-            // thread, as in the single-simulation launches
-            if (stress && (PML_CLASS_MASK[q] == 2 || PML_CLASS_MASK[q] == 4)) {
-                const unsigned nb2 = (nb + 1) / 2;
-                if (PML_CLASS_MASK[q] == 2) k_stress_pml2_batch<2><<<nb2, PTPB, 0, stream2>>>(a, t, (int)nb);
-                else k_stress_pml2_batch<4><<<nb2, PTPB, 0, stream2>>>(a, t, (int)nb);
-                ++launches;
-                continue;
-            }
             switch (PML_CLASS_MASK[q]) {
             case 1: stress ? k_stress_pml_batch<1><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<1><<<nb, PTPB, 0, stream2>>>(a, t); break;
             case 2: stress ? k_stress_pml_batch<2><<<nb, PTPB, 0, stream2>>>(a, t) : k_vel_pml_batch<2><<<nb, PTPB, 0, stream2>>>(a, t); break;

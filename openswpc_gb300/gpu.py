@@ -197,8 +197,8 @@ def make_dims(nx, ny, nz, nt, dx, dy, dz, dt, na=20, abc="pml", store="fp32", xb
     runs the shell in launches of its own, where the next two options apply;
     concurrent runs the PML shell kernels beside the interior kernels on a
     second stream (True/False; None lets the library choose by grid size);
-    pml_points: shell points per thread of the PML kernels (1 or 2; 0 lets
-    the library choose per launch class)."""
+    pml_points: shell points per thread of the PML kernels (2, or 0/1 for
+    the library default of one)."""
     d = Dims()
     d.nx, d.ny, d.nz, d.nt, d.na, d.nm = nx, ny, nz, nt, na, 3
     d.abc_type = 0 if abc == "pml" else 1
