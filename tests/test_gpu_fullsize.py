@@ -1,0 +1,75 @@
+"""Size-independent properties on the full 1024 x 1024 x 512 workload, whose
+fields are too large for the CPU oracle: the large single-source medium (a
+1-D gradient times a 5 % von Karman field, built on the device), a double-
+couple source 2 km deep (so that the wave reaches the surface within the
+run) and 64 surface receivers around the epicentre.
+
+* Linearity: the time loop is linear in the source (m_kernel.f90:75-348,
+  m_absorb_p.f90:246-531, the stress-glut injection of m_source.f90:776-848),
+  and doubling is exact in binary floating point, so a source moment twice
+  as large gives traces exactly twice as large, bit for bit, after any
+  number of steps.
+* The graph-replayed run equals the same steps launched one by one, bit for
+  bit.
+* The run stays finite and its maximum |V| at the ocean bottom grows from zero
+  as the wave reaches the surface.
+"""
+import numpy as np
+import pytest
+
+from openswpc_gb300 import configs, gpu
+
+NX, NY, NZ, DX, DT, NA = 1024, 1024, 512, 0.25, 0.01, 20
+NT = 64
+
+
+def _sim(mo, seed=20261203, ntdec_r=0):
+    zbeg = -3 * DX
+    d = gpu.make_dims(NX, NY, NZ, NT, DX, DX, DX, DT, na=NA, xbeg=-NX * DX / 2, ybeg=-NY * DX / 2, zbeg=zbeg,
+                      fcut=1.0, M0=1e16, UC=1e-15, ntdec_r=ntdec_r)
+    s = gpu.Simulation(d)
+    bg, xi, kxi0 = configs.gradient_random_fields(NX, NY, NZ, DX, zbeg, seed=seed)
+    maps, _ = s.build_medium_rmed(bg, xi, kxi0, fq_min=0.05, fq_max=5.0, fq_ref=1.0)
+    kfs = maps[0]
+    ks = int(np.ceil((2.0 - zbeg) / DX))
+    s.set_sources(np.array([[NX // 2, NY // 2, ks]], np.int32), np.array([[0.0, 0.4]]), mo=np.array([mo]),
+                  mij=np.array([[0.3, -0.5, 0.2, 0.6, -0.4, 0.7]]), stftype="kupper")
+    # 64 receivers on an 8 x 8 lattice around the epicentre (2 km apart), one
+    # cell below the free surface
+    ii, jj = np.meshgrid(NX // 2 + 8 * np.arange(-4, 4), NY // 2 + 8 * np.arange(-4, 4), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()
+    kk = kfs[jj + 2, ii + 2] + 1
+    s.set_receivers(np.stack([ii, jj, kk], 1).astype(np.int32), ntdec_w=1, flags=gpu.SWPC_WAV_V)
+    return s
+
+
+@pytest.mark.gpu
+def test_full_size_linearity_and_graph_replay():
+    a, b = _sim(1.0), _sim(2.0)
+    a.run(1, NT)
+    # the doubled source stepped one launch at a time (profiling switches the
+    # graph replay off), the single one graph-replayed
+    b.profile(True)
+    b.run(1, NT)
+    b.profile(False)
+    wa, wb = a.waveforms(), b.waveforms()
+    assert np.all(np.isfinite(wa)) and np.abs(wa).max() > 0
+    assert np.array_equal(wb, 2.0 * wa)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_full_size_vmax_finite_and_growing():
+    """max |V| at the ocean bottom every 8 steps (kernel__vmax,
+    m_kernel.f90:350-374) is finite, zero before the wave reaches the
+    surface, and positive once it has."""
+    s = _sim(1.0, ntdec_r=8)
+    got = []
+    for q in range(NT // 8):
+        s.run(q * 8 + 1, (q + 1) * 8)
+        got.append(np.asarray(s.vmax(), np.float64).max())
+    s.close()
+    got = np.array(got)
+    assert np.all(np.isfinite(got)) and got[-1] > 0
+    assert got[0] < got[-1]
