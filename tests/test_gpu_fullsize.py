@@ -6,9 +6,12 @@ run) and 64 surface receivers around the epicentre.
 
 * Linearity: the time loop is linear in the source (m_kernel.f90:75-348,
   m_absorb_p.f90:246-531, the stress-glut injection of m_source.f90:776-848),
-  and doubling is exact in binary floating point, so a source moment twice
-  as large gives traces exactly twice as large, bit for bit, after any
-  number of steps.
+  and doubling commutes with rounding in binary floating point, so a source
+  moment twice as large gives traces exactly twice as large, bit for bit,
+  after any number of steps -- except where a value falls below the normal
+  range (about 1e-38), whose fixed spacing doubling does not preserve: the
+  precursors far ahead of the wave front.  There the difference stays at
+  that absolute size.
 * The graph-replayed run equals the same steps launched one by one, bit for
   bit.
 * The run stays finite and its maximum |V| at the ocean bottom grows from zero
@@ -54,7 +57,10 @@ def test_full_size_linearity_and_graph_replay():
     b.profile(False)
     wa, wb = a.waveforms(), b.waveforms()
     assert np.all(np.isfinite(wa)) and np.abs(wa).max() > 0
-    assert np.array_equal(wb, 2.0 * wa)
+    normal = np.abs(wa) > 2.0 ** -100
+    assert normal.sum() > wa.size // 10
+    assert np.array_equal(wb[normal], 2.0 * wa[normal])
+    assert np.abs(wb - 2.0 * wa).max() <= 2.0 ** -90
     a.close()
     b.close()
 
