@@ -134,7 +134,8 @@ template <class RT, int TY, bool SHELL> struct StressSm : StressSmem<RT, TY> {};
 template <class RT, int TY> struct StressSm<RT, TY, true> : StressSmem<RT, TY> { AuxStage<TY> aux; };
 template <int TY, bool SHELL> struct VelSm : VelSmem<TY> {};
 template <int TY> struct VelSm<TY, true> : VelSmem<TY> { AuxStage<TY> aux; };
-// blocks per SM of the shell-tile kernels (8-row tiles; 16-row tiles one)
+// blocks per SM of the shell-tile kernels (8-row tiles two; 12- and 16-row
+// tiles one)
 template <int TY> struct ShellOcc { static constexpr int stress = 2, vel = 2; };
 template <> struct ShellOcc<16> { static constexpr int stress = 1, vel = 1; };
 template <> struct ShellOcc<12> { static constexpr int stress = 1, vel = 1; };
