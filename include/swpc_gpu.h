@@ -279,8 +279,8 @@ int swpc_gpu_get_dims(swpc_sim* sim, swpc_dims* out);
 int swpc_gpu_reset(swpc_sim* sim);
 
 /* z-sweep depth (planes per block) of the interior stress and velocity
- * kernels; 0 restores the automatic choice (at most 8 planes for the stress
- * kernel with FP32 memory variables, 32 with 16-bit ones, 128 for the
+ * kernels; 0 restores the automatic choice (at most 6 planes for the stress
+ * kernel with FP32 memory variables, 32 with 16-bit ones, 96 for the
  * velocity kernel, fewer when the grid is too small to fill the GPU).  The autotuner (openswpc_gb300/autotune.py) sets them.
  * set_zchunk sets both to one depth; get_zchunk returns the stress depth. */
 int swpc_gpu_set_zchunks(swpc_sim* sim, int kstress, int kvel);

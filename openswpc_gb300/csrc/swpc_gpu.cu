@@ -1085,13 +1085,15 @@ int Sim::allocate() {
     if ((rc = dalloc((void**)&d_kob, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     if ((rc = dalloc((void**)&d_kfs, 4 * (size_t)p.g.nx * p.g.ny))) return rc;
     // z chunking: enough blocks to fill the GPU at least ~8 times; then the
-    // stress kernels take chunks of at most 8 planes with FP32 memory
+    // stress kernels take chunks of at most 6 planes with FP32 memory
     // variables, 32 with 16-bit ones (neighbouring blocks sweep the same
     // planes at the same time and share their V halo rows in L2:
-    // 1024x1024x512 FP32 stress 17.6, 16.2, 16.0 ms with 492, 16, 8 planes;
-    // FP16 12.18, 11.57, 11.35 ms with 8, 16, 32 planes) and
-    // the velocity kernels chunks of at most 128 planes (its longer start-up
-    // costs more: 4.67 ms at 492, 4.54 at 123, 4.95 at 16 planes)
+    // 1024x1024x512 FP32 stress 15.91, 15.64, 15.44, 15.52, 15.65, 15.77 ms
+    // with 4, 5, 6, 8, 10, 12 planes in the grouped block order (17.6 ms with
+    // 492 in the plain order); FP16 12.18, 11.57, 11.35 ms with 8, 16, 32
+    // planes) and the velocity kernels chunks of at most 96 planes (its
+    // longer start-up costs more at 16 planes, 4.95 ms; 4.27 ms at 123,
+    // 4.256 at 99 and 82, 4.254 at 70)
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
     device = dev;
@@ -1110,8 +1112,8 @@ int Sim::allocate() {
         const int nc = (nzs + cap - 1) / cap;
         return (nzs + nc - 1) / nc;
     };
-    kchunk = kchunk_auto = even(std::min(kfill, p.rbytes == 4 ? 8 : 32));
-    kchunk_v = kchunk_v_auto = even(std::min(kfill, 128));
+    kchunk = kchunk_auto = even(std::min(kfill, p.rbytes == 4 ? 6 : 32));
+    kchunk_v = kchunk_v_auto = even(std::min(kfill, 96));
     graph_steps = 8;
     if ((rc = dalloc((void**)&d_err, 16))) return rc;
     // PML shell beside the interior: pays off only when the interior launch
