@@ -433,11 +433,16 @@ int tile_kernel_attributes();
 
 // 4-D map (x, field, y, z) over a row-interleaved group
 static int make_map(CUtensorMap* m, void* base, CUtensorMapDataType dt, int es, long long nx, int nf, long long ny,
-                    long long nz, int bx, int bf, int by) {
-    // L2 fetch granularity: each box row is one 128-byte line (FP32) or half
-    // of one (16-bit); promoting to 256 bytes would double the DRAM reads of
-    // rows whose neighbour tile is not read at the same time
-    const CUtensorMapL2promotion promo = bx * es >= 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B : CU_TENSOR_MAP_L2_PROMOTION_NONE;
+                    long long nz, int bx, int bf, int by, bool wide = false) {
+    // L2 fetch granularity: each FP32 box row is one 128-byte line (a
+    // 16-bit row half of one).  The stress kernel's maps promote to 256
+    // bytes (wide): its grouped block order keeps the x-neighbour tile,
+    // which reads the other half, resident at the same time (1024x1024x512:
+    // 15.44 -> 15.39 ms); the velocity kernel's stay at 128 (256: 4.26 ->
+    // 4.27 ms; 64: 4.32 ms)
+    const CUtensorMapL2promotion promo = bx * es >= 128 ? (wide ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B
+                                                               : CU_TENSOR_MAP_L2_PROMOTION_L2_128B)
+                                                        : CU_TENSOR_MAP_L2_PROMOTION_NONE;
     EncodeTiledFn fn = encode_fn();
     if (!fn) return set_err(SWPC_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     cuuint64_t dims[4] = {(cuuint64_t)nx, (cuuint64_t)nf, (cuuint64_t)ny, (cuuint64_t)nz};
@@ -455,16 +460,16 @@ int Sim::build_tensor_maps() {
     const CUtensorMapDataType F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     int rc;
     const int ts_ = ty_s, tv_ = ty_v;
-    if ((rc = make_map(&targs.tmV, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 40, 3, ts_ + 4))) return rc;
-    if ((rc = make_map(&targs.tmS, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 32, 6, ts_))) return rc;
-    if ((rc = make_map(&targs.tmM, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 4, ts_ + 1))) return rc;
+    if ((rc = make_map(&targs.tmV, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 40, 3, ts_ + 4, true))) return rc;
+    if ((rc = make_map(&targs.tmS, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 32, 6, ts_, true))) return rc;
+    if ((rc = make_map(&targs.tmM, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 4, ts_ + 1, true))) return rc;
     if ((rc = make_map(&targs.tmSh, S, F, 4, g.pitch, 6, g.nyp, g.nzp, 40, 6, tv_ + 4))) return rc;
     if ((rc = make_map(&targs.tmRho, M, F, 4, g.pitch, 5, g.nyp, g.nzp, 36, 1, tv_ + 1))) return rc;
     if ((rc = make_map(&targs.tmVc, V, F, 4, g.pitch, 3, g.nyp, g.nzp, 32, 3, tv_))) return rc;
     const CUtensorMapDataType RTy = dims.store == SWPC_STORE_FP32 ? F
                                     : dims.store == SWPC_STORE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                                     : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-    if ((rc = make_map(&targs.tmR, R, RTy, p.rbytes, p.rpitch, 18, p.nyi, p.nzi, 32, 18, ts_))) return rc;
+    if ((rc = make_map(&targs.tmR, R, RTy, p.rbytes, p.rpitch, 18, p.nyi, p.nzi, 32, 18, ts_, true))) return rc;
     targs.err = d_err;
     if (ts_ == 16) smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float, 16>) : sizeof(StressSmem<__half, 16>);
     else smem_stress = p.rbytes == 4 ? sizeof(StressSmem<float>) : sizeof(StressSmem<__half>);
