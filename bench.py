@@ -672,7 +672,7 @@ def member_bytes(nx, ny, nz, na=20):
     return B_INT * n_int + B_PML * (nx * ny * nz - n_int)
 
 
-def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500):
+def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500, tiles=None, zchunks=None):
     """n simulations of the batched workload advanced together (swpc_batch)
     versus the same simulations one after another on the plain path; both
     timed with CUDA events over `steps` steps and scaled to nt_full steps
@@ -688,6 +688,11 @@ def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500):
         pts = [int(np.prod(s)) for s in sizes]
         step_bytes = float(sum(member_bytes(*map(int, s)) for s in sizes))
         rec, t_tune = None, 0.0
+        for s in sims:
+            if tiles:
+                s.set_tiles(*tiles)
+            if zchunks:
+                s.set_zchunks(*zchunks)
         if tune:
             t0 = time.time()
             rec = autotune.tune(sims)
@@ -707,9 +712,8 @@ def batch_measure(nsim, steps, warmup, tune=True, seed=20261203, nt_full=1500):
         items = b.item_count()
         # the same batch as one persistent fused launch per step (8-row tiles)
         ms_persist = None
-        for s in sims:
-            tiles = s.tiles()
-        if tiles == (8, 8):
+        shape = sims[-1].tiles()
+        if shape == (8, 8):
             b.set_persistent(True)
             b.run(warmup)
             b.sync()
@@ -766,7 +770,9 @@ def batch_block(args):
 def run_batch(args):
     """Batched form: solves/s of n simulations advanced together versus the
     same simulations run one after another on the plain path."""
-    r = batch_measure(args.nsim, args.steps, args.warmup)
+    r = batch_measure(args.nsim, args.steps, args.warmup, tune=not args.no_tune,
+                      tiles=[int(v) for v in args.tiles.split(",")] if args.tiles else None,
+                      zchunks=[int(v) for v in args.zchunks.split(",")] if args.zchunks else None)
     line = {"metric": "batched solves/s", "value": r["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -1010,6 +1016,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the short batched block of the default run")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="batch workload: no autotuning (the members take --tiles/--zchunks or the library's choice)")
     ap.add_argument("--tiles", default="", help="rows of the stress and velocity tiles, e.g. 16,8 (default: 8,8)")
     ap.add_argument("--zchunks", default="", help="z-sweep depths of the stress and velocity kernels, e.g. 8,128")
     ap.add_argument("--pml-points", type=int, default=0, choices=[0, 1, 2],
