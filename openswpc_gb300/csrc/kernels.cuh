@@ -829,15 +829,17 @@ __global__ void k_shell_medium(const PArgs a, float* __restrict__ shm) {
 // One thread per shell point.  MASK: the axes damped somewhere in the parts
 // of the launch (7 = any, checked per point).  With one damped axis the
 // kernels skip two thirds of the auxiliaries and profiles and fit 64
-// registers without spilling (8 blocks per SM); the general stress kernel
-// fits 72 (7 blocks), the general velocity kernel needs 94.
+// registers without spilling (8 blocks per SM); the general kernels fit 72
+// (7 blocks; the general velocity kernel, which took 85 registers and 6
+// blocks unbounded, runs its corners 12 % faster so: 0.121 -> 0.106 ms on
+// the 1024x1024x512 grid, the 64-member batch step 17.63 -> 17.37 ms).
 template <int MASK>
 __global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_stress_pml(const PArgs a) {
     PmlPt c;
     if (pml_point(a, blockIdx.x, threadIdx.x, c)) stress_pml_at<MASK>(a, c);
 }
 template <int MASK>
-__global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml(const PArgs a) {
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_vel_pml(const PArgs a) {
     PmlPt c;
     if (pml_point(a, blockIdx.x, threadIdx.x, c)) vel_pml_at<MASK>(a, c);
 }
@@ -854,7 +856,7 @@ __global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_stress_pml_batch(co
     if (pml_point(all[e.x], e.y, threadIdx.x, c)) stress_pml_at<MASK>(all[e.x], c);
 }
 template <int MASK>
-__global__ void __launch_bounds__(PTPB, MASK == 7 ? 1 : 8) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
+__global__ void __launch_bounds__(PTPB, MASK == 7 ? 7 : 8) k_vel_pml_batch(const PArgs* __restrict__ all, const int2* __restrict__ blocks) {
     const int2 e = blocks[blockIdx.x];
     PmlPt c;
     if (pml_point(all[e.x], e.y, threadIdx.x, c)) vel_pml_at<MASK>(all[e.x], c);
